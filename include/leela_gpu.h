@@ -1,0 +1,147 @@
+/*
+ * leela_gpu.h -- C ABI of the GB300 evaluation path for Leela's policy and
+ * value networks.
+ *
+ * The host side of the engine (its Network class, Network.h:23-88) calls
+ * these functions in place of its BLAS / OpenCL backends.  No C++ exception
+ * and no CUDA or torch type crosses this boundary: plain pointers and sizes
+ * in, an int status out (0 = ok, < 0 = error; lg_last_error() gives the
+ * message for the calling thread).
+ *
+ * Board geometry is fixed at 19x19 (Network.cpp:352-355).  Input planes are
+ * bytes holding 0 or 1, [B][c_in][361], point index y*19+x, already rotated
+ * by the caller as Network.cpp:765-773 does.
+ */
+#ifndef LEELA_GPU_H
+#define LEELA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define LG_API __attribute__((visibility("default")))
+#else
+#define LG_API
+#endif
+
+#define LG_OK 0
+#define LG_ERR_ARG -1      /* bad argument or unsupported shape */
+#define LG_ERR_ALLOC -2    /* device or host allocation failed */
+#define LG_ERR_CUDA -3     /* CUDA runtime error */
+#define LG_ERR_TIMEOUT -4  /* a bounded wait ran out */
+#define LG_ERR_DEVICE -5   /* a kernel reported an error status */
+
+#define LG_FP32 0 /* plain FP32: the drop-in path */
+#define LG_BF16 1 /* BF16 activations and weights, FP32 accumulate (tcgen05) */
+#define LG_FP8W 2 /* E4M3 weights with per-output-channel FP32 scales, BF16 activations */
+
+#define LG_ACT_ELU 0  /* x > 0 ? x : exp(x) - 1 (Network.cpp:382-383) */
+#define LG_ACT_RELU 1
+
+#define LG_NET_POLICY 0
+#define LG_NET_VALUE 1
+
+/* Network shape and weights.  Conv layers in order: 5x5 c_in -> width1;
+ * n3x3 layers 3x3 (width1 ->) width -> width; head head_k x head_k width -> 1.
+ * `act` follows every conv but the head, and the head too if act_head.
+ * Value nets (value_head = 1) add FC 361 -> fc_hidden (+act) and FC
+ * fc_hidden -> 1, then tanh (value_map 0) or (1 + tanh) / 2 (value_map 1,
+ * Network.cpp:735-737).
+ *
+ * weights: one flat FP32 array, per conv W[O][C][k][k] then b[O] (the
+ * reference's OIHW arrays conv1_w, conv1_b, ... in order,
+ * Network.cpp:54-137), then for value nets W1[fc_hidden][361], b1, W2, b2.
+ * The library copies what it needs; the caller keeps ownership.
+ *
+ * LG_BF16 / LG_FP8W need c_in <= 32, width1 == width, width in {64, 128}
+ * and head_k == 1. */
+typedef struct lg_net_desc {
+    int c_in;
+    int width1;
+    int width;
+    int n3x3;
+    int head_k;
+    int act;
+    int act_head;
+    int value_head;
+    int fc_hidden;
+    int value_map;
+    int precision;
+    const float *weights;
+} lg_net_desc;
+
+typedef struct lg_ctx lg_ctx;
+
+/* Number of floats in the flat weight array of `desc`. */
+LG_API size_t lg_weight_count(const lg_net_desc *desc);
+
+/* Uploads the nets (either may be NULL) to `device` and sizes every buffer
+ * for up to max_batch positions per call.
+ * Replaces: Network::initialize (Network.cpp:201-235), i.e.
+ * OpenCL_Network::push_convolve / push_innerproduct (OpenCL.h:66-87,
+ * OpenCL.cpp:579-744) and the device pick in OpenCL::initialize
+ * (OpenCL.cpp:764-908). */
+LG_API int lg_create(const lg_net_desc *policy, const lg_net_desc *value, int device, int max_batch,
+              lg_ctx **out);
+
+/* Frees every resource of the context.  No reference counterpart (the
+ * reference keeps its nets for the life of the process). */
+LG_API void lg_destroy(lg_ctx *ctx);
+
+/* Message of the last failed call on this thread ("" if none).
+ * Replaces: cl::Error / std::runtime_error (OpenCL.cpp:665-669, 848-850). */
+LG_API const char *lg_last_error(void);
+
+/* Policy net over B positions, blocking.  probs [B][361] = softmax of the
+ * head output at `temperature`, network order (the caller un-rotates with
+ * rev_rotate_nn_idx and filters EMPTY points, Network.cpp:820-829);
+ * logits [B][361] (optional, may be NULL) = the head output before the
+ * softmax.  Host buffers.
+ * Replaces: the forward + softmax of Network::get_scored_moves_internal
+ * (Network.cpp:742-832), OpenCL_Network::forward (OpenCL.cpp:490-569) and
+ * Network::softmax (Network.cpp:450-469). */
+LG_API int lg_policy(lg_ctx *ctx, const uint8_t *planes, int B, float temperature, float *probs,
+              float *logits);
+
+/* Value net over B positions, blocking; value [B].  Host buffers.
+ * Replaces: Network::get_value_internal (Network.cpp:676-740). */
+LG_API int lg_value(lg_ctx *ctx, const uint8_t *planes, int B, float *value);
+
+/* Device-resident variants: every pointer is device memory and the work is
+ * enqueued on `stream` (a cudaStream_t, NULL = the legacy default stream);
+ * the call returns without waiting.  B may exceed max_batch. */
+LG_API int lg_policy_device(lg_ctx *ctx, const uint8_t *planes, int B, float temperature, float *probs,
+                     float *logits, void *stream);
+LG_API int lg_value_device(lg_ctx *ctx, const uint8_t *planes, int B, float *value, void *stream);
+
+/* Batching server.  lg_submit queues B positions for net LG_NET_POLICY or
+ * LG_NET_VALUE and returns at once; `out` (host, [B][361] probabilities at
+ * `temperature` or [B] values) is filled before `tag` is reported by
+ * lg_poll.  A worker thread gathers queued requests into batches of up to
+ * max_batch, pads each batch to a power-of-two bucket and replays the CUDA
+ * graph captured for that bucket.  lg_poll copies up to `max` completed tags
+ * and returns how many, waiting at most timeout_us microseconds (0 = do not
+ * wait).
+ * Replaces: Network::async_scored_moves + forward_cb (Network.cpp:484-587)
+ * and OpenCL::thread_can_issue / callback_finished / join_outstanding_cb
+ * (OpenCL.cpp:446-577), whose final wait is unbounded; this one is bounded. */
+LG_API int lg_submit(lg_ctx *ctx, int net, const uint8_t *planes, int B, float temperature, float *out,
+              void *tag);
+LG_API int lg_poll(lg_ctx *ctx, void **tags, int max, int timeout_us);
+
+/* Counters of the context: kernel launches issued so far (graph replays
+ * count their kernels), and batches served by the batching server. */
+LG_API int lg_stats(lg_ctx *ctx, long long *kernel_launches, long long *batches);
+
+/* Test hook (host-side fault injection): the n-th device call from now
+ * (n >= 1) fails with LG_ERR_CUDA before it reaches the GPU; 0 disarms. */
+LG_API int lg_inject_fault(lg_ctx *ctx, int nth_call);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

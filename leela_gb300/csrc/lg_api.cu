@@ -1,0 +1,815 @@
+// lg_api.cu -- the C ABI (include/leela_gpu.h): contexts, weight upload and
+// layout, forward orchestration, CUDA-graph cache, batching server.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "lg_kernels.h"
+
+// ------------------------------------------------------------------ errors
+
+static thread_local std::string t_last_error;
+
+void lg_set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    t_last_error = buf;
+}
+
+extern "C" const char *lg_last_error(void) { return t_last_error.c_str(); }
+
+namespace {
+
+using namespace lg;
+
+constexpr int kMaxConv = 40;
+
+// ------------------------------------------------------------ shapes
+
+struct Shape {
+    int k, cin, cout;
+};
+
+bool valid_desc(const lg_net_desc *d) {
+    return d && d->c_in > 0 && d->c_in <= 64 && d->width1 > 0 && d->width > 0 && d->n3x3 >= 0 &&
+           d->n3x3 < kMaxConv - 2 && (d->head_k == 1 || d->head_k == 3) &&
+           (d->act == LG_ACT_ELU || d->act == LG_ACT_RELU) &&
+           (!d->value_head || (d->fc_hidden > 0 && d->fc_hidden <= 4096)) &&
+           d->precision >= LG_FP32 && d->precision <= LG_FP8W;
+}
+
+std::vector<Shape> conv_shapes(const lg_net_desc *d) {
+    std::vector<Shape> s;
+    s.push_back({5, d->c_in, d->width1});
+    for (int i = 0; i < d->n3x3; ++i) s.push_back({3, i == 0 ? d->width1 : d->width, d->width});
+    s.push_back({d->head_k, d->n3x3 > 0 ? d->width : d->width1, 1});
+    return s;
+}
+
+size_t weight_count(const lg_net_desc *d) {
+    size_t n = 0;
+    for (auto &s : conv_shapes(d)) n += (size_t)s.cout * s.cin * s.k * s.k + s.cout;
+    if (d->value_head) n += (size_t)d->fc_hidden * kPoints + 2 * (size_t)d->fc_hidden + 1;
+    return n;
+}
+
+// ------------------------------------------------------------ device memory
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+// ------------------------------------------------------------ nets
+
+struct TcConv {
+    __nv_bfloat16 *w = nullptr;  // [taps][halves][N][64]
+    float *bias = nullptr;
+    float *scale = nullptr;      // FP8 weights: per-output-channel scale
+    int k, cin, cout, halves, ntaps;
+};
+
+struct Net {
+    lg_net_desc d{};
+    bool present = false;
+    std::vector<Shape> shapes;
+    // FP32 path
+    std::vector<float *> wt;     // per trunk conv: [k*k][cin][cout]
+    std::vector<float *> bias;
+    float *head_w = nullptr;     // [k*k][cin]
+    float head_b = 0.0f;
+    float *w1t = nullptr, *b1 = nullptr, *w2 = nullptr;
+    float b2 = 0.0f;
+    // tensor-core path
+    std::vector<TcConv> tc;
+    float *tc_head_w = nullptr;  // [width]
+};
+
+}  // namespace
+
+struct lg_ctx {
+    int device = 0;
+    int max_batch = 0;
+    int sm_count = 152;
+    Net nets[2];
+    cudaStream_t stream = nullptr;
+    std::vector<void *> allocs;
+    // FP32 buffers
+    float *act[2] = {nullptr, nullptr};
+    float *partial = nullptr;
+    // tensor-core buffers
+    __nv_bfloat16 *l3[2] = {nullptr, nullptr};
+    __nv_bfloat16 *l5 = nullptr;
+    int *d_err = nullptr;
+    // shared
+    uint8_t *d_planes = nullptr;
+    float *d_logits = nullptr, *d_probs = nullptr, *d_value = nullptr;
+    uint8_t *h_planes = nullptr;
+    float *h_out = nullptr, *h_out2 = nullptr;
+    int planes_c = 0;
+    std::mutex mu;
+    std::map<std::tuple<int, int, uint32_t, int>, std::pair<cudaGraphExec_t, int>> graphs;
+    std::atomic<long long> launches{0};
+    std::atomic<long long> batches{0};
+    std::atomic<int> fault_in{0};
+    // batching server
+    struct Req {
+        int net;
+        const uint8_t *planes;
+        int B;
+        float temperature;
+        float *out;
+        void *tag;
+    };
+    std::thread worker;
+    std::mutex qmu;
+    std::condition_variable qcv, dcv;
+    std::deque<Req> queue;
+    std::deque<void *> done;
+    bool stop = false;
+    bool worker_started = false;
+    int worker_error = 0;
+};
+
+namespace {
+
+template <class T>
+int dev_alloc(lg_ctx *c, T **p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        lg_set_error("cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+        *p = nullptr;
+        return LG_ERR_ALLOC;
+    }
+    c->allocs.push_back(*p);
+    return LG_OK;
+}
+
+template <class T>
+int upload(lg_ctx *c, T **p, const std::vector<T> &h) {
+    int rc = dev_alloc(c, p, h.size());
+    if (rc) return rc;
+    LG_CUDA_TRY(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return LG_OK;
+}
+
+bool tc_supported(const lg_net_desc *d) {
+    return d->c_in <= 32 && d->width1 == d->width && (d->width == 64 || d->width == 128) &&
+           d->head_k == 1 && d->n3x3 >= 1;
+}
+
+// E4M3 round-to-nearest-even with saturation at 448 (the quantiser of the
+// FP8-weight variant; E4M3 values are exact in BF16).
+float e4m3_round(float x) {
+    if (x != x) return x;
+    float a = std::fabs(x);
+    if (a >= 448.0f) return x < 0 ? -448.0f : 448.0f;
+    if (a == 0.0f) return x;
+    int e;
+    std::frexp(a, &e);
+    int ex = std::max(e - 1, -6);
+    float step = std::ldexp(1.0f, ex - 3);
+    float q = std::nearbyint(a / step) * step;
+    q = std::min(q, 448.0f);
+    return x < 0 ? -q : q;
+}
+
+int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
+    if (!valid_desc(d) || !d->weights) {
+        lg_set_error("invalid network description");
+        return LG_ERR_ARG;
+    }
+    if (d->precision != LG_FP32 && !tc_supported(d)) {
+        lg_set_error("BF16/FP8 paths need c_in <= 32, width1 == width in {64,128}, head_k == 1");
+        return LG_ERR_ARG;
+    }
+    n.d = *d;
+    n.d.weights = nullptr;
+    n.present = true;
+    n.shapes = conv_shapes(d);
+    const float *w = d->weights;
+    size_t off = 0;
+    int ntrunk = (int)n.shapes.size() - 1;
+    std::vector<std::vector<float>> Wraw(n.shapes.size()), Braw(n.shapes.size());
+    for (size_t l = 0; l < n.shapes.size(); ++l) {
+        auto s = n.shapes[l];
+        size_t nw = (size_t)s.cout * s.cin * s.k * s.k;
+        Wraw[l].assign(w + off, w + off + nw);
+        Braw[l].assign(w + off + nw, w + off + nw + s.cout);
+        off += nw + s.cout;
+    }
+    int rc;
+    // ---- FP32 layouts: W[o][c][ky][kx] -> wt[tap][c][o]
+    if (d->precision == LG_FP32) {
+        for (int l = 0; l < ntrunk; ++l) {
+            auto s = n.shapes[l];
+            int kk = s.k * s.k;
+            std::vector<float> wt((size_t)kk * s.cin * s.cout);
+            for (int o = 0; o < s.cout; ++o)
+                for (int ci = 0; ci < s.cin; ++ci)
+                    for (int t = 0; t < kk; ++t)
+                        wt[((size_t)t * s.cin + ci) * s.cout + o] =
+                            Wraw[l][((size_t)o * s.cin + ci) * kk + t];
+            float *dw, *db;
+            if ((rc = upload(c, &dw, wt)) || (rc = upload(c, &db, Braw[l]))) return rc;
+            n.wt.push_back(dw);
+            n.bias.push_back(db);
+        }
+        auto hs = n.shapes.back();
+        int kk = hs.k * hs.k;
+        std::vector<float> wh((size_t)kk * hs.cin);
+        for (int ci = 0; ci < hs.cin; ++ci)
+            for (int t = 0; t < kk; ++t) wh[(size_t)t * hs.cin + ci] = Wraw.back()[(size_t)ci * kk + t];
+        if ((rc = upload(c, &n.head_w, wh))) return rc;
+        n.head_b = Braw.back()[0];
+    } else {
+        // ---- tensor-core layouts: [tap][half][N][64] BF16, K-major rows.
+        bool fp8 = d->precision == LG_FP8W;
+        for (int l = 0; l < ntrunk; ++l) {
+            auto s = n.shapes[l];
+            TcConv t{};
+            t.k = s.k;
+            t.cin = s.cin;
+            t.cout = s.cout;
+            t.ntaps = (l == 0) ? 5 : 9;
+            // First layer: K of each vertical tap dy = the 5 horizontal taps
+            // dx x c_in channels (channel index dx*c_in + c), padded to 64s.
+            int kper = (l == 0) ? 5 * s.cin : s.cin;
+            t.halves = (kper + 63) / 64;
+            std::vector<float> scale(s.cout, 1.0f);
+            int kk = s.k * s.k;
+            if (fp8) {
+                for (int o = 0; o < s.cout; ++o) {
+                    float m = 0.0f;
+                    for (size_t i = 0; i < (size_t)s.cin * kk; ++i)
+                        m = std::max(m, std::fabs(Wraw[l][(size_t)o * s.cin * kk + i]));
+                    scale[o] = m > 0.0f ? m / 448.0f : 1.0f;
+                }
+            }
+            std::vector<__nv_bfloat16> wb((size_t)t.ntaps * t.halves * s.cout * 64,
+                                          __float2bfloat16(0.0f));
+            for (int tap = 0; tap < t.ntaps; ++tap)
+                for (int o = 0; o < s.cout; ++o)
+                    for (int kidx = 0; kidx < t.halves * 64; ++kidx) {
+                        float v = 0.0f;
+                        if (l == 0) {
+                            int dx = kidx / s.cin, ci = kidx % s.cin;
+                            if (kidx < 5 * s.cin)
+                                v = Wraw[l][((size_t)o * s.cin + ci) * kk + tap * 5 + dx];
+                        } else if (kidx < s.cin) {
+                            v = Wraw[l][((size_t)o * s.cin + kidx) * kk + tap];
+                        }
+                        if (fp8) v = e4m3_round(v / scale[o]);
+                        int half = kidx / 64;
+                        wb[(((size_t)tap * t.halves + half) * s.cout + o) * 64 + kidx % 64] =
+                            __float2bfloat16(v);
+                    }
+            if ((rc = upload(c, &t.w, wb)) || (rc = upload(c, &t.bias, Braw[l]))) return rc;
+            if (fp8 && (rc = upload(c, &t.scale, scale))) return rc;
+            n.tc.push_back(t);
+        }
+        // Fused 1x1 head weights, BF16-rounded as the precision states.
+        std::vector<float> hw(Wraw.back());
+        for (auto &v : hw) v = __bfloat162float(__float2bfloat16(v));
+        if ((rc = upload(c, &n.tc_head_w, hw))) return rc;
+        n.head_b = Braw.back()[0];
+    }
+    if (d->value_head) {
+        int H = d->fc_hidden;
+        const float *W1 = w + off;
+        std::vector<float> w1t((size_t)kPoints * H), b1(W1 + (size_t)H * kPoints,
+                                                       W1 + (size_t)H * kPoints + H);
+        std::vector<float> w2(W1 + (size_t)H * kPoints + H, W1 + (size_t)H * kPoints + 2 * H);
+        bool lowp = d->precision != LG_FP32;
+        for (int o = 0; o < H; ++o)
+            for (int i = 0; i < kPoints; ++i) {
+                float v = W1[(size_t)o * kPoints + i];
+                if (lowp) v = __bfloat162float(__float2bfloat16(v));
+                w1t[(size_t)i * H + o] = v;
+            }
+        if (lowp)
+            for (auto &v : w2) v = __bfloat162float(__float2bfloat16(v));
+        n.b2 = W1[(size_t)H * kPoints + 2 * H];
+        if ((rc = upload(c, &n.w1t, w1t)) || (rc = upload(c, &n.b1, b1)) ||
+            (rc = upload(c, &n.w2, w2)))
+            return rc;
+    }
+    return LG_OK;
+}
+
+int check_fault(lg_ctx *c) {
+    int f = c->fault_in.load();
+    if (f > 0) {
+        if (c->fault_in.fetch_sub(1) == 1) {
+            lg_set_error("injected fault");
+            return LG_ERR_CUDA;
+        }
+    }
+    return LG_OK;
+}
+
+// ------------------------------------------------------------ forward
+
+int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
+                 float *logits_out, float *value, cudaStream_t s, int *nlaunch) {
+    const lg_net_desc &d = n.d;
+    int L = 0;
+    launch_pack_planes_f32(planes, B, d.c_in, c->act[0], s);
+    ++L;
+    int cur = 0;
+    int ntrunk = (int)n.shapes.size() - 1;
+    for (int l = 0; l < ntrunk; ++l) {
+        auto sh = n.shapes[l];
+        launch_conv_f32(c->act[cur], n.wt[l], n.bias[l], c->act[cur ^ 1], B, sh.cin, sh.cout, sh.k,
+                        d.act, c->partial, s);
+        L += conv_f32_partial_floats(B, sh.cin, sh.cout, sh.k) ? 2 : 1;
+        cur ^= 1;
+    }
+    auto hs = n.shapes.back();
+    float *lg = logits_out ? logits_out : c->d_logits;
+    launch_head_conv_f32(c->act[cur], n.head_w, n.head_b, B, hs.cin, hs.k, d.act_head, d.act, lg, s);
+    ++L;
+    if (!d.value_head) {
+        launch_softmax(lg, B, T, probs, s);
+    } else {
+        launch_value_fc(lg, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value, s);
+    }
+    ++L;
+    *nlaunch = L;
+    return LG_OK;
+}
+
+int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
+               float *logits_out, float *value, cudaStream_t s, int *nlaunch) {
+    const lg_net_desc &d = n.d;
+    int L = 0;
+    const TcConv &first = n.tc[0];
+    launch_pack_planes_l5(planes, B, d.c_in, first.halves, c->l5, s);
+    ++L;
+    float *lg = logits_out ? logits_out : c->d_logits;
+    int cur = 0;
+    for (size_t l = 0; l < n.tc.size(); ++l) {
+        const TcConv &t = n.tc[l];
+        TcLayer tl{};
+        bool last = l + 1 == n.tc.size();
+        int rows = (l == 0) ? B * kL5Board : B * kL3Board;
+        const void *in = (l == 0) ? (const void *)c->l5 : (const void *)c->l3[cur];
+        int rc = encode_map_2d_bf16(&tl.in_map, in, (uint64_t)t.halves * 64, (uint64_t)rows, 64,
+                                    (l == 0) ? 128 + 80 : 128 + 48);
+        if (rc) return rc;
+        rc = encode_map_2d_bf16(&tl.w_map, t.w, 64, (uint64_t)t.ntaps * t.halves * t.cout, 64,
+                                (uint32_t)t.cout);
+        if (rc) return rc;
+        tl.bias = t.bias;
+        tl.scale = t.scale;
+        tl.head_w = last ? n.tc_head_w : nullptr;
+        tl.head_b = n.head_b;
+        tl.head_act = d.act_head;
+        tl.act = d.act;
+        tl.cin_halves = t.halves;
+        tl.n = t.cout;
+        tl.ntaps = t.ntaps;
+        tl.in_kind = (l == 0) ? 1 : 0;
+        tl.rows = rows;
+        tl.boards = B;
+        __nv_bfloat16 *out = (l == 0) ? c->l3[0] : c->l3[cur ^ 1];
+        rc = launch_tc_conv(tl, last ? nullptr : out, last ? lg : nullptr, c->d_err, s,
+                            c->sm_count);
+        if (rc) return rc;
+        ++L;
+        if (l > 0) cur ^= 1;
+    }
+    if (!d.value_head) {
+        launch_softmax(lg, B, T, probs, s);
+    } else {
+        launch_value_fc(lg, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value, s);
+    }
+    ++L;
+    *nlaunch = L;
+    return LG_OK;
+}
+
+int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
+            float *logits, float *value, cudaStream_t s, int *nlaunch) {
+    Net &n = c->nets[net];
+    if (n.d.precision == LG_FP32) return forward_fp32(c, n, planes, B, T, probs, logits, value, s, nlaunch);
+    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch);
+}
+
+// Host call: copy planes in, run (through a cached CUDA graph of
+// copy-in + forward + copy-out for this batch size), copy results out.
+int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
+             float *logits, float *value) {
+    Net &n = c->nets[net];
+    if (!n.present) {
+        lg_set_error("net %d was not created", net);
+        return LG_ERR_ARG;
+    }
+    if (B < 0 || (B > 0 && !planes)) {
+        lg_set_error("bad batch");
+        return LG_ERR_ARG;
+    }
+    int rc = check_fault(c);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    size_t per_in = (size_t)n.d.c_in * kPoints;
+    for (int b0 = 0; b0 < B; b0 += c->max_batch) {
+        int nb = std::min(c->max_batch, B - b0);
+        std::memcpy(c->h_planes, planes + (size_t)b0 * per_in, (size_t)nb * per_in);
+        uint32_t tbits;
+        std::memcpy(&tbits, &T, 4);
+        bool want_logits = logits != nullptr && !n.d.value_head;
+        auto key = std::make_tuple(net, nb, n.d.value_head ? 0u : tbits, want_logits ? 1 : 0);
+        auto it = c->graphs.find(key);
+        if (it == c->graphs.end()) {
+            cudaGraph_t g;
+            LG_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            cudaMemcpyAsync(c->d_planes, c->h_planes, (size_t)nb * per_in, cudaMemcpyHostToDevice,
+                            c->stream);
+            int nl = 0;
+            rc = forward(c, net, c->d_planes, nb, T, c->d_probs, want_logits ? c->d_logits : nullptr,
+                         c->d_value, c->stream, &nl);
+            if (n.d.value_head) {
+                cudaMemcpyAsync(c->h_out, c->d_value, (size_t)nb * sizeof(float),
+                                cudaMemcpyDeviceToHost, c->stream);
+            } else {
+                cudaMemcpyAsync(c->h_out, c->d_probs, (size_t)nb * kPoints * sizeof(float),
+                                cudaMemcpyDeviceToHost, c->stream);
+                if (want_logits)
+                    cudaMemcpyAsync(c->h_out2, c->d_logits, (size_t)nb * kPoints * sizeof(float),
+                                    cudaMemcpyDeviceToHost, c->stream);
+            }
+            cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+            if (rc) {
+                if (ce == cudaSuccess) cudaGraphDestroy(g);
+                return rc;
+            }
+            LG_CUDA_TRY(ce);
+            cudaGraphExec_t ge;
+            cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            LG_CUDA_TRY(ie);
+            it = c->graphs.emplace(key, std::make_pair(ge, nl)).first;
+        }
+        LG_CUDA_TRY(cudaGraphLaunch(it->second.first, c->stream));
+        c->launches += it->second.second;
+        LG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        int herr = 0;
+        LG_CUDA_TRY(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (herr) {
+            cudaMemset(c->d_err, 0, sizeof(int));
+            lg_set_error("kernel reported error status %d", herr);
+            return LG_ERR_DEVICE;
+        }
+        if (n.d.value_head) {
+            std::memcpy(value + b0, c->h_out, (size_t)nb * sizeof(float));
+        } else {
+            std::memcpy(probs + (size_t)b0 * kPoints, c->h_out, (size_t)nb * kPoints * sizeof(float));
+            if (want_logits)
+                std::memcpy(logits + (size_t)b0 * kPoints, c->h_out2,
+                            (size_t)nb * kPoints * sizeof(float));
+        }
+    }
+    return LG_OK;
+}
+
+int run_device(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
+               float *logits, float *value, cudaStream_t s) {
+    Net &n = c->nets[net];
+    if (!n.present) {
+        lg_set_error("net %d was not created", net);
+        return LG_ERR_ARG;
+    }
+    int rc = check_fault(c);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    size_t per_in = (size_t)n.d.c_in * kPoints;
+    for (int b0 = 0; b0 < B; b0 += c->max_batch) {
+        int nb = std::min(c->max_batch, B - b0);
+        int nl = 0;
+        rc = forward(c, net, planes + (size_t)b0 * per_in, nb, T,
+                     probs ? probs + (size_t)b0 * kPoints : nullptr,
+                     logits ? logits + (size_t)b0 * kPoints : nullptr, value ? value + b0 : nullptr,
+                     s, &nl);
+        if (rc) return rc;
+        c->launches += nl;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            lg_set_error("launch failed: %s", cudaGetErrorString(e));
+            return LG_ERR_CUDA;
+        }
+    }
+    return LG_OK;
+}
+
+// ------------------------------------------------------------ batching server
+//
+// Requests are taken in arrival order and packed into a batch of up to
+// max_batch positions of one net (and, for the policy, one temperature); the
+// batch is padded up to the next power of two so that a handful of CUDA
+// graphs (one per bucket) serve every size.
+
+int next_pow2(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+void worker_main(lg_ctx *c) {
+    cudaSetDevice(c->device);
+    std::vector<lg_ctx::Req> batch;
+    std::vector<uint8_t> staging;
+    std::vector<float> out;
+    for (;;) {
+        batch.clear();
+        {
+            std::unique_lock<std::mutex> lk(c->qmu);
+            c->qcv.wait(lk, [&] { return c->stop || !c->queue.empty(); });
+            if (c->stop && c->queue.empty()) return;
+            int total = 0;
+            int net = c->queue.front().net;
+            float T = c->queue.front().temperature;
+            while (!c->queue.empty()) {
+                auto &r = c->queue.front();
+                if (r.net != net || (net == LG_NET_POLICY && r.temperature != T)) break;
+                if (total > 0 && total + r.B > c->max_batch) break;
+                total += r.B;
+                batch.push_back(r);
+                c->queue.pop_front();
+            }
+        }
+        int net = batch[0].net;
+        Net &n = c->nets[net];
+        size_t per_in = (size_t)n.d.c_in * kPoints;
+        int total = 0;
+        for (auto &r : batch) total += r.B;
+        int bucket = std::min(next_pow2(total), std::max(total, c->max_batch));
+        staging.assign((size_t)bucket * per_in, 0);
+        size_t off = 0;
+        for (auto &r : batch) {
+            std::memcpy(staging.data() + off, r.planes, (size_t)r.B * per_in);
+            off += (size_t)r.B * per_in;
+        }
+        int per_out = n.d.value_head ? 1 : kPoints;
+        out.resize((size_t)bucket * per_out);
+        int rc;
+        {
+            std::lock_guard<std::mutex> g(c->mu);
+            rc = run_host(c, net, staging.data(), bucket, batch[0].temperature,
+                          n.d.value_head ? nullptr : out.data(), nullptr,
+                          n.d.value_head ? out.data() : nullptr);
+        }
+        c->batches++;
+        size_t o = 0;
+        for (auto &r : batch) {
+            if (rc == LG_OK) std::memcpy(r.out, out.data() + o, (size_t)r.B * per_out * sizeof(float));
+            o += (size_t)r.B * per_out;
+        }
+        {
+            std::lock_guard<std::mutex> lk(c->qmu);
+            if (rc != LG_OK) c->worker_error = rc;
+            for (auto &r : batch) c->done.push_back(r.tag);
+        }
+        c->dcv.notify_all();
+    }
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+
+extern "C" size_t lg_weight_count(const lg_net_desc *desc) {
+    if (!valid_desc(desc)) return 0;
+    return weight_count(desc);
+}
+
+extern "C" void lg_destroy(lg_ctx *c) {
+    if (!c) return;
+    if (c->worker_started) {
+        {
+            std::lock_guard<std::mutex> lk(c->qmu);
+            c->stop = true;
+        }
+        c->qcv.notify_all();
+        c->worker.join();
+    }
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &g : c->graphs) cudaGraphExecDestroy(g.second.first);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->h_planes) cudaFreeHost(c->h_planes);
+    if (c->h_out) cudaFreeHost(c->h_out);
+    if (c->h_out2) cudaFreeHost(c->h_out2);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, int device,
+                         int max_batch, lg_ctx **out) {
+    if (!out || (!policy && !value) || max_batch < 1 || max_batch > (1 << 16)) {
+        lg_set_error("lg_create: bad arguments");
+        return LG_ERR_ARG;
+    }
+    *out = nullptr;
+    if (policy && policy->value_head) {
+        lg_set_error("policy description has value_head set");
+        return LG_ERR_ARG;
+    }
+    if (value && !value->value_head) {
+        lg_set_error("value description lacks value_head");
+        return LG_ERR_ARG;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        lg_set_error("no CUDA device %d", device);
+        return LG_ERR_CUDA;
+    }
+    lg_ctx *c = new lg_ctx();
+    c->device = device;
+    c->max_batch = max_batch;
+    int rc = LG_OK;
+    auto fail = [&](int r) {
+        lg_destroy(c);
+        return r;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return fail(LG_ERR_CUDA);
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(LG_ERR_CUDA);
+    const lg_net_desc *descs[2] = {policy, value};
+    size_t max_act = 0, max_partial = 0, max_tc_l3 = 0, max_tc_l5 = 0;
+    int max_c_in = 0;
+    for (int i = 0; i < 2; ++i) {
+        if (!descs[i]) continue;
+        if ((rc = build_net(c, c->nets[i], descs[i]))) return fail(rc);
+        Net &n = c->nets[i];
+        max_c_in = std::max(max_c_in, n.d.c_in);
+        if (n.d.precision == LG_FP32) {
+            for (auto &s : n.shapes) {
+                max_act = std::max(max_act, (size_t)std::max(s.cin, s.cout));
+                for (int b = 1; b <= max_batch; b = (b < 64 ? b + 1 : b * 2))
+                    max_partial = std::max(max_partial, conv_f32_partial_floats(b, s.cin, s.cout, s.k));
+                max_partial = std::max(max_partial, conv_f32_partial_floats(max_batch, s.cin, s.cout, s.k));
+            }
+        } else {
+            if ((rc = tc_init_device())) return fail(rc);
+            max_tc_l3 = std::max(max_tc_l3, (size_t)n.d.width);
+            max_tc_l5 = std::max(max_tc_l5, (size_t)n.tc[0].halves * 64);
+        }
+    }
+    size_t mb = (size_t)max_batch;
+    if (max_act) {
+        if ((rc = dev_alloc(c, &c->act[0], mb * kPoints * max_act)) ||
+            (rc = dev_alloc(c, &c->act[1], mb * kPoints * max_act)) ||
+            (rc = dev_alloc(c, &c->partial, max_partial)))
+            return fail(rc);
+    }
+    if (max_tc_l3) {
+        if ((rc = dev_alloc(c, &c->l3[0], mb * kL3Board * max_tc_l3)) ||
+            (rc = dev_alloc(c, &c->l3[1], mb * kL3Board * max_tc_l3)) ||
+            (rc = dev_alloc(c, &c->l5, mb * kL5Board * max_tc_l5)))
+            return fail(rc);
+        // Pad rows of the L3 buffers are read as zeros and never written
+        // with anything else.
+        if (cudaMemset(c->l3[0], 0, mb * kL3Board * max_tc_l3 * 2) != cudaSuccess ||
+            cudaMemset(c->l3[1], 0, mb * kL3Board * max_tc_l3 * 2) != cudaSuccess)
+            return fail(LG_ERR_CUDA);
+    }
+    c->planes_c = max_c_in;
+    if ((rc = dev_alloc(c, &c->d_planes, mb * max_c_in * kPoints)) ||
+        (rc = dev_alloc(c, &c->d_logits, mb * kPoints)) ||
+        (rc = dev_alloc(c, &c->d_probs, mb * kPoints)) ||
+        (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)))
+        return fail(rc);
+    if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(LG_ERR_CUDA);
+    if (cudaMallocHost(&c->h_planes, mb * max_c_in * kPoints) != cudaSuccess ||
+        cudaMallocHost(&c->h_out, mb * kPoints * sizeof(float)) != cudaSuccess ||
+        cudaMallocHost(&c->h_out2, mb * kPoints * sizeof(float)) != cudaSuccess) {
+        lg_set_error("cudaMallocHost failed");
+        return fail(LG_ERR_ALLOC);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        lg_set_error("device error after upload");
+        return fail(LG_ERR_CUDA);
+    }
+    *out = c;
+    return LG_OK;
+}
+
+extern "C" int lg_policy(lg_ctx *c, const uint8_t *planes, int B, float temperature, float *probs,
+                         float *logits) {
+    if (!c || !probs || !(temperature > 0.0f)) {
+        lg_set_error("lg_policy: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    return run_host(c, LG_NET_POLICY, planes, B, temperature, probs, logits, nullptr);
+}
+
+extern "C" int lg_value(lg_ctx *c, const uint8_t *planes, int B, float *value) {
+    if (!c || !value) {
+        lg_set_error("lg_value: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    return run_host(c, LG_NET_VALUE, planes, B, 1.0f, nullptr, nullptr, value);
+}
+
+extern "C" int lg_policy_device(lg_ctx *c, const uint8_t *planes, int B, float temperature,
+                                float *probs, float *logits, void *stream) {
+    if (!c || !planes || !probs || B < 0 || !(temperature > 0.0f)) {
+        lg_set_error("lg_policy_device: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    return run_device(c, LG_NET_POLICY, planes, B, temperature, probs, logits, nullptr,
+                      (cudaStream_t)stream);
+}
+
+extern "C" int lg_value_device(lg_ctx *c, const uint8_t *planes, int B, float *value,
+                               void *stream) {
+    if (!c || !planes || !value || B < 0) {
+        lg_set_error("lg_value_device: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    return run_device(c, LG_NET_VALUE, planes, B, 1.0f, nullptr, nullptr, value,
+                      (cudaStream_t)stream);
+}
+
+extern "C" int lg_submit(lg_ctx *c, int net, const uint8_t *planes, int B, float temperature,
+                         float *out, void *tag) {
+    if (!c || (net != LG_NET_POLICY && net != LG_NET_VALUE) || !c->nets[net].present || !planes ||
+        !out || B < 1 || B > c->max_batch || !(temperature > 0.0f)) {
+        lg_set_error("lg_submit: bad arguments");
+        return LG_ERR_ARG;
+    }
+    {
+        std::lock_guard<std::mutex> lk(c->qmu);
+        if (c->worker_error) {
+            int e = c->worker_error;
+            c->worker_error = 0;
+            lg_set_error("an earlier batch failed");
+            return e;
+        }
+        if (!c->worker_started) {
+            c->worker = std::thread(worker_main, c);
+            c->worker_started = true;
+        }
+        c->queue.push_back({net, planes, B, temperature, out, tag});
+    }
+    c->qcv.notify_one();
+    return LG_OK;
+}
+
+extern "C" int lg_poll(lg_ctx *c, void **tags, int max, int timeout_us) {
+    if (!c || !tags || max < 1 || timeout_us < 0) {
+        lg_set_error("lg_poll: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::unique_lock<std::mutex> lk(c->qmu);
+    if (c->done.empty() && timeout_us > 0)
+        c->dcv.wait_for(lk, std::chrono::microseconds(timeout_us), [&] { return !c->done.empty(); });
+    int n = 0;
+    while (n < max && !c->done.empty()) {
+        tags[n++] = c->done.front();
+        c->done.pop_front();
+    }
+    if (n == 0 && c->worker_error) {
+        int e = c->worker_error;
+        c->worker_error = 0;
+        lg_set_error("a batch failed");
+        return e;
+    }
+    return n;
+}
+
+extern "C" int lg_stats(lg_ctx *c, long long *kernel_launches, long long *batches) {
+    if (!c) return LG_ERR_ARG;
+    if (kernel_launches) *kernel_launches = c->launches.load();
+    if (batches) *batches = c->batches.load();
+    return LG_OK;
+}
+
+extern "C" int lg_inject_fault(lg_ctx *c, int nth_call) {
+    if (!c || nth_call < 0) return LG_ERR_ARG;
+    c->fault_in = nth_call;
+    return LG_OK;
+}

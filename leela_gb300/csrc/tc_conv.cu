@@ -1,0 +1,435 @@
+// tc_conv.cu -- convolution layers as implicit GEMMs on the tcgen05 tensor
+// cores (BF16 operands, FP32 accumulators in TMEM).
+//
+// Reference: convolve<k,C,O> (Network.cpp:345-393) computes
+//   out[o][p] = act(b[o] + sum_{c,ky,kx} W[o][c][ky][kx] * in[c][p + (ky,kx)])
+// through an im2col matrix and one sgemm per layer.  Here the im2col never
+// exists: activations live in HBM as "flat rows" (lg_common.cuh, layouts L3
+// and L5) in which every tap of the filter is one constant row shift.  For a
+// tile of 128 consecutive rows, one TMA load brings the tile plus its halo
+// (the "window") into shared memory, and the A operand of tap t is the same
+// window read through a shared-memory descriptor that starts
+// (window_pre + shift_t) rows in.  The 128-byte swizzle is a function of the
+// absolute shared-memory address, so a descriptor may start at any row; the
+// window is loaded once and read by all 9 (or 5) taps.
+//
+// Per CTA (persistent, one per SM):
+//   warp 0        TMA producer: windows (double-buffered) and weight slices
+//                 (one tap x 64 input channels, ring of S stages)
+//   warp 1        TMEM owner and MMA issuer (one elected thread), M=128,
+//                 N=width, K=16 per instruction
+//   warps 2..5    epilogue: tcgen05.ld -> (x FP8 scale) + bias -> act ->
+//                 BF16 store, zeros on pad rows; or, for the last trunk
+//                 layer, the fused 1x1 head (dot with the head weights)
+// Accumulators are double-buffered in TMEM (2 x N columns), so the epilogue
+// of tile i overlaps the MMAs of tile i+1.
+//
+// Every mbarrier wait is bounded; on a timeout the CTA records an error code,
+// stops issuing work, drains what it issued and frees its TMEM.
+#include "lg_kernels.h"
+
+namespace lg {
+
+using namespace ptx;
+
+constexpr int kTcThreads = 192;
+constexpr uint32_t kWaitLimit = 1u << 26;
+
+struct TcParams {
+    const float *bias;
+    const float *scale;
+    const float *head_w;
+    float head_b;
+    int head_act;
+    int act;
+    int rows;
+    int ntiles;
+    __nv_bfloat16 *out;
+    float *logits;
+    int *err;
+};
+
+template <int N, int HALVES, int KIND>
+struct TcCfg {
+    static constexpr int NTAPS = KIND == 0 ? 9 : 5;
+    static constexpr int WPRE = KIND == 0 ? 24 : 40;
+    static constexpr int WROWS = 128 + 2 * WPRE;
+    static constexpr int WIN_HALF = WROWS * 128;
+    static constexpr int WIN_BYTES = HALVES * WIN_HALF;
+    static constexpr int WST_BYTES = N * 128;
+    static constexpr int BUDGET = 220 * 1024;
+    static constexpr int S_RAW = (BUDGET - 2 * WIN_BYTES) / WST_BYTES;
+    static constexpr int S = S_RAW > 8 ? 8 : S_RAW;
+    static constexpr int SMEM = 1024 + 2 * WIN_BYTES + S * WST_BYTES;
+    static constexpr int TMEM_COLS = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
+    static_assert(S >= 2, "not enough shared memory for the weight ring");
+    static_assert(SMEM <= 227 * 1024, "shared memory budget");
+};
+
+__device__ __forceinline__ int tap_shift(int kind, int t) {
+    if (kind == 0) return (t / 3 - 1) * kL3Pitch + (t % 3 - 1);
+    return (t - 2) * kL5Pitch;
+}
+
+__device__ __forceinline__ float act_apply(float v, int act) {
+    if (act == LG_ACT_ELU) return (v > 0.0f) ? v : (expf(v) - 1.0f);
+    return fmaxf(v, 0.0f);
+}
+
+template <int N, int HALVES, int KIND, bool HEAD>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tc_conv_kernel(const __grid_constant__ CUtensorMap in_map,
+                   const __grid_constant__ CUtensorMap w_map, const TcParams p) {
+    using C = TcCfg<N, HALVES, KIND>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *win = smem;                       // 2 x WIN_BYTES
+    uint8_t *wst = smem + 2 * C::WIN_BYTES;    // S x WST_BYTES
+
+    __shared__ uint64_t win_full[2], win_empty[2], w_full[C::S], w_empty[C::S];
+    __shared__ uint64_t acc_full[2], acc_empty[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&win_full[i], 1);
+            mbar_init(&win_empty[i], 1);
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], 4);
+        }
+        for (int i = 0; i < C::S; ++i) {
+            mbar_init(&w_full[i], 1);
+            mbar_init(&w_empty[i], 1);
+        }
+        abort_flag = 0;
+        fence_mbar_init();
+        prefetch_tensormap(&in_map);
+        prefetch_tensormap(&w_map);
+    }
+    if (warp == 1) tmem_alloc(&tmem_base, C::TMEM_COLS);
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    auto fail = [&](int code) {
+        atomicCAS(p.err, 0, code);
+        atomicExch(&abort_flag, 1);
+    };
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            uint32_t g = 0;
+            int local = 0;
+            for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag;
+                 tile += gridDim.x, ++local) {
+                const int wb = local & 1;
+                const uint32_t wk = (uint32_t)(local >> 1);
+                if (!mbar_wait(&win_empty[wb], (wk & 1) ^ 1, kWaitLimit)) { fail(11); break; }
+                mbar_arrive_expect_tx(&win_full[wb], C::WIN_BYTES);
+                const int row0 = tile * 128 - C::WPRE;
+                for (int h = 0; h < HALVES; ++h)
+                    tma_load_2d(win + wb * C::WIN_BYTES + h * C::WIN_HALF, &in_map, &win_full[wb],
+                                h * 64, row0);
+                for (int t = 0; t < C::NTAPS; ++t)
+                    for (int h = 0; h < HALVES; ++h, ++g) {
+                        const int s = g % C::S;
+                        const uint32_t k = g / C::S;
+                        if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(12); goto done_producer; }
+                        mbar_arrive_expect_tx(&w_full[s], C::WST_BYTES);
+                        tma_load_2d(wst + s * C::WST_BYTES, &w_map, &w_full[s], 0,
+                                    (t * HALVES + h) * N);
+                    }
+            }
+        done_producer:;
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(128, N);
+            uint32_t g = 0;
+            int local = 0;
+            for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag;
+                 tile += gridDim.x, ++local) {
+                const int wb = local & 1, acc = local & 1;
+                const uint32_t wk = (uint32_t)(local >> 1);
+                if (!mbar_wait(&acc_empty[acc], (wk & 1) ^ 1, kWaitLimit)) { fail(21); break; }
+                if (!mbar_wait(&win_full[wb], wk & 1, kWaitLimit)) { fail(22); break; }
+                tc_fence_after();
+                const uint32_t d_tmem = tmem + (uint32_t)(acc * N);
+                const uint32_t win_addr = smem_u32(win + wb * C::WIN_BYTES);
+                bool first = true;
+                for (int t = 0; t < C::NTAPS; ++t) {
+                    const uint32_t a_row = (uint32_t)(C::WPRE + tap_shift(KIND, t)) * 128u;
+                    for (int h = 0; h < HALVES; ++h, ++g) {
+                        const int s = g % C::S;
+                        const uint32_t k = g / C::S;
+                        if (!mbar_wait(&w_full[s], k & 1, kWaitLimit)) { fail(23); goto done_mma; }
+                        tc_fence_after();
+                        const uint32_t a_base = win_addr + h * C::WIN_HALF + a_row;
+                        const uint32_t b_base = smem_u32(wst + s * C::WST_BYTES);
+#pragma unroll
+                        for (int kk = 0; kk < 4; ++kk) {
+                            mma_bf16(d_tmem, sdesc_sw128(a_base + kk * 32), sdesc_sw128(b_base + kk * 32),
+                                     idesc, first ? 0u : 1u);
+                            first = false;
+                        }
+                        mma_commit(&w_empty[s]);
+                    }
+                }
+                mma_commit(&win_empty[wb]);
+                mma_commit(&acc_full[acc]);
+            }
+        done_mma:;
+        }
+    } else {
+        // ------------------------------------------------ epilogue
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        int local = 0;
+        for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag; tile += gridDim.x, ++local) {
+            const int acc = local & 1;
+            const uint32_t ak = (uint32_t)(local >> 1);
+            if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(31); break; }
+            tc_fence_after();
+            const int q = tile * 128 + row;
+            // Where this row goes: output row (L3) and board point.
+            bool valid = false;
+            int orow = -1, point = -1;
+            if (q < p.rows) {
+                if (KIND == 0) {
+                    const int b = q / kL3Board, r = q % kL3Board, y = r / kL3Pitch, x = r % kL3Pitch;
+                    orow = q;
+                    valid = (x < kBoard && y < kBoard);
+                    point = b * kPoints + y * kBoard + x;
+                } else {
+                    const int b = q / kL5Board, r = q % kL5Board, y = r / kL5Pitch, x = r % kL5Pitch;
+                    valid = y < kBoard;
+                    orow = valid ? b * kL3Board + y * kL3Pitch + x : -1;
+                    point = b * kPoints + y * kBoard + x;
+                }
+            }
+            const uint32_t t_row = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * N);
+            float head_sum = 0.0f;
+#pragma unroll 1
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                uint32_t v[16];
+                tmem_ld16(t_row + c0, v);
+                tmem_ld_wait();
+                float f[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    float x = __uint_as_float(v[i]);
+                    if (p.scale) x *= __ldg(p.scale + c0 + i);
+                    f[i] = act_apply(x + __ldg(p.bias + c0 + i), p.act);
+                }
+                if (HEAD) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) head_sum = fmaf(f[i], __ldg(p.head_w + c0 + i), head_sum);
+                } else if (orow >= 0) {
+                    uint4 pk[2];
+                    uint32_t *w32 = reinterpret_cast<uint32_t *>(pk);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        __nv_bfloat162 h2 = valid ? __floats2bfloat162_rn(f[2 * i], f[2 * i + 1])
+                                                  : __floats2bfloat162_rn(0.0f, 0.0f);
+                        w32[i] = *reinterpret_cast<uint32_t *>(&h2);
+                    }
+                    uint4 *dst = reinterpret_cast<uint4 *>(p.out + (size_t)orow * N + c0);
+                    dst[0] = pk[0];
+                    dst[1] = pk[1];
+                }
+            }
+            if (HEAD && valid) {
+                float x = head_sum + p.head_b;
+                p.logits[point] = p.head_act ? act_apply(x, p.act) : x;
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[acc]);
+        }
+    }
+
+    __syncthreads();
+    if (abort_flag && tid == 0) {
+        // Drain: wait (bounded) for any TMA still in flight into this CTA's
+        // shared memory before the CTA exits.
+        for (int i = 0; i < 2; ++i) {
+            mbar_wait(&win_full[i], 0, 1u << 16);
+            mbar_wait(&win_full[i], 1, 1u << 16);
+        }
+        for (int i = 0; i < C::S; ++i) {
+            mbar_wait(&w_full[i], 0, 1u << 16);
+            mbar_wait(&w_full[i], 1, 1u << 16);
+        }
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) tmem_dealloc(tmem, C::TMEM_COLS);
+    if (warp == 1) tmem_relinquish();
+}
+
+// ------------------------------------------------------------------ packing
+
+// planes [B][C][361] bytes -> L5 rows [B*399][halves*64] BF16, channel
+// dx*C + c = plane c at (y, x + dx - 2); zero rows y = 19, 20 and zero
+// channels >= 5C.
+__global__ void pack_planes_l5_kernel(const uint8_t *__restrict__ planes, int B, int C, int halves,
+                                      __nv_bfloat16 *__restrict__ out) {
+    const int groups = halves * 8;  // 8 channels per group
+    const size_t total = (size_t)B * kL5Board * groups;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t q = i / groups;
+        const int g = (int)(i % groups);
+        const int b = (int)(q / kL5Board), r = (int)(q % kL5Board);
+        const int y = r / kL5Pitch, x = r % kL5Pitch;
+        __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int ch = g * 8 + j;
+            float val = 0.0f;
+            if (y < kBoard && ch < 5 * C) {
+                const int dx = ch / C, c = ch % C;
+                const int sx = x + dx - 2;
+                if (sx >= 0 && sx < kBoard)
+                    val = (float)planes[((size_t)b * C + c) * kPoints + y * kBoard + sx];
+            }
+            v[j] = __float2bfloat16(val);
+        }
+        *reinterpret_cast<uint4 *>(out + q * (size_t)(halves * 64) + g * 8) =
+            *reinterpret_cast<const uint4 *>(v);
+    }
+}
+
+void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv_bfloat16 *out,
+                           cudaStream_t s) {
+    size_t total = (size_t)B * kL5Board * halves * 8;
+    int blocks = (int)std::min<size_t>((total + 255) / 256, 8192);
+    pack_planes_l5_kernel<<<blocks, 256, 0, s>>>(planes, B, C, halves, out);
+}
+
+// ------------------------------------------------------------------ launch
+
+template <int N, int HALVES, int KIND, bool HEAD>
+static int set_attr() {
+    cudaError_t e = cudaFuncSetAttribute(tc_conv_kernel<N, HALVES, KIND, HEAD>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         TcCfg<N, HALVES, KIND>::SMEM);
+    if (e != cudaSuccess) {
+        lg_set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+        return LG_ERR_CUDA;
+    }
+    return LG_OK;
+}
+
+template <int N, int HALVES, int KIND, bool HEAD>
+static int launch_impl(const TcLayer &L, const TcParams &p, cudaStream_t s, int sm_count) {
+    using Cfg = TcCfg<N, HALVES, KIND>;
+    int grid = std::min(p.ntiles, sm_count);
+    tc_conv_kernel<N, HALVES, KIND, HEAD><<<grid, kTcThreads, Cfg::SMEM, s>>>(L.in_map, L.w_map, p);
+    return LG_OK;
+}
+
+// Raises the dynamic shared-memory limit of every instantiation; called once
+// per device before any launch (and so before any stream capture).
+int tc_init_device() {
+    int rc = 0;
+#define LG_TC_ATTR(N_, H_, K_)                                  \
+    if (!rc) rc = set_attr<N_, H_, K_, false>();                 \
+    if (!rc && K_ == 0) rc = set_attr<N_, H_, K_, true>();
+    LG_TC_ATTR(128, 2, 0)
+    LG_TC_ATTR(64, 1, 0)
+    LG_TC_ATTR(128, 2, 1)
+    LG_TC_ATTR(128, 3, 1)
+    LG_TC_ATTR(64, 2, 1)
+    LG_TC_ATTR(64, 3, 1)
+#undef LG_TC_ATTR
+    return rc;
+}
+
+template <int N, int HALVES, int KIND>
+static int dispatch(const TcLayer &L, const TcParams &p, bool head, cudaStream_t s, int sm_count) {
+    if constexpr (KIND == 0) {
+        if (head) return launch_impl<N, HALVES, KIND, true>(L, p, s, sm_count);
+    } else if (head) {
+        lg_set_error("the fused head needs a 3x3 (L3) layer");
+        return LG_ERR_ARG;
+    }
+    return launch_impl<N, HALVES, KIND, false>(L, p, s, sm_count);
+}
+
+size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves) {
+    if (ntaps == 9) return n == 128 ? TcCfg<128, 2, 0>::SMEM : TcCfg<64, 1, 0>::SMEM;
+    return cin_halves == 2 ? TcCfg<128, 2, 1>::SMEM : TcCfg<128, 3, 1>::SMEM;
+}
+
+int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *logits, int *err,
+                   cudaStream_t s, int sm_count) {
+    TcParams p{};
+    p.bias = L.bias;
+    p.scale = L.scale;
+    p.head_w = L.head_w;
+    p.head_b = L.head_b;
+    p.head_act = L.head_act;
+    p.act = L.act;
+    p.rows = L.rows;
+    p.ntiles = (L.rows + 127) / 128;
+    p.out = out_l3;
+    p.logits = logits;
+    p.err = err;
+    const bool head = L.head_w != nullptr;
+    if (head && !logits) return LG_ERR_ARG;
+    if (!head && !out_l3) return LG_ERR_ARG;
+#define LG_TC_CASE(N_, H_, K_)                                                      \
+    if (L.n == N_ && L.cin_halves == H_ && L.in_kind == K_)                         \
+        return dispatch<N_, H_, K_>(L, p, head, s, sm_count);
+    LG_TC_CASE(128, 2, 0)
+    LG_TC_CASE(64, 1, 0)
+    LG_TC_CASE(128, 2, 1)
+    LG_TC_CASE(128, 3, 1)
+    LG_TC_CASE(64, 2, 1)
+    LG_TC_CASE(64, 3, 1)
+#undef LG_TC_CASE
+    lg_set_error("no tensor-core kernel for N=%d halves=%d kind=%d", L.n, L.cin_halves, L.in_kind);
+    return LG_ERR_ARG;
+}
+
+// ------------------------------------------------------------ tensor maps
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encode_map_2d_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint64_t rows,
+                       uint32_t box_inner, uint32_t box_rows) {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            !f) {
+            lg_set_error("cuTensorMapEncodeTiled not available");
+            return LG_ERR_CUDA;
+        }
+        fn = (EncodeTiledFn)f;
+    }
+    cuuint64_t dims[2] = {inner, rows};
+    cuuint64_t strides[1] = {inner * 2};
+    cuuint32_t box[2] = {box_inner, box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides,
+                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        lg_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return LG_ERR_CUDA;
+    }
+    return LG_OK;
+}
+
+}  // namespace lg

@@ -1,0 +1,141 @@
+"""The CPU oracle against the reference's own outputs (tests/golden, made by
+tests/golden/make_golden.py from the reference's compiled CPU/BLAS code)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_logit_err
+
+
+def test_weights_match_golden_checksums(weights, oracle_mod):
+    with open(os.path.join(GOLDEN, "weights.json")) as f:
+        sums = json.load(f)
+    assert oracle_mod.checksum(weights["cfg_p"][1]) == sums["cfg_policy"]
+    assert oracle_mod.checksum(weights["cfg_v"][1]) == sums["cfg_value"]
+    assert oracle_mod.checksum(weights["ref_p"][1]) == sums["ref_policy"]
+    assert oracle_mod.checksum(weights["ref_v"][1]) == sums["ref_value"]
+
+
+def test_he_normal_statistics(weights, oracle_mod):
+    n, w = weights["cfg_p"]
+    shapes = oracle_mod.conv_shapes(n)
+    k, ci, co, off = shapes[1]
+    W = w[off:off + co * ci * k * k]
+    assert abs(W.mean()) < 3e-3
+    assert abs(W.std() - np.sqrt(2.0 / (ci * k * k))) / np.sqrt(2.0 / (ci * k * k)) < 0.01
+    b = w[off + co * ci * k * k: off + co * ci * k * k + co]
+    assert np.all(b == 0)
+
+
+def test_det_log(oracle_mod):
+    L = oracle_mod.lib()
+    for x in [1e-300, 1e-9, 0.001, 0.37, 0.5, 0.999999, 1.0, 7.0]:
+        assert abs(L.or_det_log(x) - np.log(x)) <= 4e-16 * max(1.0, abs(np.log(x)))
+
+
+@pytest.mark.parametrize("rot", [0, 3])
+def test_config1_policy_matches_reference(positions, golden_config1, weights, oracle_mod, rot):
+    O = oracle_mod
+    n, w = weights["cfg_p"]
+    planes = np.stack([O.rotate_planes(p[:24], rot) for p in positions["planes_p"][:6]])
+    ref = golden_config1[f"logits_r{rot}"][:6]
+    O.enable_blas()
+    try:
+        blas = O.forward_f32(n, w, planes)
+    finally:
+        O.disable_blas()
+    # With the same BLAS the restatement reproduces the reference bit for bit.
+    if O.find_openblas():
+        assert np.array_equal(blas, ref)
+    loops = O.forward_f32(n, w, planes)
+    assert rel_logit_err(loops, ref).max() < 1e-5
+    assert np.array_equal(loops.argmax(1), ref.argmax(1))
+    probs = O.softmax_f32(ref, 1.0)
+    assert np.abs(probs - golden_config1[f"probs_r{rot}"][:6]).max() < 1e-7
+    f64 = O.forward_f64(n, w, planes)
+    assert rel_logit_err(f64, ref).max() < 1e-5
+
+
+def test_config1_value_matches_reference(positions, golden_config1, weights, oracle_mod):
+    O = oracle_mod
+    n, w = weights["cfg_v"]
+    v = O.forward_f32(n, w, positions["planes_v"][:6, :24])
+    assert np.abs(v - golden_config1["value_r0"][:6]).max() < 1e-5
+    v64 = O.forward_f64(n, w, positions["planes_v"][:6, :24])
+    assert np.abs(v64 - golden_config1["value_r0"][:6]).max() < 1e-5
+
+
+@pytest.mark.parametrize("rot", [0, 5])
+def test_reference_shaped_nets_match_reference(positions, golden_refexact, weights, oracle_mod,
+                                               rot):
+    """ELU everywhere, 3x3 heads, 32->96->128 policy, 64-wide value with the
+    (1+tanh)/2 map: the reference's own Network.cpp forward."""
+    O = oracle_mod
+    n, w = weights["ref_p"]
+    planes = np.stack([O.rotate_planes(p, rot) for p in positions["planes_p"][:4]])
+    lo = O.forward_f32(n, w, planes)
+    ref = golden_refexact[f"logits_r{rot}"][:4]
+    assert rel_logit_err(lo, ref).max() < 1e-5
+    nv, wv = weights["ref_v"]
+    pv = np.stack([O.rotate_planes(p, rot) for p in positions["planes_v"][:4]])
+    v = O.forward_f32(nv, wv, pv)
+    assert np.abs(v - golden_refexact[f"value_r{rot}"][:4]).max() < 1e-5
+
+
+def test_scored_moves_unrotation_and_ladder(positions, golden_refexact, weights, oracle_mod):
+    """Netresult assembly (Network.cpp:656-667, 820-829): softmax at the
+    search temperature 0.75, un-rotate, EMPTY points only, losing ladders 0."""
+    O = oracle_mod
+    import leela_gb300 as lg
+    n, w = weights["ref_p"]
+    for rot in (0, 5):
+        for i in range(3):
+            planes = O.rotate_planes(positions["planes_p"][i], rot)[None]
+            probs = O.softmax_f32(O.forward_f32(n, w, planes), 0.75)[0]
+            sq = positions["squares"][i]
+            ladder = positions["planes_p"][i][25]
+            got = np.full(361, -1.0, dtype=np.float32)
+            for idx in range(361):
+                if sq[idx] == 2:
+                    got[idx] = 0.0 if ladder[idx] else probs[lg.REV_ROTATE[rot][idx]]
+            ref = golden_refexact[f"probs_r{rot}"][i]
+            assert np.array_equal(got < 0, ref < 0)
+            assert np.abs(got - ref).max() < 1e-6
+
+
+def test_rotation_tables(oracle_mod):
+    import leela_gb300 as lg
+    for s in range(8):
+        for v in range(361):
+            assert oracle_mod.rotate_nn_idx(v, s) == lg.rotate_nn_idx(v, s)
+            assert lg.rotate_nn_idx(lg.rev_rotate_nn_idx(v, s), s) == v
+
+
+def test_softmax_edge_cases(oracle_mod):
+    O = oracle_mod
+    x = np.zeros(361, dtype=np.float32)
+    p = O.softmax_f32(x, 1.0)
+    assert np.allclose(p, 1.0 / 361)
+    x = np.full(361, -1e4, dtype=np.float32)
+    x[7] = 80.0
+    p = O.softmax_f32(x, 0.75)
+    assert p[7] == 1.0 and np.isfinite(p).all()
+    x = np.random.default_rng(0).normal(size=361).astype(np.float32) * 40
+    p32 = O.softmax_f32(x, 0.75)
+    p64 = O.softmax_f64(x.astype(np.float64), 0.75)
+    assert np.abs(p32 - p64).max() < 1e-6
+
+
+def test_e4m3_rounding(oracle_mod):
+    r = oracle_mod.e4m3_round
+    assert r(448.0) == 448.0 and r(1000.0) == 448.0 and r(-1000.0) == -448.0
+    assert r(1.0) == 1.0 and r(1.0625) == 1.0 and r(1.1875) == 1.25  # ties to even
+    assert r(2.0 ** -9) == 2.0 ** -9 and r(2.0 ** -11) == 0.0
+    assert r(0.3) == 0.3125 - 0.0 or abs(r(0.3) - 0.3) <= 2.0 ** -5
+
+
+def test_mcowner_labels_in_range():
+    d = np.load(os.path.join(GOLDEN, "mcowner_s0.npz"))["mcowner"]
+    assert d.shape == (64,) and np.all((d >= 0) & (d <= 1))
