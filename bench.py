@@ -1,0 +1,440 @@
+#!/usr/bin/env python
+"""Throughput of the policy + value evaluation path on GB300.
+
+Workload (one "step"): 8192 positions through BOTH benchmark nets -- policy
+(5x5 24->128, 11x 3x3 128->128, 1x1 head, ReLU, softmax over 361) and value
+(same trunk, FC 361->256 ReLU, FC 256->1, tanh) -- in batches of 256, on the
+BF16 tensor-core path.  Positions: the 1024 seeded positions of
+tests/golden/positions_s0.npz (empty board, komi 7.5, k~U[0,250] uniform legal
+moves, planes from the reference's own feature gather) under the 8 board
+symmetries = 8192 distinct inputs.  Weights: He-normal, zero biases, seeds 1
+(policy) and 2 (value).
+
+Reported (one JSON line on rank 0):
+  value       positions/s with inputs resident in HBM (lg_*_device)
+  e2e         positions/s through the host C ABI (lg_policy / lg_value with
+              host buffers; host->device and device->host copies timed)
+  roofline    the dominant kernel (tensor-core 3x3 conv), CUDA-event timed
+              inside the timed region, against the measured BF16 peak
+  cpu_baseline  the reference algorithm (im2col + OpenBLAS sgemm, one
+              position per thread) on this host's cores, bounded sample
+  fp32_plain_batch1  the plain FP32 drop-in path at batch 1 (the ratio
+              target's denominator), and top-1 agreement of BF16 vs FP64
+
+--impl reference: the reference's CPU path (the C restatement of
+Network.cpp's im2col + sgemm + bias + activation over scipy's OpenBLAS; the
+reference engine itself cannot be built where its sources are absent) on all
+host threads, same metric and config.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "positions/sec policy+value net, BF16 vs FP32 plain on GB300 at ≥99% top-1 agree"
+BATCH = 256
+POSITIONS = 8192
+# Algorithmic FLOPs of one 3x3 128->128 conv per position: 2 * 361 * 128 * 1152.
+FLOP_3X3_PER_POS = 2 * 361 * 128 * 1152
+# Policy (1,226,637,568) + value (1,226,822,912) FLOP per position.
+FLOP_PAIR_PER_POS = 2_453_460_480
+
+
+def load_positions():
+    d = np.load(os.path.join(ROOT, "tests", "golden", "positions_s0.npz"))
+    pp = np.unpackbits(d["planes_p"], axis=-1)[:, :24, :361]
+    pv = np.unpackbits(d["planes_v"], axis=-1)[:, :24, :361]
+    import leela_gb300 as lg
+    P = np.concatenate([pp[..., lg.ROTATE[s]] for s in range(8)])
+    V = np.concatenate([pv[..., lg.ROTATE[s]] for s in range(8)])
+    return np.ascontiguousarray(P), np.ascontiguousarray(V)
+
+
+def make_weights():
+    from oracle import oracle as O
+    P, V = O.make_net(O.CFG_POLICY), O.make_net(O.CFG_VALUE)
+    return P, V, O.he_weights(P, O.POLICY_SEED), O.he_weights(V, O.VALUE_SEED)
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p.get("bf16_tflops_sustained", 1700.0), p.get("hbm_gbs", 6800.0), "measured"
+    except (OSError, ValueError):
+        return 1700.0, 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------- CPU baseline
+
+def cpu_baseline(planes_p, planes_v, seconds: float = 12.0, nthreads: int = 0):
+    """The reference algorithm on the host: im2col + OpenBLAS sgemm + bias +
+    activation per layer (Network.cpp:345-423), one position per thread
+    (Network.cpp:239), every host core."""
+    from oracle import oracle as O
+    P, V, wp, wv = make_weights()
+    blas = O.enable_blas()
+    n = nthreads or os.cpu_count()
+    sample = planes_p[:512], planes_v[:512]
+    t = O.time_pair_f32(P, wp, V, wv, sample[0], sample[1], n, n)
+    iters = max(n, int(seconds / max(t, 1e-3) * n))
+    el = O.time_pair_f32(P, wp, V, wv, sample[0], sample[1], iters, n)
+    O.disable_blas()
+    return {"value": iters / el, "unit": "positions/s", "cores": n, "kind": "port",
+            "sample": f"{iters} policy+value evaluations over 512 positions, "
+                      f"{'OpenBLAS sgemm' if blas else 'plain-loop GEMM'}, {el:.1f} s"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    planes_p, planes_v = load_positions()
+    P, V, wp, wv = make_weights()
+    blas = O.enable_blas()
+    n = os.cpu_count()
+    per_step = 4 * n
+    for _ in range(args.warmup):
+        O.time_pair_f32(P, wp, V, wv, planes_p[:512], planes_v[:512], per_step, n)
+    total = 0.0
+    for _ in range(args.steps):
+        total += O.time_pair_f32(P, wp, V, wv, planes_p[:512], planes_v[:512], per_step, n)
+    value = per_step * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "positions/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "config-1 policy+value nets (5x5 24->128, 11x 3x3 128->128, "
+                               "1x1 head, ReLU, FC 361->256->1 tanh), CPU", "batch": 1,
+                   "positions_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "positions/s", "cores": n, "kind": "port",
+                         "sample": f"{per_step} policy+value evaluations per step over 512 "
+                                   f"positions, one per thread, "
+                                   f"{'OpenBLAS sgemm' if blas else 'plain-loop GEMM'}"},
+        "e2e": {"value": value, "unit": "positions/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    O.disable_blas()
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import leela_gb300 as lg
+    from leela_gb300 import build as B
+    B.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    planes_p, planes_v = load_positions()
+    P, V, wp, wv = make_weights()
+    ctx = lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"),
+                     value=lg.NetDesc.config1_value(wv, "bf16"), device=local, max_batch=BATCH)
+    d_p = torch.from_numpy(planes_p).to(dev)
+    d_v = torch.from_numpy(planes_v).to(dev)
+    d_probs = torch.empty((POSITIONS, 361), dtype=torch.float32, device=dev)
+    d_val = torch.empty(POSITIONS, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step():
+        ctx.policy_device(d_p.data_ptr(), POSITIONS, d_probs.data_ptr(), 1.0, None, sp)
+        ctx.value_device(d_v.data_ptr(), POSITIONS, d_val.data_ptr(), sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # ---------------- timed region: inputs resident in HBM (142 MB > L2)
+    launches0 = ctx.stats()["kernel_launches"]
+    ctx.profile(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    gpu_launches = ctx.stats()["kernel_launches"] - launches0
+    n3, ms3 = ctx.profile_read(lg.PROF_TC_3X3)
+    nh, msh = ctx.profile_read(lg.PROF_TC_HEAD)
+    nf, msf = ctx.profile_read(lg.PROF_TC_FIRST)
+    no, mso = ctx.profile_read(lg.PROF_OTHER)
+    ctx.profile(False)
+    ms_max = max_over_ranks(ms, world)
+    value = world * POSITIONS * args.steps / (ms_max / 1e3)
+    if args.profile_run:
+        ctx.close()
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "value": value}), flush=True)
+        return
+
+    # ---------------- e2e: host buffers through lg_policy / lg_value
+    host_p = np.ascontiguousarray(planes_p)
+    host_v = np.ascontiguousarray(planes_v)
+    ctx.policy(host_p[:BATCH])
+    ctx.value(host_v[:BATCH])
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        probs = ctx.policy(host_p)
+        vals = ctx.value(host_v)
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": world * POSITIONS * e2e_steps / t_e2e, "unit": "positions/s",
+           "h2d_bytes_per_step": int(host_p.nbytes + host_v.nbytes),
+           "d2h_bytes_per_step": int(probs.nbytes + vals.nbytes)}
+
+    extras = {}
+    if rank == 0:
+        extras = secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp)
+
+    if rank != 0:
+        ctx.close()
+        return
+    peak, hbm, peak_kind = read_peaks()
+    avg3 = ms3 / max(n3, 1) / 1e3
+    flop_launch = FLOP_3X3_PER_POS * BATCH
+    achieved = flop_launch / avg3 / 1e12 if n3 else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "tc_conv3x3_b256_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+    line = {
+        "metric": METRIC, "value": value, "unit": "positions/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic: 1024 seeded positions (reference feature gather) x 8 symmetries, "
+                "He-normal weights",
+        "config": {"workload": "config-1 policy+value nets (5x5 24->128, 11x 3x3 128->128, 1x1 "
+                               "head, ReLU, FC 361->256->1 tanh), BF16, batch 256",
+                   "batch": BATCH, "positions_per_step": POSITIONS, "precision": "bf16",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs 142 MB per step > L2 129 MB; no flush"},
+        "e2e": e2e,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "tc_conv_kernel<128,2,0> (3x3 128->128, batch 256)",
+                     "peak_source": f"bf16_tflops_sustained ({peak_kind})",
+                     "launches": n3, "avg_launch_us": avg3 * 1e6,
+                     "flop_per_launch": flop_launch},
+        "kernel_time_share": {
+            "tc_3x3": ms3, "tc_3x3_fused_head": msh, "tc_5x5_first": msf, "other": mso,
+            "launches": {"tc_3x3": n3, "tc_head": nh, "tc_first": nf, "other": no}},
+        "clocks": clk,
+        "gpu_launches": gpu_launches,
+        "pair_flop_rate_tflops": FLOP_PAIR_PER_POS * value / world / 1e12,
+    }
+    line.update(extras)
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(planes_p, planes_v, seconds=args.cpu_seconds)
+    ctx.close()
+    print(json.dumps(line), flush=True)
+
+
+def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp):
+    """FP32 batch-1 throughput, BF16 at the other batch sizes, and top-1
+    agreement with the FP64 oracle."""
+    import torch
+    out = {}
+    # FP32 plain path at batch 1 (policy + value per position).
+    with lg.Context(policy=lg.NetDesc.config1_policy(wp, "fp32"),
+                    value=lg.NetDesc.config1_value(wv, "fp32"), device=dev.index,
+                    max_batch=1) as c32:
+        n = 200
+        for i in range(5):
+            c32.policy(planes_p[i:i + 1])
+            c32.value(planes_v[i:i + 1])
+        t0 = time.perf_counter()
+        for i in range(n):
+            c32.policy(planes_p[i:i + 1])
+            c32.value(planes_v[i:i + 1])
+        host_rate = n / (time.perf_counter() - t0)
+        probs = torch.empty((1, 361), device=dev)
+        val = torch.empty(1, device=dev)
+        for i in range(5):
+            c32.policy_device(d_p[i].data_ptr(), 1, probs.data_ptr(), 1.0, None, sp)
+            c32.value_device(d_v[i].data_ptr(), 1, val.data_ptr(), sp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(n):
+            c32.policy_device(d_p[i].data_ptr(), 1, probs.data_ptr(), 1.0, None, sp)
+            c32.value_device(d_v[i].data_ptr(), 1, val.data_ptr(), sp)
+        e1.record()
+        torch.cuda.synchronize()
+        dev_rate = n / (e0.elapsed_time(e1) / 1e3)
+    out["fp32_plain_batch1"] = {"host_api_positions_per_s": host_rate,
+                                "device_positions_per_s": dev_rate}
+    # BF16 at the other configured batch sizes (device-resident inputs).
+    by_batch = {}
+    for b in (1, 8, 64, 256):
+        with lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"),
+                        value=lg.NetDesc.config1_value(wv, "bf16"), device=dev.index,
+                        max_batch=b) as cb:
+            probs = torch.empty((b, 361), device=dev)
+            val = torch.empty(b, device=dev)
+            reps = max(4, min(200, 4096 // b))
+            for i in range(3):
+                cb.policy_device(d_p.data_ptr(), b, probs.data_ptr(), 1.0, None, sp)
+                cb.value_device(d_v.data_ptr(), b, val.data_ptr(), sp)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for i in range(reps):
+                off = (i * b) % (8192 - b + 1)
+                cb.policy_device(d_p[off].data_ptr(), b, probs.data_ptr(), 1.0, None, sp)
+                cb.value_device(d_v[off].data_ptr(), b, val.data_ptr(), sp)
+            e1.record()
+            torch.cuda.synchronize()
+            by_batch[str(b)] = b * reps / (e0.elapsed_time(e1) / 1e3)
+    out["bf16_by_batch_positions_per_s"] = by_batch
+    out["ratio_bf16_batched_vs_fp32_batch1"] = by_batch["256"] / dev_rate
+    # Top-1 agreement with the FP64 oracle (BF16 and FP8 weights), 256 positions.
+    from oracle import oracle as O
+    P, V = O.make_net(O.CFG_POLICY), O.make_net(O.CFG_VALUE)
+    idx = np.arange(0, 8192, 32)
+    O.enable_blas()
+    l64 = O.forward_f64(P, wp, planes_p[idx])
+    v64 = O.forward_f64(V, wv, planes_v[idx])
+    O.disable_blas()
+    p64 = O.softmax_f64(l64, 1.0)
+    agree = {}
+    for prec in ("bf16", "fp8w"):
+        with lg.Context(policy=lg.NetDesc.config1_policy(wp, prec),
+                        value=lg.NetDesc.config1_value(wv, prec), device=dev.index,
+                        max_batch=256) as cq:
+            pr, lo = cq.policy(planes_p[idx], 1.0, return_logits=True)
+            vq = cq.value(planes_v[idx])
+        agree[prec] = {"top1": float((lo.argmax(1) == l64.argmax(1)).mean()),
+                       "prob_max_abs_err": float(np.abs(pr - p64).max()),
+                       "prob_mean_abs_err": float(np.abs(pr - p64).mean()),
+                       "value_max_abs_err": float(np.abs(vq - v64).max()),
+                       "value_mean_abs_err": float(np.abs(vq - v64).mean()),
+                       "positions": int(idx.size)}
+    out["vs_fp64_oracle"] = agree
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-run", action="store_true",
+                    help="only the device-resident warm-up and timed steps (for ncu)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -137,6 +137,21 @@ LG_API int lg_poll(lg_ctx *ctx, void **tags, int max, int timeout_us);
  * count their kernels), and batches served by the batching server. */
 LG_API int lg_stats(lg_ctx *ctx, long long *kernel_launches, long long *batches);
 
+/* Per-kernel timing for the roofline report.  lg_profile(ctx, 1) clears the
+ * counters and brackets every kernel launched by later device-pointer calls
+ * (lg_policy_device / lg_value_device) with CUDA events on the launching
+ * stream; lg_profile_read waits for those events and returns, for one kernel
+ * kind, the number of launches and their summed duration.  No reference
+ * counterpart (the reference prints only wall-clock p/s, Network.cpp:147-199). */
+#define LG_PROF_TC_3X3 0   /* tensor-core 3x3 trunk conv */
+#define LG_PROF_TC_HEAD 1  /* tensor-core 3x3 conv with the fused 1x1 head */
+#define LG_PROF_TC_FIRST 2 /* tensor-core 5x5 first layer */
+#define LG_PROF_FP32_CONV 3 /* FP32 conv (+ split-K reduction) */
+#define LG_PROF_OTHER 4    /* plane packing, head conv, softmax, value FC */
+#define LG_PROF_KINDS 5
+LG_API int lg_profile(lg_ctx *ctx, int enable);
+LG_API int lg_profile_read(lg_ctx *ctx, int kind, long long *launches, double *total_ms);
+
 /* Test hook (host-side fault injection): the n-th device call from now
  * (n >= 1) fails with LG_ERR_CUDA before it reaches the GPU; 0 disarms. */
 LG_API int lg_inject_fault(lg_ctx *ctx, int nth_call);

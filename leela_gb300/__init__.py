@@ -32,6 +32,7 @@ POINTS = 361
 LG_FP32, LG_BF16, LG_FP8W = 0, 1, 2
 LG_ACT_ELU, LG_ACT_RELU = 0, 1
 LG_NET_POLICY, LG_NET_VALUE = 0, 1
+PROF_TC_3X3, PROF_TC_HEAD, PROF_TC_FIRST, PROF_FP32_CONV, PROF_OTHER = range(5)
 PRECISIONS = {"fp32": LG_FP32, "bf16": LG_BF16, "fp8w": LG_FP8W, "fp8": LG_FP8W}
 
 ERRORS = {-1: "bad argument", -2: "allocation failed", -3: "CUDA error", -4: "timeout",
@@ -55,7 +56,7 @@ _lib_lock = threading.Lock()
 
 EXPORTS = ["lg_weight_count", "lg_create", "lg_destroy", "lg_last_error", "lg_policy",
            "lg_value", "lg_policy_device", "lg_value_device", "lg_submit", "lg_poll",
-           "lg_stats", "lg_inject_fault"]
+           "lg_stats", "lg_inject_fault", "lg_profile", "lg_profile_read"]
 
 
 def library():
@@ -82,6 +83,8 @@ def library():
             L.lg_poll.argtypes = [vp, P(vp), i32, i32]
             L.lg_stats.argtypes = [vp, P(ctypes.c_longlong), P(ctypes.c_longlong)]
             L.lg_inject_fault.argtypes = [vp, i32]
+            L.lg_profile.argtypes = [vp, i32]
+            L.lg_profile_read.argtypes = [vp, i32, P(ctypes.c_longlong), P(ctypes.c_double)]
             _lib = L
     return _lib
 
@@ -214,6 +217,14 @@ class Context:
         a, b = ctypes.c_longlong(), ctypes.c_longlong()
         _check(library().lg_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
         return {"kernel_launches": a.value, "batches": b.value}
+
+    def profile(self, enable: bool = True):
+        _check(library().lg_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self, kind: int):
+        n, ms = ctypes.c_longlong(), ctypes.c_double()
+        _check(library().lg_profile_read(self._h, kind, ctypes.byref(n), ctypes.byref(ms)))
+        return n.value, ms.value
 
     def inject_fault(self, nth_call: int):
         _check(library().lg_inject_fault(self._h, nth_call))

@@ -224,15 +224,26 @@ __device__ float block_reduce(float v, bool is_max, float *red) {
     return r;
 }
 
+// The head output of one point: the sum of `nparts` partial sums (the
+// tensor-core path splits the 1x1 head's channel sum over TMEM lane
+// quarters), plus the head bias, then the head activation if any.
+__device__ __forceinline__ float head_value(const HeadIn &h, int b, int p) {
+    size_t i = (size_t)b * kPoints + p;
+    float s = h.parts[i];
+    for (int k = 1; k < h.nparts; ++k) s += h.parts[(size_t)k * h.part_stride + i];
+    s += h.head_b;
+    return h.head_act ? act_fn(s, h.act) : s;
+}
+
 // Network.cpp:450-469 per board: alpha = max/T; p = exp(x/T - alpha)/sum.
-__global__ void __launch_bounds__(384) softmax_kernel(const float *__restrict__ logits, int B,
-                                                      float temperature,
+__global__ void __launch_bounds__(384) softmax_kernel(const HeadIn h, int B, float temperature,
                                                       float *__restrict__ probs) {
     __shared__ float red[32];
     int b = blockIdx.x;
     if (b >= B) return;
     int p = threadIdx.x;
-    float x = (p < kPoints) ? logits[(size_t)b * kPoints + p] : -FLT_MAX;
+    float x = (p < kPoints) ? head_value(h, b, p) : -FLT_MAX;
+    if (h.logits_out && p < kPoints) h.logits_out[(size_t)b * kPoints + p] = x;
     float mx = block_reduce<384>(x, true, red);
     float alpha = mx / temperature;
     float e = (p < kPoints) ? expf((x / temperature) - alpha) : 0.0f;
@@ -242,7 +253,7 @@ __global__ void __launch_bounds__(384) softmax_kernel(const float *__restrict__ 
 
 // innerproduct<361,H> (+act) then innerproduct<H,1>, then tanh or (1+tanh)/2
 // (Network.cpp:395-423, 733-737).  w1t is W1 transposed to [361][H].
-__global__ void __launch_bounds__(256) value_fc_kernel(const float *__restrict__ x361, int B,
+__global__ void __launch_bounds__(256) value_fc_kernel(const HeadIn h, int B,
                                                        const float *__restrict__ w1t,
                                                        const float *__restrict__ b1,
                                                        const float *__restrict__ w2, float b2,
@@ -252,14 +263,18 @@ __global__ void __launch_bounds__(256) value_fc_kernel(const float *__restrict__
     __shared__ float red[32];
     int b = blockIdx.x;
     if (b >= B) return;
-    for (int i = threadIdx.x; i < kPoints; i += blockDim.x) xs[i] = x361[(size_t)b * kPoints + i];
+    for (int i = threadIdx.x; i < kPoints; i += blockDim.x) {
+        float x = head_value(h, b, i);
+        xs[i] = x;
+        if (h.logits_out) h.logits_out[(size_t)b * kPoints + i] = x;
+    }
     __syncthreads();
     float part = 0.0f;
     for (int o = threadIdx.x; o < H; o += blockDim.x) {
         float s = 0.0f;
         for (int i = 0; i < kPoints; ++i) s = fmaf(w1t[(size_t)i * H + o], xs[i], s);
-        float h = act_fn(b1[o] + s, act);
-        part = fmaf(w2[o], h, part);
+        float hv = act_fn(b1[o] + s, act);
+        part = fmaf(w2[o], hv, part);
     }
     float tot = block_reduce<256>(part, false, red);
     if (threadIdx.x == 0) {
@@ -324,13 +339,13 @@ void launch_head_conv_f32(const float *in, const float *wh, float bias, int B, i
     head_conv_f32<<<blocks, 256, 0, s>>>(in, wh, bias, B, C, k, do_act, act, logits);
 }
 
-void launch_softmax(const float *logits, int B, float temperature, float *probs, cudaStream_t s) {
-    softmax_kernel<<<B, 384, 0, s>>>(logits, B, temperature, probs);
+void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s) {
+    softmax_kernel<<<B, 384, 0, s>>>(h, B, temperature, probs);
 }
 
-void launch_value_fc(const float *x361, int B, const float *w1t, const float *b1, const float *w2,
+void launch_value_fc(const HeadIn &h, int B, const float *w1t, const float *b1, const float *w2,
                      float b2, int H, int act, int value_map, float *value, cudaStream_t s) {
-    value_fc_kernel<<<B, 256, 0, s>>>(x361, B, w1t, b1, w2, b2, H, act, value_map, value);
+    value_fc_kernel<<<B, 256, 0, s>>>(h, B, w1t, b1, w2, b2, H, act, value_map, value);
 }
 
 }  // namespace lg

@@ -120,11 +120,19 @@ struct lg_ctx {
     // shared
     uint8_t *d_planes = nullptr;
     float *d_logits = nullptr, *d_probs = nullptr, *d_value = nullptr;
+    float *d_parts = nullptr;  // fused-head partial sums, [4][max_batch * 361]
     uint8_t *h_planes = nullptr;
     float *h_out = nullptr, *h_out2 = nullptr;
     int planes_c = 0;
     std::mutex mu;
     std::map<std::tuple<int, int, uint32_t, int>, std::pair<cudaGraphExec_t, int>> graphs;
+    // Per-kernel timing (device-pointer calls only): CUDA events around each
+    // launch on the launching stream, resolved by lg_profile_read.
+    bool profiling = false;
+    std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>> prof_pending;
+    std::vector<cudaEvent_t> event_pool;
+    long long prof_launches[LG_PROF_KINDS] = {};
+    double prof_ms[LG_PROF_KINDS] = {};
     std::atomic<long long> launches{0};
     std::atomic<long long> batches{0};
     std::atomic<int> fault_in{0};
@@ -327,16 +335,52 @@ int check_fault(lg_ctx *c) {
 
 // ------------------------------------------------------------ forward
 
+cudaEvent_t pool_event(lg_ctx *c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Brackets one kernel launch with events when profiling is on.
+struct ProfScope {
+    lg_ctx *c;
+    int kind;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(lg_ctx *c_, bool on, int kind_, cudaStream_t s_) : c(on ? c_ : nullptr), kind(kind_), s(s_) {
+        if (c) {
+            a = pool_event(c);
+            b = pool_event(c);
+            cudaEventRecord(a, s);
+        }
+    }
+    ~ProfScope() {
+        if (c) {
+            cudaEventRecord(b, s);
+            c->prof_pending.emplace_back(kind, a, b);
+        }
+    }
+};
+
 int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
-                 float *logits_out, float *value, cudaStream_t s, int *nlaunch) {
+                 float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof) {
     const lg_net_desc &d = n.d;
     int L = 0;
-    launch_pack_planes_f32(planes, B, d.c_in, c->act[0], s);
+    {
+        ProfScope ps(c, prof, LG_PROF_OTHER, s);
+        launch_pack_planes_f32(planes, B, d.c_in, c->act[0], s);
+    }
     ++L;
     int cur = 0;
     int ntrunk = (int)n.shapes.size() - 1;
     for (int l = 0; l < ntrunk; ++l) {
         auto sh = n.shapes[l];
+        ProfScope ps(c, prof, LG_PROF_FP32_CONV, s);
         launch_conv_f32(c->act[cur], n.wt[l], n.bias[l], c->act[cur ^ 1], B, sh.cin, sh.cout, sh.k,
                         d.act, c->partial, s);
         L += conv_f32_partial_floats(B, sh.cin, sh.cout, sh.k) ? 2 : 1;
@@ -344,12 +388,18 @@ int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float
     }
     auto hs = n.shapes.back();
     float *lg = logits_out ? logits_out : c->d_logits;
-    launch_head_conv_f32(c->act[cur], n.head_w, n.head_b, B, hs.cin, hs.k, d.act_head, d.act, lg, s);
+    {
+        ProfScope ps(c, prof, LG_PROF_OTHER, s);
+        launch_head_conv_f32(c->act[cur], n.head_w, n.head_b, B, hs.cin, hs.k, d.act_head, d.act, lg, s);
+    }
     ++L;
-    if (!d.value_head) {
-        launch_softmax(lg, B, T, probs, s);
-    } else {
-        launch_value_fc(lg, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value, s);
+    {
+        ProfScope ps(c, prof, LG_PROF_OTHER, s);
+        HeadIn h{lg, 1, 0, 0.0f, 0, d.act, nullptr};
+        if (!d.value_head)
+            launch_softmax(h, B, T, probs, s);
+        else
+            launch_value_fc(h, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value, s);
     }
     ++L;
     *nlaunch = L;
@@ -357,49 +407,50 @@ int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float
 }
 
 int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
-               float *logits_out, float *value, cudaStream_t s, int *nlaunch) {
+               float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof) {
     const lg_net_desc &d = n.d;
     int L = 0;
     const TcConv &first = n.tc[0];
-    launch_pack_planes_l5(planes, B, d.c_in, first.halves, c->l5, s);
+    {
+        ProfScope ps(c, prof, LG_PROF_OTHER, s);
+        launch_pack_planes_l5(planes, B, d.c_in, first.halves, c->l5, s);
+    }
     ++L;
     float *lg = logits_out ? logits_out : c->d_logits;
+    const size_t part_stride = (size_t)B * kPoints;
     int cur = 0;
     for (size_t l = 0; l < n.tc.size(); ++l) {
         const TcConv &t = n.tc[l];
+        const bool last = l + 1 == n.tc.size();
         TcLayer tl{};
-        bool last = l + 1 == n.tc.size();
-        int rows = (l == 0) ? B * kL5Board : B * kL3Board;
-        const void *in = (l == 0) ? (const void *)c->l5 : (const void *)c->l3[cur];
-        int rc = encode_map_2d_bf16(&tl.in_map, in, (uint64_t)t.halves * 64, (uint64_t)rows, 64,
-                                    (l == 0) ? 128 + 80 : 128 + 48);
-        if (rc) return rc;
-        rc = encode_map_2d_bf16(&tl.w_map, t.w, 64, (uint64_t)t.ntaps * t.halves * t.cout, 64,
-                                (uint32_t)t.cout);
-        if (rc) return rc;
+        tl.in = (l == 0) ? (const void *)c->l5 : (const void *)c->l3[cur];
+        tl.w = t.w;
         tl.bias = t.bias;
         tl.scale = t.scale;
         tl.head_w = last ? n.tc_head_w : nullptr;
-        tl.head_b = n.head_b;
-        tl.head_act = d.act_head;
         tl.act = d.act;
         tl.cin_halves = t.halves;
         tl.n = t.cout;
-        tl.ntaps = t.ntaps;
         tl.in_kind = (l == 0) ? 1 : 0;
-        tl.rows = rows;
-        tl.boards = B;
+        tl.rows = (l == 0) ? B * kL5Board : B * kL3Board;
         __nv_bfloat16 *out = (l == 0) ? c->l3[0] : c->l3[cur ^ 1];
-        rc = launch_tc_conv(tl, last ? nullptr : out, last ? lg : nullptr, c->d_err, s,
-                            c->sm_count);
+        int rc;
+        {
+            ProfScope ps(c, prof, l == 0 ? LG_PROF_TC_FIRST : (last ? LG_PROF_TC_HEAD : LG_PROF_TC_3X3), s);
+            rc = launch_tc_conv(tl, last ? nullptr : out, last ? c->d_parts : nullptr, part_stride,
+                                c->d_err, s, c->sm_count);
+        }
         if (rc) return rc;
         ++L;
         if (l > 0) cur ^= 1;
     }
-    if (!d.value_head) {
-        launch_softmax(lg, B, T, probs, s);
-    } else {
-        launch_value_fc(lg, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value, s);
+    {
+        ProfScope ps(c, prof, LG_PROF_OTHER, s);
+        HeadIn h{c->d_parts, tc_head_parts(d.width), part_stride, n.head_b, d.act_head, d.act, lg};
+        if (!d.value_head)
+            launch_softmax(h, B, T, probs, s);
+        else
+            launch_value_fc(h, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value, s);
     }
     ++L;
     *nlaunch = L;
@@ -407,10 +458,11 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
 }
 
 int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
-            float *logits, float *value, cudaStream_t s, int *nlaunch) {
+            float *logits, float *value, cudaStream_t s, int *nlaunch, bool prof = false) {
     Net &n = c->nets[net];
-    if (n.d.precision == LG_FP32) return forward_fp32(c, n, planes, B, T, probs, logits, value, s, nlaunch);
-    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch);
+    if (n.d.precision == LG_FP32)
+        return forward_fp32(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof);
+    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof);
 }
 
 // Host call: copy planes in, run (through a cached CUDA graph of
@@ -507,7 +559,7 @@ int run_device(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float 
         rc = forward(c, net, planes + (size_t)b0 * per_in, nb, T,
                      probs ? probs + (size_t)b0 * kPoints : nullptr,
                      logits ? logits + (size_t)b0 * kPoints : nullptr, value ? value + b0 : nullptr,
-                     s, &nl);
+                     s, &nl, c->profiling);
         if (rc) return rc;
         c->launches += nl;
         cudaError_t e = cudaGetLastError();
@@ -613,6 +665,11 @@ extern "C" void lg_destroy(lg_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &g : c->graphs) cudaGraphExecDestroy(g.second.first);
+    for (auto &t : c->prof_pending) {
+        cudaEventDestroy(std::get<1>(t));
+        cudaEventDestroy(std::get<2>(t));
+    }
+    for (auto e : c->event_pool) cudaEventDestroy(e);
     for (void *p : c->allocs) cudaFree(p);
     if (c->h_planes) cudaFreeHost(c->h_planes);
     if (c->h_out) cudaFreeHost(c->h_out);
@@ -696,7 +753,8 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
     if ((rc = dev_alloc(c, &c->d_planes, mb * max_c_in * kPoints)) ||
         (rc = dev_alloc(c, &c->d_logits, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_probs, mb * kPoints)) ||
-        (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)))
+        (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)) ||
+        (rc = dev_alloc(c, &c->d_parts, 4 * mb * kPoints)))
         return fail(rc);
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(LG_ERR_CUDA);
     if (cudaMallocHost(&c->h_planes, mb * max_c_in * kPoints) != cudaSuccess ||
@@ -811,5 +869,43 @@ extern "C" int lg_stats(lg_ctx *c, long long *kernel_launches, long long *batche
 extern "C" int lg_inject_fault(lg_ctx *c, int nth_call) {
     if (!c || nth_call < 0) return LG_ERR_ARG;
     c->fault_in = nth_call;
+    return LG_OK;
+}
+
+extern "C" int lg_profile(lg_ctx *c, int enable) {
+    if (!c) return LG_ERR_ARG;
+    std::lock_guard<std::mutex> g(c->mu);
+    c->profiling = enable != 0;
+    for (int k = 0; k < LG_PROF_KINDS; ++k) {
+        c->prof_launches[k] = 0;
+        c->prof_ms[k] = 0.0;
+    }
+    for (auto &t : c->prof_pending) {
+        c->event_pool.push_back(std::get<1>(t));
+        c->event_pool.push_back(std::get<2>(t));
+    }
+    c->prof_pending.clear();
+    return LG_OK;
+}
+
+extern "C" int lg_profile_read(lg_ctx *c, int kind, long long *launches, double *total_ms) {
+    if (!c || kind < 0 || kind >= LG_PROF_KINDS) {
+        lg_set_error("lg_profile_read: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    for (auto &t : c->prof_pending) {
+        cudaEvent_t a = std::get<1>(t), b = std::get<2>(t);
+        LG_CUDA_TRY(cudaEventSynchronize(b));
+        float ms = 0.0f;
+        LG_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+        c->prof_launches[std::get<0>(t)] += 1;
+        c->prof_ms[std::get<0>(t)] += ms;
+        c->event_pool.push_back(a);
+        c->event_pool.push_back(b);
+    }
+    c->prof_pending.clear();
+    if (launches) *launches = c->prof_launches[kind];
+    if (total_ms) *total_ms = c->prof_ms[kind];
     return LG_OK;
 }

@@ -13,8 +13,20 @@ void launch_conv_f32(const float *in, const float *wt, const float *bias, float 
                      int C, int O, int k, int act, float *partial, cudaStream_t s);
 void launch_head_conv_f32(const float *in, const float *wh, float bias, int B, int C, int k,
                           int do_act, int act, float *logits, cudaStream_t s);
-void launch_softmax(const float *logits, int B, float temperature, float *probs, cudaStream_t s);
-void launch_value_fc(const float *x361, int B, const float *w1t, const float *b1, const float *w2,
+// Input of the finish kernels: the head output of point (b, p) is
+//   act_head?(sum_k parts[k * part_stride + b * 361 + p] + head_b).
+// When logits_out is set the finish kernel also writes that value there.
+struct HeadIn {
+    const float *parts;
+    int nparts;
+    size_t part_stride;
+    float head_b;
+    int head_act;
+    int act;
+    float *logits_out;
+};
+void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s);
+void launch_value_fc(const HeadIn &h, int B, const float *w1t, const float *b1, const float *w2,
                      float b2, int H, int act, int value_map, float *value, cudaStream_t s);
 
 // ------------------------------------------------- tensor-core (tcgen05) path
@@ -23,28 +35,29 @@ void launch_value_fc(const float *x361, int B, const float *w1t, const float *b1
 // activation rows (L3 or L5 layout), N = output channels, K = taps x input
 // channels.  See tc_conv.cu.
 struct TcLayer {
-    CUtensorMap in_map;   // activations: [rows][cin] BF16, box {64, window rows}
-    CUtensorMap w_map;    // weights: [taps * halves * N][64] BF16, box {64, N}
-    const float *bias;    // [N]
-    const float *scale;   // [N] per-output-channel weight scale (FP8 weights), or null
-    const float *head_w;  // [N] fused 1x1 head weights (last trunk layer), or null
-    float head_b;
-    int head_act;         // 1: activation after the fused head
+    const void *in;       // activations: [rows][cin_halves*64] BF16 (L3 or L5 rows)
+    const void *w;        // weights: [taps][cin_halves][n][64] BF16
+    const float *bias;    // [n]
+    const float *scale;   // [n] per-output-channel weight scale (FP8 weights), or null
+    const float *head_w;  // [n] fused 1x1 head weights (last trunk layer), or null;
+                          // the fused head writes raw channel sums (no bias)
     int act;              // LG_ACT_*
     int cin_halves;       // input channels / 64
     int n;                // output channels (64 or 128)
-    int ntaps;            // 9 (3x3, L3 input) or 5 (expanded 5x5, L5 input)
-    int in_kind;          // 0: L3 input (3x3); 1: L5 input (5x5 first layer)
+    int in_kind;          // 0: L3 input (3x3); 1: L5 input (expanded 5x5 first layer)
     int rows;             // input rows processed (B * 400 or B * 399)
-    int boards;
 };
 
 // Expanded 5x5 input: planes [B][C][361] bytes -> L5 BF16 rows with
 // halves*64 channels: channel dx*C + c = plane c at (y, x + dx - 2).
 void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv_bfloat16 *out,
                            cudaStream_t s);
-int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *logits, int *err,
-                   cudaStream_t s, int sm_count);
+// Writes the layer output (L3 rows) or, for the fused head, head partial sums
+// into parts ([tc_head_parts(n)][boards*361]).  Returns LG_ERR_ARG if no
+// kernel covers the shape.
+int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *parts, size_t part_stride,
+                   int *err, cudaStream_t s, int sm_count);
+int tc_head_parts(int n);
 size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves);
 int tc_init_device();
 // Head kernels for the tensor-core path (logits already produced by the

@@ -18,9 +18,11 @@
 //                 (one tap x 64 input channels, ring of S stages)
 //   warp 1        TMEM owner and MMA issuer (one elected thread), M=128,
 //                 N=width, K=16 per instruction
-//   warps 2..5    epilogue: tcgen05.ld -> (x FP8 scale) + bias -> act ->
-//                 BF16 store, zeros on pad rows; or, for the last trunk
-//                 layer, the fused 1x1 head (dot with the head weights)
+//   warps 2..9    epilogue: tcgen05.ld -> (x FP8 scale) + bias -> act ->
+//                 BF16 store, zeros on pad rows.  Two warps per TMEM lane
+//                 quarter, each taking half of the output channels.  For the
+//                 last trunk layer the fused 1x1 head (dot with the head
+//                 weights) runs on warps 2..5 over all channels.
 // Accumulators are double-buffered in TMEM (2 x N columns), so the epilogue
 // of tile i overlaps the MMAs of tile i+1.
 //
@@ -32,22 +34,62 @@ namespace lg {
 
 using namespace ptx;
 
-constexpr int kTcThreads = 192;
+constexpr int kTcThreads = 320;
+constexpr int kEpiWarps = 8;
+// Kernel T: 2 control warps + 16 epilogue warps (4 per TMEM lane quarter).
+constexpr int kTcThreadsT = 576;
+constexpr int kEpiWarpsT = 16;
 constexpr uint32_t kWaitLimit = 1u << 26;
 
 struct TcParams {
     const float *bias;
     const float *scale;
     const float *head_w;
-    float head_b;
-    int head_act;
     int act;
     int rows;
     int ntiles;
     __nv_bfloat16 *out;
-    float *logits;
+    float *parts;
+    size_t part_stride;
     int *err;
 };
+
+__device__ __forceinline__ int tap_shift(int kind, int t) {
+    if (kind == 0) return (t / 3 - 1) * kL3Pitch + (t % 3 - 1);
+    return (t - 2) * kL5Pitch;
+}
+
+__device__ __forceinline__ float act_apply(float v, int act) {
+    if (act == LG_ACT_ELU) return (v > 0.0f) ? v : (expf(v) - 1.0f);
+    return fmaxf(v, 0.0f);
+}
+
+// Where flat input row q of a layer lands: output row in L3 (-1: none),
+// whether it is a board point, and the point index b*361 + y*19 + x.
+template <int KIND>
+__device__ __forceinline__ void row_target(int q, int rows, int &orow, bool &valid, int &point) {
+    orow = -1;
+    valid = false;
+    point = 0;
+    if (q >= rows) return;
+    if (KIND == 0) {
+        const int b = q / kL3Board, r = q % kL3Board, y = r / kL3Pitch, x = r % kL3Pitch;
+        orow = q;
+        valid = (x < kBoard && y < kBoard);
+        point = b * kPoints + y * kBoard + x;
+    } else {
+        const int b = q / kL5Board, r = q % kL5Board, y = r / kL5Pitch, x = r % kL5Pitch;
+        valid = y < kBoard;
+        orow = valid ? b * kL3Board + y * kL3Pitch + x : -1;
+        point = b * kPoints + y * kBoard + x;
+    }
+}
+
+// ===========================================================================
+// Kernel A: M = 128 flat rows (positions), N = output channels (any width a
+// multiple of 16 up to 256; used for 64-wide nets).  Weight slices stream
+// through a ring; the window of rows is the A operand.
+// ===========================================================================
 
 template <int N, int HALVES, int KIND>
 struct TcCfg {
@@ -66,16 +108,6 @@ struct TcCfg {
     static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
-__device__ __forceinline__ int tap_shift(int kind, int t) {
-    if (kind == 0) return (t / 3 - 1) * kL3Pitch + (t % 3 - 1);
-    return (t - 2) * kL5Pitch;
-}
-
-__device__ __forceinline__ float act_apply(float v, int act) {
-    if (act == LG_ACT_ELU) return (v > 0.0f) ? v : (expf(v) - 1.0f);
-    return fmaxf(v, 0.0f);
-}
-
 template <int N, int HALVES, int KIND, bool HEAD>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_conv_kernel(const __grid_constant__ CUtensorMap in_map,
@@ -90,6 +122,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __shared__ uint64_t acc_full[2], acc_empty[2];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
+    __shared__ float s_bias[N], s_scale[N], s_head[N];
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     if (tid == 0) {
@@ -97,7 +130,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mbar_init(&win_full[i], 1);
             mbar_init(&win_empty[i], 1);
             mbar_init(&acc_full[i], 1);
-            mbar_init(&acc_empty[i], 4);
+            mbar_init(&acc_empty[i], kEpiWarps);
         }
         for (int i = 0; i < C::S; ++i) {
             mbar_init(&w_full[i], 1);
@@ -107,6 +140,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         fence_mbar_init();
         prefetch_tensormap(&in_map);
         prefetch_tensormap(&w_map);
+    }
+    for (int i = tid; i < N; i += kTcThreads) {
+        s_bias[i] = p.bias[i];
+        s_scale[i] = p.scale ? p.scale[i] : 1.0f;
+        s_head[i] = HEAD ? p.head_w[i] : 0.0f;
     }
     if (warp == 1) tmem_alloc(&tmem_base, C::TMEM_COLS);
     __syncthreads();
@@ -187,64 +225,53 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else {
         // ------------------------------------------------ epilogue
         const int quarter = warp & 3;
+        const int chalf = (warp - 2) >> 2;
         const int row = quarter * 32 + lane;
+        constexpr int NCOLS = HEAD ? N : N / 2;
+        const bool active = HEAD ? (chalf == 0) : true;
+        const int cbase = HEAD ? 0 : chalf * (N / 2);
         int local = 0;
         for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag; tile += gridDim.x, ++local) {
             const int acc = local & 1;
             const uint32_t ak = (uint32_t)(local >> 1);
             if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(31); break; }
             tc_fence_after();
-            const int q = tile * 128 + row;
-            // Where this row goes: output row (L3) and board point.
-            bool valid = false;
-            int orow = -1, point = -1;
-            if (q < p.rows) {
-                if (KIND == 0) {
-                    const int b = q / kL3Board, r = q % kL3Board, y = r / kL3Pitch, x = r % kL3Pitch;
-                    orow = q;
-                    valid = (x < kBoard && y < kBoard);
-                    point = b * kPoints + y * kBoard + x;
-                } else {
-                    const int b = q / kL5Board, r = q % kL5Board, y = r / kL5Pitch, x = r % kL5Pitch;
-                    valid = y < kBoard;
-                    orow = valid ? b * kL3Board + y * kL3Pitch + x : -1;
-                    point = b * kPoints + y * kBoard + x;
-                }
-            }
-            const uint32_t t_row = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * N);
-            float head_sum = 0.0f;
+            if (active) {
+                int orow, point;
+                bool valid;
+                row_target<KIND>(tile * 128 + row, p.rows, orow, valid, point);
+                const uint32_t t_row =
+                    tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * N + cbase);
+                float head_sum = 0.0f;
 #pragma unroll 1
-            for (int c0 = 0; c0 < N; c0 += 16) {
-                uint32_t v[16];
-                tmem_ld16(t_row + c0, v);
-                tmem_ld_wait();
-                float f[16];
+                for (int c0 = 0; c0 < NCOLS; c0 += 32) {
+                    uint32_t v[32];
+                    tmem_ld32(t_row + c0, v);
+                    tmem_ld_wait();
+                    float f[32];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    float x = __uint_as_float(v[i]);
-                    if (p.scale) x *= __ldg(p.scale + c0 + i);
-                    f[i] = act_apply(x + __ldg(p.bias + c0 + i), p.act);
-                }
-                if (HEAD) {
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) head_sum = fmaf(f[i], __ldg(p.head_w + c0 + i), head_sum);
-                } else if (orow >= 0) {
-                    uint4 pk[2];
-                    uint32_t *w32 = reinterpret_cast<uint32_t *>(pk);
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        __nv_bfloat162 h2 = valid ? __floats2bfloat162_rn(f[2 * i], f[2 * i + 1])
-                                                  : __floats2bfloat162_rn(0.0f, 0.0f);
-                        w32[i] = *reinterpret_cast<uint32_t *>(&h2);
+                    for (int i = 0; i < 32; ++i) {
+                        const int c = cbase + c0 + i;
+                        f[i] = act_apply(fmaf(__uint_as_float(v[i]), s_scale[c], s_bias[c]), p.act);
                     }
-                    uint4 *dst = reinterpret_cast<uint4 *>(p.out + (size_t)orow * N + c0);
-                    dst[0] = pk[0];
-                    dst[1] = pk[1];
+                    if (HEAD) {
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) head_sum = fmaf(f[i], s_head[cbase + c0 + i], head_sum);
+                    } else if (orow >= 0) {
+                        uint4 pk[4];
+                        uint32_t *w32 = reinterpret_cast<uint32_t *>(pk);
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) {
+                            __nv_bfloat162 h2 = valid ? __floats2bfloat162_rn(f[2 * i], f[2 * i + 1])
+                                                      : __floats2bfloat162_rn(0.0f, 0.0f);
+                            w32[i] = *reinterpret_cast<uint32_t *>(&h2);
+                        }
+                        uint4 *dst = reinterpret_cast<uint4 *>(p.out + (size_t)orow * N + cbase + c0);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) dst[i] = pk[i];
+                    }
                 }
-            }
-            if (HEAD && valid) {
-                float x = head_sum + p.head_b;
-                p.logits[point] = p.head_act ? act_apply(x, p.act) : x;
+                if (HEAD && valid) p.parts[point] = head_sum;
             }
             tc_fence_before();
             __syncwarp();
@@ -268,6 +295,243 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     tc_fence_after();
     if (warp == 1) tmem_dealloc(tmem, C::TMEM_COLS);
+    if (warp == 1) tmem_relinquish();
+}
+
+// ===========================================================================
+// Kernel T ("transposed"): M = 128 output channels (the weight slice is the
+// A operand), N = 256 flat rows (the shifted window is the B operand).  A
+// tcgen05 MMA with M=128 needs N=256 to reach the tensor pipe's full rate
+// (N <= 128 is bound by the per-instruction time), so 128-wide layers run
+// here.  The D tile in TMEM is [channel lane][row column]: the epilogue warp
+// for lane quarter q owns channels 32q..32q+31 and stores, per row, one
+// 64-byte run of channels.
+// ===========================================================================
+
+template <int HALVES, int KIND>
+struct TcTCfg {
+    static constexpr int NTAPS = KIND == 0 ? 9 : 5;
+    static constexpr int TP = 256;  // rows per tile
+    static constexpr int WPRE = KIND == 0 ? 24 : 40;
+    static constexpr int WROWS = TP + 2 * WPRE;
+    static constexpr int SUBROWS = WROWS / 2;   // TMA box rows (<= 256)
+    static constexpr int WIN_HALF = WROWS * 128; // one 64-channel half of a window
+    static constexpr int NWIN = 3;               // ring of half-windows
+    static constexpr int WST_BYTES = 128 * 128;
+    static constexpr int BUDGET = 220 * 1024;
+    static constexpr int S_RAW = (BUDGET - NWIN * WIN_HALF) / WST_BYTES;
+    static constexpr int S = S_RAW > 8 ? 8 : S_RAW;
+    static constexpr int SMEM = 1024 + NWIN * WIN_HALF + S * WST_BYTES;
+    static_assert(SUBROWS % 8 == 0 && SUBROWS <= 256, "window sub-box");
+    static_assert(S >= 3, "not enough shared memory for the weight ring");
+    static_assert(SMEM <= 227 * 1024, "shared memory budget");
+};
+
+// 32 values per lane -> lane L holds the sum over the warp of value L
+// (31 shuffles: each step keeps the half of the values named by one lane bit).
+__device__ __forceinline__ float warp_transpose_sum(float (&a)[32], int lane) {
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const bool upper = (lane & w) != 0;
+#pragma unroll
+        for (int i = 0; i < w; ++i) {
+            float keep = upper ? a[i + w] : a[i];
+            float send = upper ? a[i] : a[i + w];
+            a[i] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+        }
+    }
+    return a[0];
+}
+
+template <int HALVES, int KIND, bool HEAD>
+__global__ void __launch_bounds__(kTcThreadsT, 1)
+    tc_convT_kernel(const __grid_constant__ CUtensorMap in_map,
+                    const __grid_constant__ CUtensorMap w_map, const TcParams p) {
+    using C = TcTCfg<HALVES, KIND>;
+    constexpr int NO = 128;  // output channels
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *win = smem;                          // NWIN x WIN_HALF
+    uint8_t *wst = smem + C::NWIN * C::WIN_HALF;  // S x WST_BYTES
+
+    __shared__ uint64_t win_full[C::NWIN], win_empty[C::NWIN], w_full[C::S], w_empty[C::S];
+    __shared__ uint64_t acc_full[2], acc_empty[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    if (tid == 0) {
+        for (int i = 0; i < C::NWIN; ++i) {
+            mbar_init(&win_full[i], 1);
+            mbar_init(&win_empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], kEpiWarpsT);
+        }
+        for (int i = 0; i < C::S; ++i) {
+            mbar_init(&w_full[i], 1);
+            mbar_init(&w_empty[i], 1);
+        }
+        abort_flag = 0;
+        fence_mbar_init();
+        prefetch_tensormap(&in_map);
+        prefetch_tensormap(&w_map);
+    }
+    if (warp == 1) tmem_alloc(&tmem_base, 512);
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    auto fail = [&](int code) {
+        atomicCAS(p.err, 0, code);
+        atomicExch(&abort_flag, 1);
+    };
+
+    // K order per tile: channel half h outer, tap t inner, so that half h of
+    // the next tile's window loads while half h+1 of this tile computes.
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            uint32_t g = 0, wn = 0;
+            for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag; tile += gridDim.x) {
+                const int row0 = tile * C::TP - C::WPRE;
+                for (int h = 0; h < HALVES; ++h, ++wn) {
+                    const int ws = wn % C::NWIN;
+                    const uint32_t wk = wn / C::NWIN;
+                    if (!mbar_wait(&win_empty[ws], (wk & 1) ^ 1, kWaitLimit)) { fail(41); goto done_producer; }
+                    mbar_arrive_expect_tx(&win_full[ws], C::WIN_HALF);
+                    for (int sb = 0; sb < 2; ++sb)
+                        tma_load_2d(win + ws * C::WIN_HALF + sb * C::SUBROWS * 128, &in_map,
+                                    &win_full[ws], h * 64, row0 + sb * C::SUBROWS);
+                    for (int t = 0; t < C::NTAPS; ++t, ++g) {
+                        const int s = g % C::S;
+                        const uint32_t k = g / C::S;
+                        if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(42); goto done_producer; }
+                        mbar_arrive_expect_tx(&w_full[s], C::WST_BYTES);
+                        tma_load_2d(wst + s * C::WST_BYTES, &w_map, &w_full[s], 0,
+                                    (t * HALVES + h) * NO);
+                    }
+                }
+            }
+        done_producer:;
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(128, C::TP);
+            uint32_t g = 0, wn = 0;
+            int local = 0;
+            for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag;
+                 tile += gridDim.x, ++local) {
+                const int acc = local & 1;
+                const uint32_t ak = (uint32_t)(local >> 1);
+                if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(51); break; }
+                tc_fence_after();
+                const uint32_t d_tmem = tmem + (uint32_t)(acc * C::TP);
+                bool first = true;
+                for (int h = 0; h < HALVES; ++h, ++wn) {
+                    const int ws = wn % C::NWIN;
+                    const uint32_t wk = wn / C::NWIN;
+                    if (!mbar_wait(&win_full[ws], wk & 1, kWaitLimit)) { fail(52); goto done_mma; }
+                    tc_fence_after();
+                    const uint32_t win_addr = smem_u32(win + ws * C::WIN_HALF);
+                    for (int t = 0; t < C::NTAPS; ++t, ++g) {
+                        const int s = g % C::S;
+                        const uint32_t k = g / C::S;
+                        if (!mbar_wait(&w_full[s], k & 1, kWaitLimit)) { fail(53); goto done_mma; }
+                        tc_fence_after();
+                        const uint32_t a_base = smem_u32(wst + s * C::WST_BYTES);
+                        const uint32_t b_base =
+                            win_addr + (uint32_t)(C::WPRE + tap_shift(KIND, t)) * 128u;
+#pragma unroll
+                        for (int kk = 0; kk < 4; ++kk) {
+                            mma_bf16(d_tmem, sdesc_sw128(a_base + kk * 32), sdesc_sw128(b_base + kk * 32),
+                                     idesc, first ? 0u : 1u);
+                            first = false;
+                        }
+                        mma_commit(&w_empty[s]);
+                    }
+                    mma_commit(&win_empty[ws]);
+                }
+                mma_commit(&acc_full[acc]);
+            }
+        done_mma:;
+        }
+    } else {
+        // ------------------------------------------------ epilogue
+        const int quarter = warp & 3;
+        const int rq = (warp - 2) >> 2;          // rows [rq*64, +64) of the tile
+        const int o = quarter * 32 + lane;       // this lane's output channel
+        const float bias = __ldg(p.bias + o);
+        const float scale = p.scale ? __ldg(p.scale + o) : 1.0f;
+        const float hw = HEAD ? __ldg(p.head_w + o) : 0.0f;
+        int local = 0;
+        for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag; tile += gridDim.x, ++local) {
+            const int acc = local & 1;
+            const uint32_t ak = (uint32_t)(local >> 1);
+            if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(61); break; }
+            tc_fence_after();
+            const uint32_t t_base = tmem + ((uint32_t)(quarter * 32) << 16) +
+                                    (uint32_t)(acc * C::TP + rq * 64);
+            const int q_base = tile * C::TP + rq * 64;
+            uint32_t v[2][32];
+            tmem_ld32(t_base, v[0]);
+            tmem_ld32(t_base + 32, v[1]);
+            tmem_ld_wait();
+            tc_fence_before();
+            __syncwarp();
+            // TMEM is read: release the accumulator before the stores.
+            if (lane == 0) mbar_arrive(&acc_empty[acc]);
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                float f[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) f[j] = act_apply(fmaf(__uint_as_float(v[c][j]), scale, bias), p.act);
+                if (HEAD) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) f[j] *= hw;
+                    const float sum = warp_transpose_sum(f, lane);
+                    int orow, point;
+                    bool valid;
+                    row_target<KIND>(q_base + c * 32 + lane, p.rows, orow, valid, point);
+                    if (valid) p.parts[(size_t)quarter * p.part_stride + point] = sum;
+                } else {
+                    // Lane j works out where row (c*32 + j) goes once; the warp
+                    // then walks the 32 rows with that code broadcast:
+                    // -1 = no output, >= 0 = board point row, <= -2 = pad
+                    // row -(code + 2) (written as zero).
+                    int orow, point;
+                    bool valid;
+                    row_target<KIND>(q_base + c * 32 + lane, p.rows, orow, valid, point);
+                    const int code = orow < 0 ? -1 : (valid ? orow : -(orow + 2));
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int cj = __shfl_sync(0xffffffffu, code, j);
+                        if (cj != -1) {
+                            const int r = cj >= 0 ? cj : -(cj + 2);
+                            p.out[(size_t)r * NO + o] = __float2bfloat16_rn(cj >= 0 ? f[j] : 0.0f);
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    __syncthreads();
+    if (abort_flag && tid == 0) {
+        for (int i = 0; i < C::NWIN; ++i) {
+            mbar_wait(&win_full[i], 0, 1u << 16);
+            mbar_wait(&win_full[i], 1, 1u << 16);
+        }
+        for (int i = 0; i < C::S; ++i) {
+            mbar_wait(&w_full[i], 0, 1u << 16);
+            mbar_wait(&w_full[i], 1, 1u << 16);
+        }
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) tmem_dealloc(tmem, 512);
     if (warp == 1) tmem_relinquish();
 }
 
@@ -313,11 +577,9 @@ void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv
 
 // ------------------------------------------------------------------ launch
 
-template <int N, int HALVES, int KIND, bool HEAD>
-static int set_attr() {
-    cudaError_t e = cudaFuncSetAttribute(tc_conv_kernel<N, HALVES, KIND, HEAD>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         TcCfg<N, HALVES, KIND>::SMEM);
+template <class K, int SMEM>
+static int set_attr(K kern) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
     if (e != cudaSuccess) {
         lg_set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
         return LG_ERR_CUDA;
@@ -325,74 +587,85 @@ static int set_attr() {
     return LG_OK;
 }
 
-template <int N, int HALVES, int KIND, bool HEAD>
-static int launch_impl(const TcLayer &L, const TcParams &p, cudaStream_t s, int sm_count) {
-    using Cfg = TcCfg<N, HALVES, KIND>;
-    int grid = std::min(p.ntiles, sm_count);
-    tc_conv_kernel<N, HALVES, KIND, HEAD><<<grid, kTcThreads, Cfg::SMEM, s>>>(L.in_map, L.w_map, p);
-    return LG_OK;
-}
-
 // Raises the dynamic shared-memory limit of every instantiation; called once
 // per device before any launch (and so before any stream capture).
 int tc_init_device() {
     int rc = 0;
-#define LG_TC_ATTR(N_, H_, K_)                                  \
-    if (!rc) rc = set_attr<N_, H_, K_, false>();                 \
-    if (!rc && K_ == 0) rc = set_attr<N_, H_, K_, true>();
-    LG_TC_ATTR(128, 2, 0)
-    LG_TC_ATTR(64, 1, 0)
-    LG_TC_ATTR(128, 2, 1)
-    LG_TC_ATTR(128, 3, 1)
-    LG_TC_ATTR(64, 2, 1)
-    LG_TC_ATTR(64, 3, 1)
-#undef LG_TC_ATTR
+#define LG_A(N_, H_, K_, HD_) \
+    if (!rc) rc = set_attr<decltype(&tc_conv_kernel<N_, H_, K_, HD_>), TcCfg<N_, H_, K_>::SMEM>(tc_conv_kernel<N_, H_, K_, HD_>);
+#define LG_T(H_, K_, HD_) \
+    if (!rc) rc = set_attr<decltype(&tc_convT_kernel<H_, K_, HD_>), TcTCfg<H_, K_>::SMEM>(tc_convT_kernel<H_, K_, HD_>);
+    LG_A(64, 1, 0, false) LG_A(64, 1, 0, true) LG_A(64, 2, 1, false) LG_A(64, 3, 1, false)
+    LG_A(128, 3, 1, false)
+    LG_T(2, 0, false) LG_T(2, 0, true) LG_T(2, 1, false)
+#undef LG_A
+#undef LG_T
     return rc;
 }
 
-template <int N, int HALVES, int KIND>
-static int dispatch(const TcLayer &L, const TcParams &p, bool head, cudaStream_t s, int sm_count) {
-    if constexpr (KIND == 0) {
-        if (head) return launch_impl<N, HALVES, KIND, true>(L, p, s, sm_count);
-    } else if (head) {
-        lg_set_error("the fused head needs a 3x3 (L3) layer");
-        return LG_ERR_ARG;
-    }
-    return launch_impl<N, HALVES, KIND, false>(L, p, s, sm_count);
+int tc_head_parts(int n) { return n == 128 ? 4 : 1; }
+
+template <int N, int HALVES, int KIND, bool HEAD>
+static int launch_a(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) {
+    using Cfg = TcCfg<N, HALVES, KIND>;
+    CUtensorMap in_map, w_map;
+    int rc = encode_map_2d_bf16(&in_map, L.in, (uint64_t)HALVES * 64, (uint64_t)L.rows, 64, Cfg::WROWS);
+    if (!rc) rc = encode_map_2d_bf16(&w_map, L.w, 64, (uint64_t)Cfg::NTAPS * HALVES * N, 64, N);
+    if (rc) return rc;
+    p.ntiles = (L.rows + 127) / 128;
+    int grid = std::min(p.ntiles, sm_count);
+    tc_conv_kernel<N, HALVES, KIND, HEAD><<<grid, kTcThreads, Cfg::SMEM, s>>>(in_map, w_map, p);
+    return LG_OK;
+}
+
+template <int HALVES, int KIND, bool HEAD>
+static int launch_t(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) {
+    using Cfg = TcTCfg<HALVES, KIND>;
+    CUtensorMap in_map, w_map;
+    int rc = encode_map_2d_bf16(&in_map, L.in, (uint64_t)HALVES * 64, (uint64_t)L.rows, 64, Cfg::SUBROWS);
+    if (!rc) rc = encode_map_2d_bf16(&w_map, L.w, 64, (uint64_t)Cfg::NTAPS * HALVES * 128, 64, 128);
+    if (rc) return rc;
+    p.ntiles = (L.rows + Cfg::TP - 1) / Cfg::TP;
+    int grid = std::min(p.ntiles, sm_count);
+    tc_convT_kernel<HALVES, KIND, HEAD><<<grid, kTcThreadsT, Cfg::SMEM, s>>>(in_map, w_map, p);
+    return LG_OK;
 }
 
 size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves) {
-    if (ntaps == 9) return n == 128 ? TcCfg<128, 2, 0>::SMEM : TcCfg<64, 1, 0>::SMEM;
-    return cin_halves == 2 ? TcCfg<128, 2, 1>::SMEM : TcCfg<128, 3, 1>::SMEM;
+    if (n == 128 && cin_halves == 2) return ntaps == 9 ? TcTCfg<2, 0>::SMEM : TcTCfg<2, 1>::SMEM;
+    if (n == 128) return TcCfg<128, 3, 1>::SMEM;
+    return ntaps == 9 ? TcCfg<64, 1, 0>::SMEM : TcCfg<64, 2, 1>::SMEM;
 }
 
-int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *logits, int *err,
-                   cudaStream_t s, int sm_count) {
+int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *parts, size_t part_stride,
+                   int *err, cudaStream_t s, int sm_count) {
     TcParams p{};
     p.bias = L.bias;
     p.scale = L.scale;
     p.head_w = L.head_w;
-    p.head_b = L.head_b;
-    p.head_act = L.head_act;
     p.act = L.act;
     p.rows = L.rows;
-    p.ntiles = (L.rows + 127) / 128;
     p.out = out_l3;
-    p.logits = logits;
+    p.parts = parts;
+    p.part_stride = part_stride;
     p.err = err;
     const bool head = L.head_w != nullptr;
-    if (head && !logits) return LG_ERR_ARG;
-    if (!head && !out_l3) return LG_ERR_ARG;
-#define LG_TC_CASE(N_, H_, K_)                                                      \
-    if (L.n == N_ && L.cin_halves == H_ && L.in_kind == K_)                         \
-        return dispatch<N_, H_, K_>(L, p, head, s, sm_count);
-    LG_TC_CASE(128, 2, 0)
-    LG_TC_CASE(64, 1, 0)
-    LG_TC_CASE(128, 2, 1)
-    LG_TC_CASE(128, 3, 1)
-    LG_TC_CASE(64, 2, 1)
-    LG_TC_CASE(64, 3, 1)
-#undef LG_TC_CASE
+    if ((head && (!parts || L.in_kind != 0)) || (!head && !out_l3) || L.rows <= 0) {
+        lg_set_error("launch_tc_conv: bad layer arguments");
+        return LG_ERR_ARG;
+    }
+    if (L.n == 128 && L.cin_halves == 2 && L.in_kind == 0)
+        return head ? launch_t<2, 0, true>(L, p, s, sm_count) : launch_t<2, 0, false>(L, p, s, sm_count);
+    if (L.n == 128 && L.cin_halves == 2 && L.in_kind == 1 && !head)
+        return launch_t<2, 1, false>(L, p, s, sm_count);
+    if (L.n == 128 && L.cin_halves == 3 && L.in_kind == 1 && !head)
+        return launch_a<128, 3, 1, false>(L, p, s, sm_count);
+    if (L.n == 64 && L.cin_halves == 1 && L.in_kind == 0)
+        return head ? launch_a<64, 1, 0, true>(L, p, s, sm_count) : launch_a<64, 1, 0, false>(L, p, s, sm_count);
+    if (L.n == 64 && L.cin_halves == 2 && L.in_kind == 1 && !head)
+        return launch_a<64, 2, 1, false>(L, p, s, sm_count);
+    if (L.n == 64 && L.cin_halves == 3 && L.in_kind == 1 && !head)
+        return launch_a<64, 3, 1, false>(L, p, s, sm_count);
     lg_set_error("no tensor-core kernel for N=%d halves=%d kind=%d", L.n, L.cin_halves, L.in_kind);
     return LG_ERR_ARG;
 }

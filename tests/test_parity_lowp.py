@@ -98,3 +98,31 @@ def test_lowp_rejects_unsupported_shape(gpu_lib, weights):
     lg = gpu_lib
     with pytest.raises(lg.LeelaGPUError):
         lg.Context(policy=lg.NetDesc.reference_policy(weights["ref_p"][1], "bf16"), max_batch=4)
+
+
+@pytest.mark.parametrize("value_head", [0, 1])
+def test_bf16_64_wide_net(gpu_lib, oracle_mod, positions, value_head):
+    """64-wide nets (the distilled-net shape: 5x5 24->64, 5x 3x3 64->64, 1x1
+    head) run on the M=128-rows tensor-core kernel; same bars as above
+    against the FP64 oracle with BF16-rounded weights."""
+    lg, O = gpu_lib, oracle_mod
+    shape = dict(c_in=24, width1=64, width=64, n3x3=5, head_k=1, act=O.RELU, act_head=0,
+                 value_head=value_head, fc_hidden=64 if value_head else 0, value_map=0)
+    n = O.make_net(shape)
+    w = O.he_weights(n, 7)
+    src = positions["planes_v" if value_head else "planes_p"][:64, :24]
+    O.enable_blas()
+    try:
+        ref = O.forward_f64(n, O.quantize_weights(n, w, "bf16"), src)
+    finally:
+        O.disable_blas()
+    desc = lg.NetDesc(w, **shape, precision="bf16")
+    with lg.Context(policy=None if value_head else desc, value=desc if value_head else None,
+                    max_batch=64) as c:
+        if value_head:
+            v = c.value(src)
+            assert np.abs(v - ref).max() <= 3e-2
+        else:
+            _, logits = c.policy(src, 1.0, return_logits=True)
+            assert (logits.argmax(1) == ref.argmax(1)).mean() >= 0.95
+            assert rel_logit_err(logits, ref).max() <= 5e-2
