@@ -137,6 +137,27 @@ LG_API int lg_poll(lg_ctx *ctx, void **tags, int max, int timeout_us);
  * count their kernels), and batches served by the batching server. */
 LG_API int lg_stats(lg_ctx *ctx, long long *kernel_launches, long long *batches);
 
+/* FP32 policy forward that allocates nothing (no counterpart in the
+ * reference).  Same inputs, outputs and results as lg_policy_device on an
+ * FP32 policy net, for callers that cannot call cudaMalloc at evaluation
+ * time: a search thread in a process whose device memory is owned by
+ * another allocator, a latency path that must not absorb cudaMalloc /
+ * cudaFree's device-wide synchronisation, or a host callback where CUDA
+ * allocation is not allowed.  Its scratch (activations, split-K partial
+ * sums, logits when `logits` is NULL) is one static 8 MiB device array in
+ * the library, held by every GPU that loads it until the process exits.
+ *   - B is limited to 4 positions per call; larger B, or a net whose
+ *     scratch would not fit, is rejected with LG_ERR_ARG and a message.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream
+ *     capture.
+ *   - Every call, on every context, shares the one array: calls whose work
+ *     overlaps on the GPU (different streams, or different host threads
+ *     without ordering) race on it.  Nothing in it needs to start at zero.
+ * All pointers are device memory; work is enqueued on `stream`. */
+LG_API int lg_policy_device_static(lg_ctx *ctx, const uint8_t *planes, int B, float temperature,
+                                   float *probs, float *logits, void *stream);
+
 /* Per-kernel timing for the roofline report.  lg_profile(ctx, 1) clears the
  * counters and brackets every kernel launched by later device-pointer calls
  * (lg_policy_device / lg_value_device) with CUDA events on the launching

@@ -56,7 +56,8 @@ _lib_lock = threading.Lock()
 
 EXPORTS = ["lg_weight_count", "lg_create", "lg_destroy", "lg_last_error", "lg_policy",
            "lg_value", "lg_policy_device", "lg_value_device", "lg_submit", "lg_poll",
-           "lg_stats", "lg_inject_fault", "lg_profile", "lg_profile_read"]
+           "lg_stats", "lg_inject_fault", "lg_profile", "lg_profile_read",
+           "lg_policy_device_static"]
 
 
 def library():
@@ -84,6 +85,7 @@ def library():
             L.lg_stats.argtypes = [vp, P(ctypes.c_longlong), P(ctypes.c_longlong)]
             L.lg_inject_fault.argtypes = [vp, i32]
             L.lg_profile.argtypes = [vp, i32]
+            L.lg_policy_device_static.argtypes = [vp, vp, i32, f32, vp, vp, vp]
             L.lg_profile_read.argtypes = [vp, i32, P(ctypes.c_longlong), P(ctypes.c_double)]
             _lib = L
     return _lib
@@ -198,6 +200,14 @@ class Context:
                       logits_ptr: int | None = None, stream: int | None = None):
         _check(library().lg_policy_device(self._h, planes_ptr, B, temperature, probs_ptr,
                                           logits_ptr, stream))
+
+    def policy_device_static(self, planes_ptr: int, B: int, probs_ptr: int,
+                             temperature: float = 1.0, logits_ptr: int | None = None,
+                             stream: int | None = None):
+        """lg_policy_device_static: FP32 policy, B <= 4, scratch in the
+        library's static device array (no allocation)."""
+        _check(library().lg_policy_device_static(self._h, planes_ptr, B, temperature, probs_ptr,
+                                                 logits_ptr, stream))
 
     def value_device(self, planes_ptr: int, B: int, value_ptr: int, stream: int | None = None):
         _check(library().lg_value_device(self._h, planes_ptr, B, value_ptr, stream))

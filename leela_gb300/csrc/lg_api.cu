@@ -909,3 +909,108 @@ extern "C" int lg_profile_read(lg_ctx *c, int kind, long long *launches, double 
     if (total_ms) *total_ms = c->prof_ms[kind];
     return LG_OK;
 }
+
+// ============================================================================
+// FP32 policy forward with no allocation at call time.
+//
+// For callers that must not allocate device memory when they evaluate a
+// position: a search thread inside a process whose device memory belongs to
+// another allocator, code that must not hit cudaMalloc/cudaFree's implicit
+// device synchronisation in its latency path, or a host callback where CUDA
+// allocation calls are not allowed.  The conv layers' split-K partial sums,
+// the two activation buffers and the logits live in one file-scope device
+// array of kStaticScratchBytes, shared by every call on every context.
+// ============================================================================
+
+namespace {
+constexpr size_t kStaticScratchBytes = 8u << 20;  // 8 MiB, held by every GPU that loads this library
+constexpr int kStaticMaxBatch = 4;
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+void *g_static_ptr[kStaticMaxDevices] = {};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+extern "C" int lg_policy_device_static(lg_ctx *c, const uint8_t *planes, int B, float temperature,
+                                       float *probs, float *logits, void *stream) {
+    if (!c || !planes || !probs || !(temperature > 0.0f) || B < 0) {
+        lg_set_error("lg_policy_device_static: bad arguments");
+        return LG_ERR_ARG;
+    }
+    if (B > kStaticMaxBatch) {
+        lg_set_error("lg_policy_device_static: batch %d exceeds the static scratch limit of %d positions",
+                     B, kStaticMaxBatch);
+        return LG_ERR_ARG;
+    }
+    Net &n = c->nets[LG_NET_POLICY];
+    if (!n.present || n.d.precision != LG_FP32) {
+        lg_set_error("lg_policy_device_static: needs an FP32 policy net");
+        return LG_ERR_ARG;
+    }
+    if (B == 0) return LG_OK;
+    // Scratch layout: activations x2, split-K partials, logits.
+    size_t max_ch = (size_t)n.d.c_in, max_partial = 0;
+    for (auto &sh : n.shapes) {
+        max_ch = std::max(max_ch, (size_t)std::max(sh.cin, sh.cout));
+        max_partial = std::max(max_partial, conv_f32_partial_floats(B, sh.cin, sh.cout, sh.k));
+    }
+    const size_t act_bytes = align256((size_t)B * kPoints * max_ch * sizeof(float));
+    const size_t part_bytes = align256(max_partial * sizeof(float));
+    const size_t logit_bytes = align256((size_t)B * kPoints * sizeof(float));
+    const size_t need = 2 * act_bytes + part_bytes + logit_bytes;
+    if (need > kStaticScratchBytes) {
+        lg_set_error("lg_policy_device_static: this net needs %zu bytes of scratch at batch %d, the static "
+                     "array holds %zu",
+                     need, B, kStaticScratchBytes);
+        return LG_ERR_ARG;
+    }
+    if (c->device < 0 || c->device >= kStaticMaxDevices) {
+        lg_set_error("lg_policy_device_static: device %d out of range", c->device);
+        return LG_ERR_ARG;
+    }
+    LG_CUDA_TRY(cudaSetDevice(c->device));
+    void *base;
+    {
+        // Once per device, with that device current: the device address of
+        // the array (its name in host code is only a host-side stand-in).
+        std::lock_guard<std::mutex> g(g_static_mu);
+        if (!g_static_ptr[c->device]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+            if (e != cudaSuccess || !p) {
+                lg_set_error("cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
+                return LG_ERR_CUDA;
+            }
+            g_static_ptr[c->device] = p;
+        }
+        base = g_static_ptr[c->device];
+    }
+    unsigned char *b = static_cast<unsigned char *>(base);
+    float *act[2] = {reinterpret_cast<float *>(b), reinterpret_cast<float *>(b + act_bytes)};
+    float *partial = reinterpret_cast<float *>(b + 2 * act_bytes);
+    float *lg = logits ? logits : reinterpret_cast<float *>(b + 2 * act_bytes + part_bytes);
+    cudaStream_t s = (cudaStream_t)stream;
+    const lg_net_desc &d = n.d;
+    launch_pack_planes_f32(planes, B, d.c_in, act[0], s);
+    int cur = 0;
+    const int ntrunk = (int)n.shapes.size() - 1;
+    for (int l = 0; l < ntrunk; ++l) {
+        auto sh = n.shapes[l];
+        launch_conv_f32(act[cur], n.wt[l], n.bias[l], act[cur ^ 1], B, sh.cin, sh.cout, sh.k, d.act,
+                        partial, s);
+        cur ^= 1;
+    }
+    auto hs = n.shapes.back();
+    launch_head_conv_f32(act[cur], n.head_w, n.head_b, B, hs.cin, hs.k, d.act_head, d.act, lg, s);
+    HeadIn h{lg, 1, 0, 0.0f, 0, d.act, nullptr};
+    launch_softmax(h, B, temperature, probs, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        lg_set_error("lg_policy_device_static: launch failed: %s", cudaGetErrorString(e));
+        return LG_ERR_CUDA;
+    }
+    return LG_OK;
+}
