@@ -315,7 +315,7 @@ def run_ours(args, world, rank, local):
         "e2e": e2e,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "tc_conv_kernel<128,2,0> (3x3 128->128, batch 256)",
+                     "kernel": "tc_convT_kernel<2,0,0> (3x3 128->128, batch 256)",
                      "peak_source": f"bf16_tflops_sustained ({peak_kind})",
                      "launches": n3, "avg_launch_us": avg3 * 1e6,
                      "flop_per_launch": flop_launch},

@@ -252,35 +252,79 @@ __global__ void __launch_bounds__(384) softmax_kernel(const HeadIn h, int B, flo
 }
 
 // innerproduct<361,H> (+act) then innerproduct<H,1>, then tanh or (1+tanh)/2
-// (Network.cpp:395-423, 733-737).  w1t is W1 transposed to [361][H].
-__global__ void __launch_bounds__(256) value_fc_kernel(const HeadIn h, int B,
-                                                       const float *__restrict__ w1t,
-                                                       const float *__restrict__ b1,
-                                                       const float *__restrict__ w2, float b2,
-                                                       int H, int act, int value_map,
-                                                       float *__restrict__ value) {
-    __shared__ float xs[kPoints];
-    __shared__ float red[32];
-    int b = blockIdx.x;
+// (Network.cpp:395-423, 733-737), as a small tiled GEMM over boards:
+// value_fc1_kernel computes hidden = act(b1 + x361 . W1^T) for a tile of 32
+// boards x 64 hidden units (K = 361 staged through shared memory, the 361
+// head outputs formed on the fly from the head partial sums) and writes each
+// board's partial w2 . hidden over its 64 units; value_final_kernel adds the
+// partials in a fixed order, b2, and applies the value map.  w1t is W1
+// transposed to [361][H].
+constexpr int kFcBM = 16, kFcBN = 64, kFcBK = 32;
+
+__global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
+                                                        const float *__restrict__ w1t,
+                                                        const float *__restrict__ b1,
+                                                        const float *__restrict__ w2, int H,
+                                                        int act, float *__restrict__ part) {
+    __shared__ float Xs[kFcBK][kFcBM + 1];
+    __shared__ float Ws[kFcBK][kFcBN];
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;  // hidden tx + 16j (j<4), board ty
+    const int b0 = blockIdx.x * kFcBM, n0 = blockIdx.y * kFcBN;
+    float acc[1][4] = {};
+    for (int k0 = 0; k0 < kPoints; k0 += kFcBK) {
+        for (int i = tid; i < kFcBK * kFcBM; i += 256) {
+            const int kk = i % kFcBK, bb = i / kFcBK;  // consecutive threads read consecutive points
+            const int b = b0 + bb, k = k0 + kk;
+            float x = 0.0f;
+            if (b < B && k < kPoints) {
+                x = head_value(h, b, k);
+                if (h.logits_out && blockIdx.y == 0) h.logits_out[(size_t)b * kPoints + k] = x;
+            }
+            Xs[kk][bb] = x;
+        }
+        for (int i = tid; i < kFcBK * kFcBN; i += 256) {
+            const int kk = i / kFcBN, n = i % kFcBN;
+            const int k = k0 + kk;
+            Ws[kk][n] = (k < kPoints && n0 + n < H) ? w1t[(size_t)k * H + n0 + n] : 0.0f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < kFcBK; ++kk) {
+            float w[4];
+            const float a = Xs[kk][ty];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) w[j] = Ws[kk][tx + 16 * j];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[0][j] = fmaf(a, w[j], acc[0][j]);
+        }
+        __syncthreads();
+    }
+    // Partial second FC over this CTA's hidden units, reduced over the 16
+    // threads (tx) that share a board.
+#pragma unroll
+    for (int i = 0; i < 1; ++i) {
+        float sum = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int n = n0 + tx + 16 * j;
+            if (n < H) sum = fmaf(w2[n], act_fn(b1[n] + acc[i][j], act), sum);
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        const int b = b0 + ty + 16 * i;
+        if (tx == 0 && b < B) part[(size_t)b * gridDim.y + blockIdx.y] = sum;
+    }
+}
+
+__global__ void value_final_kernel(const float *__restrict__ part, int nparts, int B, float b2,
+                                   int value_map, float *__restrict__ value) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
-    for (int i = threadIdx.x; i < kPoints; i += blockDim.x) {
-        float x = head_value(h, b, i);
-        xs[i] = x;
-        if (h.logits_out) h.logits_out[(size_t)b * kPoints + i] = x;
-    }
-    __syncthreads();
-    float part = 0.0f;
-    for (int o = threadIdx.x; o < H; o += blockDim.x) {
-        float s = 0.0f;
-        for (int i = 0; i < kPoints; ++i) s = fmaf(w1t[(size_t)i * H + o], xs[i], s);
-        float hv = act_fn(b1[o] + s, act);
-        part = fmaf(w2[o], hv, part);
-    }
-    float tot = block_reduce<256>(part, false, red);
-    if (threadIdx.x == 0) {
-        float t = tanhf(b2 + tot);
-        value[b] = value_map ? (1.0f + t) / 2.0f : t;
-    }
+    float s = 0.0f;
+    for (int k = 0; k < nparts; ++k) s += part[(size_t)b * nparts + k];
+    const float t = tanhf(b2 + s);
+    value[b] = value_map ? (1.0f + t) / 2.0f : t;
 }
 
 // ------------------------------------------------------------ host launchers
@@ -344,8 +388,13 @@ void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cud
 }
 
 void launch_value_fc(const HeadIn &h, int B, const float *w1t, const float *b1, const float *w2,
-                     float b2, int H, int act, int value_map, float *value, cudaStream_t s) {
-    value_fc_kernel<<<B, 256, 0, s>>>(h, B, w1t, b1, w2, b2, H, act, value_map, value);
+                     float b2, int H, int act, int value_map, float *value, float *part,
+                     cudaStream_t s) {
+    dim3 grid((B + kFcBM - 1) / kFcBM, (H + kFcBN - 1) / kFcBN);
+    value_fc1_kernel<<<grid, 256, 0, s>>>(h, B, w1t, b1, w2, H, act, part);
+    value_final_kernel<<<(B + 127) / 128, 128, 0, s>>>(part, (int)grid.y, B, b2, value_map, value);
 }
+
+size_t value_fc_part_floats(int B, int H) { return (size_t)B * ((H + kFcBN - 1) / kFcBN); }
 
 }  // namespace lg

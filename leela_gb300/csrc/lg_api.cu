@@ -121,6 +121,7 @@ struct lg_ctx {
     uint8_t *d_planes = nullptr;
     float *d_logits = nullptr, *d_probs = nullptr, *d_value = nullptr;
     float *d_parts = nullptr;  // fused-head partial sums, [4][max_batch * 361]
+    float *d_fcpart = nullptr; // value-head FC partial sums
     uint8_t *h_planes = nullptr;
     float *h_out = nullptr, *h_out2 = nullptr;
     int planes_c = 0;
@@ -399,9 +400,10 @@ int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float
         if (!d.value_head)
             launch_softmax(h, B, T, probs, s);
         else
-            launch_value_fc(h, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value, s);
+            launch_value_fc(h, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
+                            c->d_fcpart, s);
     }
-    ++L;
+    L += d.value_head ? 2 : 1;
     *nlaunch = L;
     return LG_OK;
 }
@@ -450,9 +452,10 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
         if (!d.value_head)
             launch_softmax(h, B, T, probs, s);
         else
-            launch_value_fc(h, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value, s);
+            launch_value_fc(h, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
+                            c->d_fcpart, s);
     }
-    ++L;
+    L += d.value_head ? 2 : 1;
     *nlaunch = L;
     return LG_OK;
 }
@@ -754,7 +757,8 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
         (rc = dev_alloc(c, &c->d_logits, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_probs, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)) ||
-        (rc = dev_alloc(c, &c->d_parts, 4 * mb * kPoints)))
+        (rc = dev_alloc(c, &c->d_parts, 4 * mb * kPoints)) ||
+        (rc = dev_alloc(c, &c->d_fcpart, value_fc_part_floats(max_batch, 4096))))
         return fail(rc);
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(LG_ERR_CUDA);
     if (cudaMallocHost(&c->h_planes, mb * max_c_in * kPoints) != cudaSuccess ||

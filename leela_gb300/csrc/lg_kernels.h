@@ -26,8 +26,12 @@ struct HeadIn {
     float *logits_out;
 };
 void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s);
+// Value head: two launches (tiled FC1 + partial FC2, then a fixed-order sum
+// and the value map); `part` holds value_fc_part_floats(B, H) floats.
 void launch_value_fc(const HeadIn &h, int B, const float *w1t, const float *b1, const float *w2,
-                     float b2, int H, int act, int value_map, float *value, cudaStream_t s);
+                     float b2, int H, int act, int value_map, float *value, float *part,
+                     cudaStream_t s);
+size_t value_fc_part_floats(int B, int H);
 
 // ------------------------------------------------- tensor-core (tcgen05) path
 //
@@ -65,6 +69,6 @@ int tc_init_device();
 
 // Tensor-map encoding through the driver entry point (no -lcuda needed).
 int encode_map_2d_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint64_t rows,
-                       uint32_t box_inner, uint32_t box_rows);
+                       uint32_t box_inner, uint32_t box_rows, bool swizzle128 = true);
 
 }  // namespace lg

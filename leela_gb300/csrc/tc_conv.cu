@@ -30,6 +30,8 @@
 // stops issuing work, drains what it issued and frees its TMEM.
 #include "lg_kernels.h"
 
+#include <cstring>
+
 namespace lg {
 
 using namespace ptx;
@@ -318,10 +320,16 @@ struct TcTCfg {
     static constexpr int WIN_HALF = WROWS * 128; // one 64-channel half of a window
     static constexpr int NWIN = 3;               // ring of half-windows
     static constexpr int WST_BYTES = 128 * 128;
+    // L3 outputs are contiguous rows: the epilogue stages 32 rows x 128
+    // channels per row group in shared memory and writes them with one TMA
+    // store.  (The first layer's L5 -> L3 row remap stores directly.)
+    static constexpr bool STAGED = KIND == 0;
+    static constexpr int STG_BYTES = 32 * 256;
+    static constexpr int STG_TOTAL = STAGED ? 4 * STG_BYTES : 0;
     static constexpr int BUDGET = 220 * 1024;
-    static constexpr int S_RAW = (BUDGET - NWIN * WIN_HALF) / WST_BYTES;
+    static constexpr int S_RAW = (BUDGET - NWIN * WIN_HALF - STG_TOTAL) / WST_BYTES;
     static constexpr int S = S_RAW > 8 ? 8 : S_RAW;
-    static constexpr int SMEM = 1024 + NWIN * WIN_HALF + S * WST_BYTES;
+    static constexpr int SMEM = 1024 + NWIN * WIN_HALF + STG_TOTAL + S * WST_BYTES;
     static_assert(SUBROWS % 8 == 0 && SUBROWS <= 256, "window sub-box");
     static_assert(S >= 3, "not enough shared memory for the weight ring");
     static_assert(SMEM <= 227 * 1024, "shared memory budget");
@@ -346,16 +354,18 @@ __device__ __forceinline__ float warp_transpose_sum(float (&a)[32], int lane) {
 template <int HALVES, int KIND, bool HEAD>
 __global__ void __launch_bounds__(kTcThreadsT, 1)
     tc_convT_kernel(const __grid_constant__ CUtensorMap in_map,
-                    const __grid_constant__ CUtensorMap w_map, const TcParams p) {
+                    const __grid_constant__ CUtensorMap w_map,
+                    const __grid_constant__ CUtensorMap out_map, const TcParams p) {
     using C = TcTCfg<HALVES, KIND>;
     constexpr int NO = 128;  // output channels
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *win = smem;                          // NWIN x WIN_HALF
-    uint8_t *wst = smem + C::NWIN * C::WIN_HALF;  // S x WST_BYTES
+    uint8_t *stg = smem + C::NWIN * C::WIN_HALF;  // 4 x STG_BYTES (staged outputs)
+    uint8_t *wst = stg + C::STG_TOTAL;            // S x WST_BYTES
 
     __shared__ uint64_t win_full[C::NWIN], win_empty[C::NWIN], w_full[C::S], w_empty[C::S];
-    __shared__ uint64_t acc_full[2], acc_empty[2];
+    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
 
@@ -369,6 +379,10 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
             mbar_init(&acc_full[i], 1);
             mbar_init(&acc_empty[i], kEpiWarpsT);
         }
+        for (int i = 0; i < 4; ++i) {
+            mbar_init(&stg_full[i], 4);
+            mbar_init(&stg_empty[i], 1);
+        }
         for (int i = 0; i < C::S; ++i) {
             mbar_init(&w_full[i], 1);
             mbar_init(&w_empty[i], 1);
@@ -377,6 +391,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         fence_mbar_init();
         prefetch_tensormap(&in_map);
         prefetch_tensormap(&w_map);
+        if (C::STAGED && !HEAD) prefetch_tensormap(&out_map);
     }
     if (warp == 1) tmem_alloc(&tmem_base, 512);
     __syncthreads();
@@ -496,6 +511,35 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                     bool valid;
                     row_target<KIND>(q_base + c * 32 + lane, p.rows, orow, valid, point);
                     if (valid) p.parts[(size_t)quarter * p.part_stride + point] = sum;
+                } else if (C::STAGED) {
+                    // Rows q_base + c*32 .. +31 -> staging buffer of this row
+                    // group as [32 rows][128 channels] BF16 (pad rows 0), then
+                    // one TMA store by the group's quarter-0 warp.
+                    const uint32_t use = (uint32_t)(local * 2 + c);
+                    uint8_t *buf = stg + rq * C::STG_BYTES;
+                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) { fail(62); break; }
+                    const int row_lane = q_base + c * 32 + lane;
+                    const int rl = row_lane % kL3Board;
+                    const bool valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
+                    const unsigned vmask = __ballot_sync(0xffffffffu, valid_lane);
+                    __nv_bfloat16 *col = reinterpret_cast<__nv_bfloat16 *>(buf) + o;
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        col[j * 128] = __float2bfloat16_rn(((vmask >> j) & 1u) ? f[j] : 0.0f);
+                    fence_proxy_async();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&stg_full[rq]);
+                    if (quarter == 0 && lane == 0) {
+                        if (!mbar_wait(&stg_full[rq], use & 1, kWaitLimit)) {
+                            fail(63);
+                        } else {
+                            tma_store_2d(&out_map, buf, 0, q_base + c * 32);
+                            bulk_commit();
+                            bulk_wait_read0();
+                        }
+                        mbar_arrive(&stg_empty[rq]);
+                    }
+                    __syncwarp();
                 } else {
                     // Lane j works out where row (c*32 + j) goes once; the warp
                     // then walks the 32 rows with that code broadcast:
@@ -518,6 +562,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         }
     }
 
+    if (C::STAGED && !HEAD && warp >= 2 && (warp & 3) == 0 && lane == 0) bulk_wait0();
     __syncthreads();
     if (abort_flag && tid == 0) {
         for (int i = 0; i < C::NWIN; ++i) {
@@ -539,40 +584,53 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
 
 // planes [B][C][361] bytes -> L5 rows [B*399][halves*64] BF16, channel
 // dx*C + c = plane c at (y, x + dx - 2); zero rows y = 19, 20 and zero
-// channels >= 5C.
-__global__ void pack_planes_l5_kernel(const uint8_t *__restrict__ planes, int B, int C, int halves,
-                                      __nv_bfloat16 *__restrict__ out) {
-    const int groups = halves * 8;  // 8 channels per group
-    const size_t total = (size_t)B * kL5Board * groups;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-         i += (size_t)gridDim.x * blockDim.x) {
-        const size_t q = i / groups;
-        const int g = (int)(i % groups);
-        const int b = (int)(q / kL5Board), r = (int)(q % kL5Board);
+// channels >= 5C.  One CTA per board: the board's planes are staged in
+// shared memory, then every 16-byte group of every row is written once.
+constexpr int kPackMaxC = 64;
+__global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__restrict__ planes, int B,
+                                                             int C, int halves,
+                                                             __nv_bfloat16 *__restrict__ out) {
+    __shared__ uint8_t sp[kPackMaxC * kPoints];
+    const int b = blockIdx.x;
+    if (b >= B) return;
+    const uint8_t *src = planes + (size_t)b * C * kPoints;
+    for (int i = threadIdx.x; i < C * kPoints; i += blockDim.x) sp[i] = src[i];
+    __syncthreads();
+    const int groups = halves * 8;
+    __nv_bfloat16 *dst = out + (size_t)b * kL5Board * groups * 8;
+    const bool aligned = (C % 8) == 0;  // then a group of 8 channels shares one dx
+    for (int i = threadIdx.x; i < kL5Board * groups; i += blockDim.x) {
+        const int r = i / groups, g = i % groups;
         const int y = r / kL5Pitch, x = r % kL5Pitch;
         __align__(16) __nv_bfloat16 v[8];
+        if (aligned) {
+            const int ch0 = g * 8;
+            const int dx = ch0 / C, c0 = ch0 - dx * C;
+            const int sx = x + dx - 2;
+            const bool in = y < kBoard && ch0 < 5 * C && sx >= 0 && sx < kBoard;
+            const uint8_t *col = sp + c0 * kPoints + y * kBoard + sx;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int ch = g * 8 + j;
-            float val = 0.0f;
-            if (y < kBoard && ch < 5 * C) {
-                const int dx = ch / C, c = ch % C;
-                const int sx = x + dx - 2;
-                if (sx >= 0 && sx < kBoard)
-                    val = (float)planes[((size_t)b * C + c) * kPoints + y * kBoard + sx];
+            for (int j = 0; j < 8; ++j) v[j] = __float2bfloat16(in ? (float)col[j * kPoints] : 0.0f);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int ch = g * 8 + j;
+                float val = 0.0f;
+                if (y < kBoard && ch < 5 * C) {
+                    const int dx = ch / C, c = ch % C;
+                    const int sx = x + dx - 2;
+                    if (sx >= 0 && sx < kBoard) val = (float)sp[c * kPoints + y * kBoard + sx];
+                }
+                v[j] = __float2bfloat16(val);
             }
-            v[j] = __float2bfloat16(val);
         }
-        *reinterpret_cast<uint4 *>(out + q * (size_t)(halves * 64) + g * 8) =
-            *reinterpret_cast<const uint4 *>(v);
+        *reinterpret_cast<uint4 *>(dst + (size_t)i * 8) = *reinterpret_cast<const uint4 *>(v);
     }
 }
 
 void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv_bfloat16 *out,
                            cudaStream_t s) {
-    size_t total = (size_t)B * kL5Board * halves * 8;
-    int blocks = (int)std::min<size_t>((total + 255) / 256, 8192);
-    pack_planes_l5_kernel<<<blocks, 256, 0, s>>>(planes, B, C, halves, out);
+    pack_planes_l5_kernel<<<B, 256, 0, s>>>(planes, B, C, halves, out);
 }
 
 // ------------------------------------------------------------------ launch
@@ -621,13 +679,16 @@ static int launch_a(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) 
 template <int HALVES, int KIND, bool HEAD>
 static int launch_t(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) {
     using Cfg = TcTCfg<HALVES, KIND>;
-    CUtensorMap in_map, w_map;
+    CUtensorMap in_map, w_map, out_map;
+    std::memset(&out_map, 0, sizeof out_map);
     int rc = encode_map_2d_bf16(&in_map, L.in, (uint64_t)HALVES * 64, (uint64_t)L.rows, 64, Cfg::SUBROWS);
     if (!rc) rc = encode_map_2d_bf16(&w_map, L.w, 64, (uint64_t)Cfg::NTAPS * HALVES * 128, 64, 128);
+    if (!rc && Cfg::STAGED && !HEAD)
+        rc = encode_map_2d_bf16(&out_map, p.out, 128, (uint64_t)L.rows, 128, 32, /*swizzle=*/false);
     if (rc) return rc;
     p.ntiles = (L.rows + Cfg::TP - 1) / Cfg::TP;
     int grid = std::min(p.ntiles, sm_count);
-    tc_convT_kernel<HALVES, KIND, HEAD><<<grid, kTcThreadsT, Cfg::SMEM, s>>>(in_map, w_map, p);
+    tc_convT_kernel<HALVES, KIND, HEAD><<<grid, kTcThreadsT, Cfg::SMEM, s>>>(in_map, w_map, out_map, p);
     return LG_OK;
 }
 
@@ -678,7 +739,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 int encode_map_2d_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint64_t rows,
-                       uint32_t box_inner, uint32_t box_rows) {
+                       uint32_t box_inner, uint32_t box_rows, bool swizzle128) {
     static EncodeTiledFn fn = nullptr;
     if (!fn) {
         cudaDriverEntryPointQueryResult q;
@@ -696,7 +757,8 @@ int encode_map_2d_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint6
     cuuint32_t box[2] = {box_inner, box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides,
-                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         lg_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
