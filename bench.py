@@ -225,6 +225,8 @@ def run_ours(args, world, rank, local):
     P, V, wp, wv = make_weights()
     ctx = lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"),
                      value=lg.NetDesc.config1_value(wv, "bf16"), device=local, max_batch=BATCH)
+    import tempfile
+    ctx.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{BATCH}.json"))
     d_p = torch.from_numpy(planes_p).to(dev)
     d_v = torch.from_numpy(planes_v).to(dev)
     d_probs = torch.empty((POSITIONS, 361), dtype=torch.float32, device=dev)
@@ -333,6 +335,78 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def serving_config3(lg, wp, wv, planes_p, planes_v, device, n_req=100_000, rate=200_000.0,
+                    mean_batch=48, max_batch=512):
+    """Uneven batching as the search produces it: n_req single-position
+    requests with Poisson arrivals (rate per second, seed 2), grouped into
+    batches of Geometric(mean 48) sizes clipped to [1, 512] (seed 3).  Each
+    batch is submitted to both nets (lg_submit) at its last arrival; the
+    server merges what is queued, pads to a power-of-two bucket and replays
+    that bucket's CUDA graph.  Latency = completion of both nets - arrival."""
+    import tempfile
+    import threading as th
+    arrivals = np.cumsum(np.random.default_rng(2).exponential(1.0 / rate, n_req))
+    rng = np.random.default_rng(3)
+    sizes, total = [], 0
+    while total < n_req:
+        b = int(min(max(rng.geometric(1.0 / mean_batch), 1), max_batch, n_req - total))
+        sizes.append(b)
+        total += b
+    n_pos = planes_p.shape[0]
+    with lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"),
+                    value=lg.NetDesc.config1_value(wv, "bf16"), device=device,
+                    max_batch=max_batch) as ctx:
+        ctx.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{max_batch}.json"))
+        b = 1
+        while b <= max_batch:  # capture every bucket's graphs before the clock starts
+            ctx.policy(planes_p[:b])
+            ctx.value(planes_v[:b])
+            b *= 2
+        batches, start = [], 0
+        for k, sz in enumerate(sizes):
+            idx = np.arange(start, start + sz) % n_pos
+            batches.append((np.ascontiguousarray(planes_p[idx]), np.ascontiguousarray(planes_v[idx]),
+                            np.empty((sz, 361), np.float32), np.empty(sz, np.float32), start, sz))
+            start += sz
+        done = {}
+        stop = th.Event()
+
+        def poller():
+            while not stop.is_set() or len(done) < 2 * len(batches):
+                for t in ctx.poll(512, timeout_us=2000):
+                    done[t] = time.perf_counter()
+                if stop.is_set() and len(done) >= 2 * len(batches):
+                    break
+
+        pt = th.Thread(target=poller, daemon=True)
+        pt.start()
+        t0 = time.perf_counter() + 0.01
+        for k, (bp, bv, op, ov, st, sz) in enumerate(batches):
+            due = t0 + arrivals[st + sz - 1]
+            while time.perf_counter() < due:
+                pass
+            ctx.submit(lg.LG_NET_POLICY, bp, op, tag=2 * k + 1)
+            ctx.submit(lg.LG_NET_VALUE, bv, ov, tag=2 * k + 2)
+        stop.set()
+        pt.join(timeout=60)
+        served = ctx.stats()["batches"]
+    if len(done) < 2 * len(batches):
+        return {"error": f"only {len(done)} of {2 * len(batches)} submissions completed"}
+    lat = np.empty(n_req)
+    last = 0.0
+    for k, (_, _, _, _, st, sz) in enumerate(batches):
+        comp = max(done[2 * k + 1], done[2 * k + 2])
+        last = max(last, comp)
+        lat[st:st + sz] = comp - (t0 + arrivals[st:st + sz])
+    return {"requests": n_req, "arrival_rate_per_s": rate, "client_batches": len(sizes),
+            "server_batches": int(served), "mean_client_batch": float(np.mean(sizes)),
+            "throughput_positions_per_s": n_req / (last - (t0 + arrivals[0])),
+            "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "note": "policy + value per request; BF16; CUDA graph per power-of-two bucket "
+                    "(host copies inside the graph); autotuned kernel choice per bucket"}
+
+
 def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp):
     """FP32 batch-1 throughput, BF16 at the other batch sizes, and top-1
     agreement with the FP64 oracle."""
@@ -414,6 +488,7 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
                        "value_mean_abs_err": float(np.abs(vq - v64).mean()),
                        "positions": int(idx.size)}
     out["vs_fp64_oracle"] = agree
+    out["serving_config3"] = serving_config3(lg, wp, wv, planes_p, planes_v, dev.index)
     return out
 
 

@@ -158,6 +158,22 @@ LG_API int lg_stats(lg_ctx *ctx, long long *kernel_launches, long long *batches)
 LG_API int lg_policy_device_static(lg_ctx *ctx, const uint8_t *planes, int B, float temperature,
                                    float *probs, float *logits, void *stream);
 
+/* Autotuner.  For every power-of-two batch bucket up to max_batch, times the
+ * context's tensor-core nets with each kernel choice for the 3x3 layers and
+ * for the first layer (256-row tiles on the transposed kernel, or 128-row
+ * tiles, which put twice as many CTAs on a small batch) and keeps the
+ * fastest.  With a cache path, a table saved for the same device, SM count
+ * and net shapes is loaded instead (unless force), and a new table is saved
+ * there (written to a temporary file and renamed).  Without tuning every
+ * bucket uses the 256-row kernel.  No reference counterpart (the OpenCL
+ * backend reads a fixed cfg_rowtiles, OpenCL.cpp:634-646).
+ * lg_tuning reports the choice for batch B; it returns 1 once tuned, 0 if
+ * not, < 0 on error. */
+LG_API int lg_autotune(lg_ctx *ctx, const char *cache_path, int force);
+LG_API int lg_tuning(lg_ctx *ctx, int B, int *variant_3x3, int *variant_first);
+/* Sets the kernel choice of B's bucket by hand (0 or 1 each, as above). */
+LG_API int lg_set_tuning(lg_ctx *ctx, int B, int variant_3x3, int variant_first);
+
 /* Per-kernel timing for the roofline report.  lg_profile(ctx, 1) clears the
  * counters and brackets every kernel launched by later device-pointer calls
  * (lg_policy_device / lg_value_device) with CUDA events on the launching

@@ -57,7 +57,7 @@ _lib_lock = threading.Lock()
 EXPORTS = ["lg_weight_count", "lg_create", "lg_destroy", "lg_last_error", "lg_policy",
            "lg_value", "lg_policy_device", "lg_value_device", "lg_submit", "lg_poll",
            "lg_stats", "lg_inject_fault", "lg_profile", "lg_profile_read",
-           "lg_policy_device_static"]
+           "lg_policy_device_static", "lg_autotune", "lg_tuning", "lg_set_tuning"]
 
 
 def library():
@@ -86,6 +86,9 @@ def library():
             L.lg_inject_fault.argtypes = [vp, i32]
             L.lg_profile.argtypes = [vp, i32]
             L.lg_policy_device_static.argtypes = [vp, vp, i32, f32, vp, vp, vp]
+            L.lg_autotune.argtypes = [vp, ctypes.c_char_p, i32]
+            L.lg_tuning.argtypes = [vp, i32, P(i32), P(i32)]
+            L.lg_set_tuning.argtypes = [vp, i32, i32, i32]
             L.lg_profile_read.argtypes = [vp, i32, P(ctypes.c_longlong), P(ctypes.c_double)]
             _lib = L
     return _lib
@@ -235,6 +238,19 @@ class Context:
         n, ms = ctypes.c_longlong(), ctypes.c_double()
         _check(library().lg_profile_read(self._h, kind, ctypes.byref(n), ctypes.byref(ms)))
         return n.value, ms.value
+
+    def autotune(self, cache_path: str | None = None, force: bool = False):
+        """Pick the tensor-core kernel per batch bucket (see lg_autotune)."""
+        _check(library().lg_autotune(self._h, cache_path.encode() if cache_path else None,
+                                     1 if force else 0))
+
+    def tuning(self, B: int):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        tuned = _check(library().lg_tuning(self._h, B, ctypes.byref(a), ctypes.byref(b)))
+        return {"tuned": bool(tuned), "conv3x3": a.value, "first": b.value}
+
+    def set_tuning(self, B: int, conv3x3: int, first: int):
+        _check(library().lg_set_tuning(self._h, B, conv3x3, first))
 
     def inject_fault(self, nth_call: int):
         _check(library().lg_inject_fault(self._h, nth_call))

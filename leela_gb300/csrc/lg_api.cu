@@ -134,6 +134,11 @@ struct lg_ctx {
     std::vector<cudaEvent_t> event_pool;
     long long prof_launches[LG_PROF_KINDS] = {};
     double prof_ms[LG_PROF_KINDS] = {};
+    // Kernel choice per power-of-two batch bucket (index = log2) for the
+    // 128-wide tensor-core layers: [bucket][0] 3x3 layers (and fused head),
+    // [bucket][1] first layer; 0 = 256-row transposed kernel, 1 = 128-row.
+    int tc_variant[17][2] = {};
+    bool tuned = false;
     std::atomic<long long> launches{0};
     std::atomic<long long> batches{0};
     std::atomic<int> fault_in{0};
@@ -420,6 +425,9 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
     ++L;
     float *lg = logits_out ? logits_out : c->d_logits;
     const size_t part_stride = (size_t)B * kPoints;
+    int bl = 0;
+    while ((1 << bl) < B && bl < 16) ++bl;
+    const int var3 = c->tc_variant[bl][0], var1 = c->tc_variant[bl][1];
     int cur = 0;
     for (size_t l = 0; l < n.tc.size(); ++l) {
         const TcConv &t = n.tc[l];
@@ -435,6 +443,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
         tl.n = t.cout;
         tl.in_kind = (l == 0) ? 1 : 0;
         tl.rows = (l == 0) ? B * kL5Board : B * kL3Board;
+        tl.variant = (l == 0) ? var1 : var3;
         __nv_bfloat16 *out = (l == 0) ? c->l3[0] : c->l3[cur ^ 1];
         int rc;
         {
@@ -448,7 +457,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
     }
     {
         ProfScope ps(c, prof, LG_PROF_OTHER, s);
-        HeadIn h{c->d_parts, tc_head_parts(d.width), part_stride, n.head_b, d.act_head, d.act, lg};
+        HeadIn h{c->d_parts, tc_head_parts(d.width, var3), part_stride, n.head_b, d.act_head, d.act, lg};
         if (!d.value_head)
             launch_softmax(h, B, T, probs, s);
         else
@@ -598,16 +607,21 @@ void worker_main(lg_ctx *c) {
             std::unique_lock<std::mutex> lk(c->qmu);
             c->qcv.wait(lk, [&] { return c->stop || !c->queue.empty(); });
             if (c->stop && c->queue.empty()) return;
+            // The oldest request picks the net (and temperature); every queued
+            // request of that kind joins, in arrival order, while it fits.
             int total = 0;
-            int net = c->queue.front().net;
-            float T = c->queue.front().temperature;
-            while (!c->queue.empty()) {
-                auto &r = c->queue.front();
-                if (r.net != net || (net == LG_NET_POLICY && r.temperature != T)) break;
-                if (total > 0 && total + r.B > c->max_batch) break;
-                total += r.B;
-                batch.push_back(r);
-                c->queue.pop_front();
+            const int net = c->queue.front().net;
+            const float T = c->queue.front().temperature;
+            for (auto it = c->queue.begin(); it != c->queue.end();) {
+                const bool same = it->net == net && (net != LG_NET_POLICY || it->temperature == T);
+                if (!same) {
+                    ++it;
+                    continue;
+                }
+                if (total > 0 && total + it->B > c->max_batch) break;
+                total += it->B;
+                batch.push_back(*it);
+                it = c->queue.erase(it);
             }
         }
         int net = batch[0].net;
@@ -1016,5 +1030,182 @@ extern "C" int lg_policy_device_static(lg_ctx *c, const uint8_t *planes, int B, 
         lg_set_error("lg_policy_device_static: launch failed: %s", cudaGetErrorString(e));
         return LG_ERR_CUDA;
     }
+    return LG_OK;
+}
+
+// ============================================================================
+// Autotuner: for every power-of-two batch bucket up to max_batch, time the
+// tensor-core nets' forward with each kernel choice for the 3x3 layers and
+// for the first layer (256-row transposed kernel or 128-row kernel), keep
+// the fastest, and cache the table as JSON keyed by device name, SM count
+// and net widths.  FP32 nets have nothing to tune.
+// ============================================================================
+
+namespace {
+
+std::string tune_key(lg_ctx *c) {
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, c->device);
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s|sm%d|p%d/%d/%d|v%d/%d/%d|mb%d", prop.name, c->sm_count,
+             c->nets[0].present ? c->nets[0].d.precision : -1, c->nets[0].present ? c->nets[0].d.width : 0,
+             c->nets[0].present ? c->nets[0].d.c_in : 0, c->nets[1].present ? c->nets[1].d.precision : -1,
+             c->nets[1].present ? c->nets[1].d.width : 0, c->nets[1].present ? c->nets[1].d.c_in : 0,
+             c->max_batch);
+    return buf;
+}
+
+bool load_tuning(lg_ctx *c, const char *path) {
+    FILE *f = fopen(path, "r");
+    if (!f) return false;
+    std::string text;
+    char buf[4096];
+    size_t n;
+    while ((n = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
+    fclose(f);
+    std::string key = "\"key\": \"" + tune_key(c) + "\"";
+    if (text.find(key) == std::string::npos) return false;
+    int table[17][2] = {};
+    for (int b = 0; b <= 16; ++b) {
+        char pat[64];
+        snprintf(pat, sizeof pat, "\"%d\": [", 1 << b);
+        size_t pos = text.find(pat);
+        if (pos == std::string::npos) continue;
+        int a = 0, d = 0;
+        if (sscanf(text.c_str() + pos + strlen(pat), "%d, %d", &a, &d) != 2) return false;
+        table[b][0] = a;
+        table[b][1] = d;
+    }
+    std::memcpy(c->tc_variant, table, sizeof table);
+    return true;
+}
+
+int save_tuning(lg_ctx *c, const char *path, const double (*ms)[4]) {
+    std::string tmp = std::string(path) + ".tmp";
+    FILE *f = fopen(tmp.c_str(), "w");
+    if (!f) {
+        lg_set_error("cannot write %s", tmp.c_str());
+        return LG_ERR_ARG;
+    }
+    fprintf(f, "{\n \"key\": \"%s\",\n \"order\": \"[3x3 layers, first layer] 0 = 256-row transposed, 1 = 128-row\",\n \"table\": {",
+            tune_key(c).c_str());
+    bool first = true;
+    for (int b = 0; (1 << b) <= c->max_batch && b <= 16; ++b) {
+        fprintf(f, "%s\n  \"%d\": [%d, %d]", first ? "" : ",", 1 << b, c->tc_variant[b][0],
+                c->tc_variant[b][1]);
+        first = false;
+    }
+    fprintf(f, "\n },\n \"ms_per_forward\": {");
+    first = true;
+    for (int b = 0; (1 << b) <= c->max_batch && b <= 16; ++b) {
+        fprintf(f, "%s\n  \"%d\": [%.4f, %.4f, %.4f, %.4f]", first ? "" : ",", 1 << b, ms[b][0], ms[b][1],
+                ms[b][2], ms[b][3]);
+        first = false;
+    }
+    fprintf(f, "\n }\n}\n");
+    fclose(f);
+    if (rename(tmp.c_str(), path) != 0) {
+        lg_set_error("cannot rename %s", tmp.c_str());
+        return LG_ERR_ARG;
+    }
+    return LG_OK;
+}
+
+}  // namespace
+
+extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
+    if (!c) {
+        lg_set_error("lg_autotune: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    bool any_tc = false;
+    for (int i = 0; i < 2; ++i) any_tc |= c->nets[i].present && c->nets[i].d.precision != LG_FP32;
+    if (!any_tc) return LG_OK;
+    if (cache_path && !force && load_tuning(c, cache_path)) {
+        for (auto &gr : c->graphs) cudaGraphExecDestroy(gr.second.first);
+        c->graphs.clear();
+        c->tuned = true;
+        return LG_OK;
+    }
+    LG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaEvent_t e0, e1;
+    LG_CUDA_TRY(cudaEventCreate(&e0));
+    LG_CUDA_TRY(cudaEventCreate(&e1));
+    LG_CUDA_TRY(cudaMemsetAsync(c->d_planes, 0, (size_t)c->max_batch * c->planes_c * kPoints, c->stream));
+    double ms[17][4] = {};
+    int rc = LG_OK;
+    for (int b = 0; (1 << b) <= c->max_batch && b <= 16 && rc == LG_OK; ++b) {
+        const int B = 1 << b;
+        double best = 1e30;
+        int best_v = 0;
+        for (int v = 0; v < 4 && rc == LG_OK; ++v) {
+            c->tc_variant[b][0] = v & 1;
+            c->tc_variant[b][1] = v >> 1;
+            const int reps = B >= 64 ? 5 : 20;
+            float t = 0.0f;
+            for (int it = 0; it < 2 + reps && rc == LG_OK; ++it) {
+                if (it == 2) cudaEventRecord(e0, c->stream);
+                for (int net = 0; net < 2 && rc == LG_OK; ++net) {
+                    Net &n = c->nets[net];
+                    if (!n.present || n.d.precision == LG_FP32) continue;
+                    int nl = 0;
+                    rc = forward(c, net, c->d_planes, B, 1.0f, c->d_probs, nullptr, c->d_value, c->stream, &nl);
+                }
+            }
+            if (rc) break;
+            cudaEventRecord(e1, c->stream);
+            LG_CUDA_TRY(cudaEventSynchronize(e1));
+            cudaEventElapsedTime(&t, e0, e1);
+            ms[b][v] = t / reps;
+            if (ms[b][v] < best) {
+                best = ms[b][v];
+                best_v = v;
+            }
+        }
+        c->tc_variant[b][0] = best_v & 1;
+        c->tc_variant[b][1] = best_v >> 1;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int herr = 0;
+    cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (rc == LG_OK && herr) {
+        cudaMemset(c->d_err, 0, sizeof(int));
+        lg_set_error("kernel reported error status %d during tuning", herr);
+        rc = LG_ERR_DEVICE;
+    }
+    for (auto &gr : c->graphs) cudaGraphExecDestroy(gr.second.first);
+    c->graphs.clear();
+    if (rc != LG_OK) {
+        std::memset(c->tc_variant, 0, sizeof c->tc_variant);
+        return rc;
+    }
+    c->tuned = true;
+    if (cache_path) return save_tuning(c, cache_path, ms);
+    return LG_OK;
+}
+
+extern "C" int lg_tuning(lg_ctx *c, int B, int *variant_3x3, int *variant_first) {
+    if (!c || B < 1) return LG_ERR_ARG;
+    int bl = 0;
+    while ((1 << bl) < B && bl < 16) ++bl;
+    if (variant_3x3) *variant_3x3 = c->tc_variant[bl][0];
+    if (variant_first) *variant_first = c->tc_variant[bl][1];
+    return c->tuned ? 1 : 0;
+}
+
+extern "C" int lg_set_tuning(lg_ctx *c, int B, int variant_3x3, int variant_first) {
+    if (!c || B < 1 || variant_3x3 < 0 || variant_3x3 > 1 || variant_first < 0 || variant_first > 1) {
+        lg_set_error("lg_set_tuning: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    int bl = 0;
+    while ((1 << bl) < B && bl < 16) ++bl;
+    c->tc_variant[bl][0] = variant_3x3;
+    c->tc_variant[bl][1] = variant_first;
+    for (auto &gr : c->graphs) cudaGraphExecDestroy(gr.second.first);
+    c->graphs.clear();
     return LG_OK;
 }

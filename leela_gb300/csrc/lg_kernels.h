@@ -50,6 +50,7 @@ struct TcLayer {
     int n;                // output channels (64 or 128)
     int in_kind;          // 0: L3 input (3x3); 1: L5 input (expanded 5x5 first layer)
     int rows;             // input rows processed (B * 400 or B * 399)
+    int variant;          // for n == 128: 0 = 256-row transposed kernel, 1 = 128-row kernel
 };
 
 // Expanded 5x5 input: planes [B][C][361] bytes -> L5 BF16 rows with
@@ -61,7 +62,7 @@ void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv
 // kernel covers the shape.
 int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *parts, size_t part_stride,
                    int *err, cudaStream_t s, int sm_count);
-int tc_head_parts(int n);
+int tc_head_parts(int n, int variant = 0);
 size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves);
 int tc_init_device();
 // Head kernels for the tensor-core path (logits already produced by the

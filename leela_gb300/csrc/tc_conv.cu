@@ -654,14 +654,14 @@ int tc_init_device() {
 #define LG_T(H_, K_, HD_) \
     if (!rc) rc = set_attr<decltype(&tc_convT_kernel<H_, K_, HD_>), TcTCfg<H_, K_>::SMEM>(tc_convT_kernel<H_, K_, HD_>);
     LG_A(64, 1, 0, false) LG_A(64, 1, 0, true) LG_A(64, 2, 1, false) LG_A(64, 3, 1, false)
-    LG_A(128, 3, 1, false)
+    LG_A(128, 3, 1, false) LG_A(128, 2, 0, false) LG_A(128, 2, 0, true) LG_A(128, 2, 1, false)
     LG_T(2, 0, false) LG_T(2, 0, true) LG_T(2, 1, false)
 #undef LG_A
 #undef LG_T
     return rc;
 }
 
-int tc_head_parts(int n) { return n == 128 ? 4 : 1; }
+int tc_head_parts(int n, int variant) { return (n == 128 && variant == 0) ? 4 : 1; }
 
 template <int N, int HALVES, int KIND, bool HEAD>
 static int launch_a(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) {
@@ -715,6 +715,10 @@ int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *parts, size_t
         lg_set_error("launch_tc_conv: bad layer arguments");
         return LG_ERR_ARG;
     }
+    if (L.n == 128 && L.cin_halves == 2 && L.in_kind == 0 && L.variant == 1)
+        return head ? launch_a<128, 2, 0, true>(L, p, s, sm_count) : launch_a<128, 2, 0, false>(L, p, s, sm_count);
+    if (L.n == 128 && L.cin_halves == 2 && L.in_kind == 1 && !head && L.variant == 1)
+        return launch_a<128, 2, 1, false>(L, p, s, sm_count);
     if (L.n == 128 && L.cin_halves == 2 && L.in_kind == 0)
         return head ? launch_t<2, 0, true>(L, p, s, sm_count) : launch_t<2, 0, false>(L, p, s, sm_count);
     if (L.n == 128 && L.cin_halves == 2 && L.in_kind == 1 && !head)

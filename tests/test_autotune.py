@@ -1,0 +1,61 @@
+"""Kernel variants for 128-wide tensor-core layers and the autotuner that
+picks between them per batch bucket (lg_autotune / lg_tuning /
+lg_set_tuning)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_logit_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def f64(positions, weights, oracle_mod):
+    O = oracle_mod
+    O.enable_blas()
+    try:
+        lp = O.forward_f64(weights["cfg_p"][0], weights["cfg_p"][1], positions["planes_p"][:64, :24])
+        v = O.forward_f64(weights["cfg_v"][0], weights["cfg_v"][1], positions["planes_v"][:64, :24])
+    finally:
+        O.disable_blas()
+    return lp, v
+
+
+@pytest.mark.parametrize("v3,v1", [(0, 0), (1, 0), (0, 1), (1, 1)])
+@pytest.mark.parametrize("B", [1, 5, 64])
+def test_every_variant_meets_the_bf16_bars(gpu_lib, weights, positions, f64, v3, v1, B):
+    lg = gpu_lib
+    lp64, v64 = f64
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"), max_batch=64) as c:
+        c.set_tuning(B, v3, v1)
+        _, logits = c.policy(positions["planes_p"][:B, :24], 1.0, return_logits=True)
+        v = c.value(positions["planes_v"][:B, :24])
+    assert rel_logit_err(logits, lp64[:B]).max() <= 5e-2
+    assert np.abs(v - v64[:B]).max() <= 3e-2
+    if B == 64:
+        assert (logits.argmax(1) == lp64.argmax(1)).mean() >= 0.95
+
+
+def test_autotune_writes_and_reloads_its_cache(gpu_lib, weights, positions, tmp_path):
+    lg = gpu_lib
+    path = str(tmp_path / "tune.json")
+    kw = dict(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
+              value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"), max_batch=32)
+    with lg.Context(**kw) as c:
+        assert not c.tuning(4)["tuned"]
+        ref = c.policy(positions["planes_p"][:20, :24])
+        c.autotune(path)
+        table = {b: c.tuning(b) for b in (1, 2, 4, 8, 16, 32)}
+        assert all(t["tuned"] for t in table.values())
+        after = c.policy(positions["planes_p"][:20, :24])
+        assert np.abs(after - ref).max() < 1e-4
+    with open(path) as f:
+        saved = json.load(f)
+    assert set(saved["table"]) == {"1", "2", "4", "8", "16", "32"}
+    with lg.Context(**kw) as c2:
+        c2.autotune(path)  # loads, no timing
+        assert {b: c2.tuning(b) for b in table} == table
