@@ -489,7 +489,24 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
                        "positions": int(idx.size)}
     out["vs_fp64_oracle"] = agree
     out["serving_config3"] = serving_config3(lg, wp, wv, planes_p, planes_v, dev.index)
+    out["distill_config4"] = distill_config4(wp, wv, planes_p, planes_v, dev.index)
     return out
+
+
+def distill_config4(wp, wv, planes_p, planes_v, device):
+    """BASELINE config 4 on the fixture positions: the student is trained on
+    positions 0..895 (x8 symmetries), evaluated on 896..1023; labels are the
+    full FP32 policy net's softmax and 2*mc_owner(64)-1.  Run at the
+    specified teacher temperature 1 and, as an ablation, at 0.05 (the
+    He-normal teacher's policies are nearly flat at temperature 1)."""
+    from leela_gb300 import distill
+    mc = np.load(os.path.join(ROOT, "tests", "golden", "mcowner_s0.npz"))["mcowner"]
+    pos_index = np.arange(planes_p.shape[0]) % 1024
+    res = {}
+    for name, temp in (("teacher_T1", 1.0), ("teacher_T0.05", 0.05)):
+        res[name] = distill.run_config4(planes_p, planes_v, pos_index, mc, wp, wv, device,
+                                        teacher_temperature=temp, time_budget_s=25.0)
+    return res
 
 
 def main():

@@ -174,6 +174,44 @@ LG_API int lg_tuning(lg_ctx *ctx, int B, int *variant_3x3, int *variant_first);
 /* Sets the kernel choice of B's bucket by hand (0 or 1 each, as above). */
 LG_API int lg_set_tuning(lg_ctx *ctx, int B, int variant_3x3, int variant_first);
 
+/* ---------------------------------------------------------------------
+ * Distilled student net (no reference counterpart; the reference trained
+ * offline with Caffe, Network.cpp:1381-1509).  One trunk (5x5 c_in -> width,
+ * n3x3 x 3x3 width -> width, ReLU) with a 1x1 policy head (softmax over
+ * 361) and a 1x1 value head -> FC 361 -> fc_hidden (ReLU) -> FC -> tanh,
+ * trained in FP32 on the GPU by this library's forward and backward kernels
+ * with Adam.  Loss = KL(target policy || softmax) + value_weight *
+ * (value - target)^2, averaged over the batch.
+ *
+ * Flat parameter layout (host side): per conv W[O][C][k][k] then b[O]; then
+ * policy head w[width], b; value head w[width], b; W1[fc_hidden][361],
+ * b1[fc_hidden], W2[fc_hidden], b2.  The trunk + policy head is a valid
+ * lg_net_desc weight array for a policy net (head_k 1), and the trunk +
+ * value head + FC one for a value net, so a trained student can be served
+ * by lg_create at any precision.
+ *
+ * planes / targets are device pointers: planes [B][c_in][361] bytes, target
+ * probabilities [B][361], target values [B] in [-1, 1]. */
+typedef struct lg_student lg_student;
+LG_API int lg_student_create(int device, int c_in, int width, int n3x3, int fc_hidden, int max_batch,
+                             lg_student **out);
+LG_API void lg_student_destroy(lg_student *st);
+LG_API size_t lg_student_param_count(const lg_student *st);
+LG_API int lg_student_set_params(lg_student *st, const float *host, size_t n);
+LG_API int lg_student_get_params(lg_student *st, float *host, size_t n);
+/* One Adam step (lr, betas 0.9 / 0.999, eps 1e-8); host_loss (optional)
+ * receives {policy KL, value MSE} of the batch. */
+LG_API int lg_student_train_step(lg_student *st, const uint8_t *planes, int B, const float *target_probs,
+                                 const float *target_value, float lr, float value_weight, float *host_loss,
+                                 void *stream);
+/* Loss gradients in the flat host layout, no update (gradient checks). */
+LG_API int lg_student_grads(lg_student *st, const uint8_t *planes, int B, const float *target_probs,
+                            const float *target_value, float value_weight, float *host_grads,
+                            float *host_loss);
+/* FP32 forward: probabilities at temperature 1 and values (device). */
+LG_API int lg_student_forward(lg_student *st, const uint8_t *planes, int B, float *probs, float *value,
+                              void *stream);
+
 /* Per-kernel timing for the roofline report.  lg_profile(ctx, 1) clears the
  * counters and brackets every kernel launched by later device-pointer calls
  * (lg_policy_device / lg_value_device) with CUDA events on the launching

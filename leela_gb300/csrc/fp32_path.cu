@@ -24,7 +24,8 @@ namespace lg {
 __device__ __forceinline__ float act_fn(float v, int act) {
     // ELU exactly as the reference writes it: x > 0 ? x : exp(x) - 1.
     if (act == LG_ACT_ELU) return (v > 0.0f) ? v : (expf(v) - 1.0f);
-    return (v > 0.0f) ? v : 0.0f;
+    if (act == LG_ACT_RELU) return (v > 0.0f) ? v : 0.0f;
+    return v;  // any other code: identity (used by the training kernels)
 }
 
 // planes [B][C][361] 0/1 bytes -> NHWC FP32 [B*361][C]

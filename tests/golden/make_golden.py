@@ -24,7 +24,9 @@ own code for:
                        64 positions, rotations 0 and 3
   weights.json         FNV-1a checksums of every weight set, so a test can
                        confirm another host draws the same weights
-  mcowner_s0.npz       Playout::mc_owner(state, 64) for the first 64 positions
+  mcowner_s0.npz       Playout::mc_owner(state, 64) for all 1024 positions (the
+                       win rate of the side to move; the distilled net's value
+                       labels)
 
 The fixtures need nothing from the reference at test time.
 """
@@ -117,7 +119,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, "config1_s0.npz"), **out)
 
         pre = os.path.join(td, "mc")
-        run([harness, "mcowner", str(N_OUT), str(SEED), "64", str(args.threads), pre])
+        run([harness, "mcowner", str(N_POS), str(SEED), "64", str(args.threads), pre])
         np.savez_compressed(os.path.join(HERE, "mcowner_s0.npz"),
                             mcowner=np.fromfile(pre + ".mcowner", np.float32))
 

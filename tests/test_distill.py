@@ -1,0 +1,106 @@
+"""The distilled student: GPU training kernels against the FP64 oracle, a
+training run that lowers the loss, export to the serving paths, and the
+entropy-gated fallback."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def student_mod(gpu_lib):
+    from leela_gb300 import distill
+    return distill
+
+
+def _targets(rng, B):
+    logits = rng.normal(0, 2.0, (B, 361))
+    t = np.exp(logits - logits.max(1, keepdims=True))
+    return (t / t.sum(1, keepdims=True)).astype(np.float32), rng.uniform(-0.8, 0.8, B).astype(np.float32)
+
+
+def test_student_gradients_match_fp64_oracle(student_mod, positions):
+    import torch
+    from oracle import distill_oracle as D
+    st = student_mod.Student(max_batch=8)
+    st.init_he(3)
+    p = st.get_params()
+    rng = np.random.default_rng(5)
+    # small random biases so that no layer is exactly at a ReLU kink
+    planes = np.ascontiguousarray(positions["planes_p"][10:13, :24])
+    t, vt = _targets(rng, 3)
+    d_planes = torch.from_numpy(planes).cuda()
+    d_t = torch.from_numpy(t).cuda()
+    d_v = torch.from_numpy(vt).cuda()
+    (kl, mse), g = st.grads(d_planes.data_ptr(), 3, d_t.data_ptr(), d_v.data_ptr(), 0.5)
+    (kl64, mse64), g64 = D.loss_and_grads(p, planes, t, vt, 0.5, 24, 64, 5, 64)
+    assert abs(kl - kl64) <= 1e-4 * abs(kl64) + 1e-6
+    assert abs(mse - mse64) <= 1e-4 * abs(mse64) + 1e-6
+    # per parameter tensor, norm-wise relative error; the floor covers
+    # tensors whose exact gradient is zero (the policy-head bias: the
+    # softmax and the target both sum to 1)
+    floor = 1e-4 * np.abs(g64).max()
+    off = 0
+    for s in D.shapes(24, 64, 5, 64):
+        sizes = [s[3] * s[2] * s[1] * s[1], s[3]] if s[0] == "conv" else [s[1]]
+        for n in sizes:
+            a, b = g[off:off + n], g64[off:off + n]
+            off += n
+            denom = max(np.abs(b).max(), floor)
+            assert np.abs(a - b).max() / denom <= 2e-3, (s, n, np.abs(a - b).max(), denom)
+    st.close()
+
+
+def test_training_lowers_the_loss(student_mod, positions):
+    import torch
+    st = student_mod.Student(max_batch=64)
+    st.init_he(1)
+    rng = np.random.default_rng(7)
+    planes = torch.from_numpy(np.ascontiguousarray(positions["planes_p"][:64, :24])).cuda()
+    t, vt = _targets(rng, 64)
+    d_t, d_v = torch.from_numpy(t).cuda(), torch.from_numpy(vt).cuda()
+    log = student_mod.train(st, planes, d_t, d_v, steps=300, batch=64, lr=2e-3, log_every=50)
+    first, last = log[0], log[-1]
+    assert last[1] + last[2] < 0.7 * (first[1] + first[2]), log
+    st.close()
+
+
+def test_exported_nets_match_the_student_forward(student_mod, gpu_lib, positions):
+    import torch
+    lg = gpu_lib
+    st = student_mod.Student(max_batch=32)
+    st.init_he(2)
+    planes = torch.from_numpy(np.ascontiguousarray(positions["planes_p"][:20, :24])).cuda()
+    probs = torch.empty((20, 361), device="cuda")
+    val = torch.empty(20, device="cuda")
+    st.forward(planes.data_ptr(), 20, probs.data_ptr(), val.data_ptr())
+    torch.cuda.synchronize()
+    with lg.Context(policy=st.policy_desc("fp32"), value=st.value_desc("fp32"), max_batch=32) as c:
+        p2 = c.policy(planes.cpu().numpy())
+        v2 = c.value(planes.cpu().numpy())
+    assert np.abs(probs.cpu().numpy() - p2).max() < 1e-5
+    assert np.abs(val.cpu().numpy() - v2).max() < 1e-5
+    st.close()
+
+
+def test_gate_routes_by_entropy(student_mod, gpu_lib, weights, positions):
+    import torch
+    lg = gpu_lib
+    st = student_mod.Student(max_batch=64)
+    st.init_he(4)
+    pp = torch.from_numpy(np.ascontiguousarray(positions["planes_p"][:40, :24])).cuda()
+    pv = torch.from_numpy(np.ascontiguousarray(positions["planes_v"][:40, :24])).cuda()
+    with lg.Context(policy=st.policy_desc("bf16"), value=st.value_desc("bf16"), max_batch=64) as cs, \
+            lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
+                       value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"),
+                       max_batch=64) as cf:
+        never = student_mod.GatedEvaluator(cs, cf, threshold=1e9)
+        p, v, m = never.evaluate(pp, pv)
+        assert not m.any().item()
+        assert np.array_equal(p.cpu().numpy(), cs.policy(pp.cpu().numpy()))
+        always = student_mod.GatedEvaluator(cs, cf, threshold=-1.0)
+        p, v, m = always.evaluate(pp, pv)
+        assert m.all().item()
+        assert np.array_equal(p.cpu().numpy(), cf.policy(pp.cpu().numpy()))
+        assert np.array_equal(v.cpu().numpy(), cf.value(pv.cpu().numpy()))
+    st.close()

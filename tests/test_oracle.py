@@ -138,4 +138,4 @@ def test_e4m3_rounding(oracle_mod):
 
 def test_mcowner_labels_in_range():
     d = np.load(os.path.join(GOLDEN, "mcowner_s0.npz"))["mcowner"]
-    assert d.shape == (64,) and np.all((d >= 0) & (d <= 1))
+    assert d.shape == (1024,) and np.all((d >= 0) & (d <= 1))
