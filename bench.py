@@ -357,10 +357,18 @@ def serving_config3(lg, wp, wv, planes_p, planes_v, device, n_req=100_000, rate=
                     value=lg.NetDesc.config1_value(wv, "bf16"), device=device,
                     max_batch=max_batch) as ctx:
         ctx.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{max_batch}.json"))
-        b = 1
-        while b <= max_batch:  # capture every bucket's graphs before the clock starts
-            ctx.policy(planes_p[:b])
-            ctx.value(planes_v[:b])
+        # Capture every bucket's graphs (both server slots) before the clock starts.
+        b, tag = 1, 10_000_000
+        while b <= max_batch:
+            for _ in range(2):
+                for net, src in ((lg.LG_NET_POLICY, planes_p), (lg.LG_NET_VALUE, planes_v)):
+                    x = np.ascontiguousarray(src[:b])
+                    o = np.empty((b, 361) if net == lg.LG_NET_POLICY else b, np.float32)
+                    tag += 1
+                    ctx.submit(net, x, o, tag=tag)
+                    for _ in range(5000):
+                        if ctx.poll(4, timeout_us=1000):
+                            break
             b *= 2
         batches, start = [], 0
         for k, sz in enumerate(sizes):

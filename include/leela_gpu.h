@@ -76,6 +76,21 @@ typedef struct lg_net_desc {
 
 typedef struct lg_ctx lg_ctx;
 
+/* Weight files.  lg_weights_save writes n nets (description + flat weights,
+ * an optional name of up to 15 characters each) with a checksum, through a
+ * temporary file and a rename.  lg_weights_load reads net `index`: with
+ * weights == NULL it only reports the description and *count_out (to size a
+ * buffer); with a buffer of `capacity` floats it also copies the weights and
+ * sets desc->weights to that buffer.  Returns the number of nets in the file,
+ * or LG_ERR_ARG with a message (missing file, bad magic or version,
+ * checksum mismatch, truncation, count that does not fit the shape).
+ * Replaces: the compiled-in weight arrays of NN.cpp / NN128.cpp /
+ * NNValue.cpp (declared at Network.cpp:54-137), whose concatenation in
+ * declaration order is exactly the flat lg_net_desc array. */
+LG_API int lg_weights_save(const char *path, const lg_net_desc *descs, const char *const *names, int n);
+LG_API int lg_weights_load(const char *path, int index, lg_net_desc *desc, char *name16, float *weights,
+                           size_t capacity, size_t *count_out);
+
 /* Number of floats in the flat weight array of `desc`. */
 LG_API size_t lg_weight_count(const lg_net_desc *desc);
 
@@ -117,6 +132,17 @@ LG_API int lg_value(lg_ctx *ctx, const uint8_t *planes, int B, float *value);
 LG_API int lg_policy_device(lg_ctx *ctx, const uint8_t *planes, int B, float temperature, float *probs,
                      float *logits, void *stream);
 LG_API int lg_value_device(lg_ctx *ctx, const uint8_t *planes, int B, float *value, void *stream);
+
+/* 8-symmetry ensemble, device pointers, enqueued on `stream`: each of the B
+ * positions (planes [B][c_in][361], unrotated) is evaluated under all 8
+ * symmetries as one batch of 8B (8B <= max_batch); policy results are
+ * un-rotated and averaged to board order (probs [B][361]: the caller keeps
+ * the EMPTY points, as Network.cpp:820-829 does), values averaged
+ * (value [B]).  Replaces: the AVERAGE_ALL branches of get_scored_moves and
+ * get_value (Network.cpp:642-654, 606-615), which run 8 sequential forwards. */
+LG_API int lg_policy_avg8_device(lg_ctx *ctx, const uint8_t *planes, int B, float temperature,
+                                 float *probs, void *stream);
+LG_API int lg_value_avg8_device(lg_ctx *ctx, const uint8_t *planes, int B, float *value, void *stream);
 
 /* Batching server.  lg_submit queues B positions for net LG_NET_POLICY or
  * LG_NET_VALUE and returns at once; `out` (host, [B][361] probabilities at

@@ -57,7 +57,9 @@ _lib_lock = threading.Lock()
 EXPORTS = ["lg_weight_count", "lg_create", "lg_destroy", "lg_last_error", "lg_policy",
            "lg_value", "lg_policy_device", "lg_value_device", "lg_submit", "lg_poll",
            "lg_stats", "lg_inject_fault", "lg_profile", "lg_profile_read",
-           "lg_policy_device_static", "lg_autotune", "lg_tuning", "lg_set_tuning"]
+           "lg_policy_device_static", "lg_autotune", "lg_tuning", "lg_set_tuning",
+           "lg_policy_avg8_device", "lg_value_avg8_device", "lg_weights_save",
+           "lg_weights_load"]
 
 
 def library():
@@ -89,6 +91,11 @@ def library():
             L.lg_autotune.argtypes = [vp, ctypes.c_char_p, i32]
             L.lg_tuning.argtypes = [vp, i32, P(i32), P(i32)]
             L.lg_set_tuning.argtypes = [vp, i32, i32, i32]
+            L.lg_policy_avg8_device.argtypes = [vp, vp, i32, f32, vp, vp]
+            L.lg_weights_save.argtypes = [ctypes.c_char_p, P(_Desc), P(ctypes.c_char_p), i32]
+            L.lg_weights_load.argtypes = [ctypes.c_char_p, i32, P(_Desc), ctypes.c_char_p, vp,
+                                          ctypes.c_size_t, P(ctypes.c_size_t)]
+            L.lg_value_avg8_device.argtypes = [vp, vp, i32, vp, vp]
             L.lg_profile_read.argtypes = [vp, i32, P(ctypes.c_longlong), P(ctypes.c_double)]
             _lib = L
     return _lib
@@ -212,6 +219,17 @@ class Context:
         _check(library().lg_policy_device_static(self._h, planes_ptr, B, temperature, probs_ptr,
                                                  logits_ptr, stream))
 
+    def policy_avg8_device(self, planes_ptr: int, B: int, probs_ptr: int,
+                           temperature: float = 1.0, stream: int | None = None):
+        """AVERAGE_ALL: the 8 symmetries of each position in one batch,
+        un-rotated and averaged on the device (board order)."""
+        _check(library().lg_policy_avg8_device(self._h, planes_ptr, B, temperature, probs_ptr,
+                                               stream))
+
+    def value_avg8_device(self, planes_ptr: int, B: int, value_ptr: int,
+                          stream: int | None = None):
+        _check(library().lg_value_avg8_device(self._h, planes_ptr, B, value_ptr, stream))
+
     def value_device(self, planes_ptr: int, B: int, value_ptr: int, stream: int | None = None):
         _check(library().lg_value_device(self._h, planes_ptr, B, value_ptr, stream))
 
@@ -305,3 +323,35 @@ def get_scored_moves(ctx: Context, planes32: np.ndarray, squares: np.ndarray,
                 val = 0.0
             out.append((val, idx))
     return out
+
+
+# ------------------------------------------------------------------ weight files
+
+def save_weights(path: str, nets):
+    """nets: list of (name, NetDesc).  Writes the checksummed weight file of
+    lg_weights_save."""
+    arr = (_Desc * len(nets))(*[d._struct() for _, d in nets])
+    names = (ctypes.c_char_p * len(nets))(*[n.encode()[:15] for n, _ in nets])
+    _check(library().lg_weights_save(path.encode(), arr, names, len(nets)))
+
+
+def load_weights(path: str):
+    """Returns [(name, NetDesc)] from a file written by save_weights."""
+    L = library()
+    out = []
+    i = 0
+    while True:
+        d = _Desc()
+        name = ctypes.create_string_buffer(16)
+        count = ctypes.c_size_t()
+        n = _check(L.lg_weights_load(path.encode(), i, ctypes.byref(d), name, None, 0,
+                                     ctypes.byref(count)))
+        w = np.empty(count.value, dtype=np.float32)
+        _check(L.lg_weights_load(path.encode(), i, ctypes.byref(d), name, w.ctypes.data, w.size,
+                                 ctypes.byref(count)))
+        out.append((name.value.decode(), NetDesc(w, d.c_in, d.width1, d.width, d.n3x3, d.head_k,
+                                                 d.act, d.act_head, d.value_head, d.fc_hidden,
+                                                 d.value_map, precision=d.precision)))
+        i += 1
+        if i >= n:
+            return out

@@ -151,6 +151,10 @@ struct lg_ctx {
         float *out;
         void *tag;
     };
+    // the worker's two pinned slots (separate from the blocking calls' buffers)
+    uint8_t *srv_planes[2] = {nullptr, nullptr};
+    float *srv_out[2] = {nullptr, nullptr};
+    cudaEvent_t srv_done[2] = {nullptr, nullptr};
     std::thread worker;
     std::mutex qmu;
     std::condition_variable qcv, dcv;
@@ -596,67 +600,152 @@ int next_pow2(int x) {
     return p;
 }
 
+// Launches one server batch whose planes are already in pinned slot `slot`:
+// a CUDA graph per (net, bucket, temperature, slot) holding the copy in, the
+// forward and the copy out; completion is recorded on srv_done[slot].
+int server_launch(lg_ctx *c, int slot, int net, int nb, float T) {
+    Net &n = c->nets[net];
+    const size_t per_in = (size_t)n.d.c_in * kPoints;
+    uint32_t tbits;
+    std::memcpy(&tbits, &T, 4);
+    auto key = std::make_tuple(net, nb, n.d.value_head ? 0u : tbits, 2 + slot);
+    auto it = c->graphs.find(key);
+    if (it == c->graphs.end()) {
+        cudaGraph_t g;
+        LG_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        cudaMemcpyAsync(c->d_planes, c->srv_planes[slot], (size_t)nb * per_in, cudaMemcpyHostToDevice,
+                        c->stream);
+        int nl = 0;
+        int rc = forward(c, net, c->d_planes, nb, T, c->d_probs, nullptr, c->d_value, c->stream, &nl);
+        if (n.d.value_head)
+            cudaMemcpyAsync(c->srv_out[slot], c->d_value, (size_t)nb * sizeof(float), cudaMemcpyDeviceToHost,
+                            c->stream);
+        else
+            cudaMemcpyAsync(c->srv_out[slot], c->d_probs, (size_t)nb * kPoints * sizeof(float),
+                            cudaMemcpyDeviceToHost, c->stream);
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+        if (rc) {
+            if (ce == cudaSuccess) cudaGraphDestroy(g);
+            return rc;
+        }
+        LG_CUDA_TRY(ce);
+        cudaGraphExec_t ge;
+        cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        LG_CUDA_TRY(ie);
+        it = c->graphs.emplace(key, std::make_pair(ge, nl)).first;
+    }
+    LG_CUDA_TRY(cudaGraphLaunch(it->second.first, c->stream));
+    LG_CUDA_TRY(cudaEventRecord(c->srv_done[slot], c->stream));
+    c->launches += it->second.second;
+    return LG_OK;
+}
+
+int server_finish(lg_ctx *c, int slot) {
+    LG_CUDA_TRY(cudaEventSynchronize(c->srv_done[slot]));
+    int herr = 0;
+    LG_CUDA_TRY(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+        cudaMemset(c->d_err, 0, sizeof(int));
+        lg_set_error("kernel reported error status %d", herr);
+        return LG_ERR_DEVICE;
+    }
+    return LG_OK;
+}
+
+// The server thread keeps at most two batches in flight: while batch k runs
+// on the GPU it packs and launches batch k+1 into the other pinned slot,
+// then waits for batch k and hands its results back.
 void worker_main(lg_ctx *c) {
     cudaSetDevice(c->device);
-    std::vector<lg_ctx::Req> batch;
-    std::vector<uint8_t> staging;
-    std::vector<float> out;
+    struct Flight {
+        std::vector<lg_ctx::Req> reqs;
+        int net = 0, slot = 0, rc = LG_OK;
+        bool live = false;
+    } fl[2];
+    int next_slot = 0;
     for (;;) {
-        batch.clear();
+        std::vector<lg_ctx::Req> batch;
+        bool have_inflight = fl[0].live || fl[1].live;
         {
             std::unique_lock<std::mutex> lk(c->qmu);
-            c->qcv.wait(lk, [&] { return c->stop || !c->queue.empty(); });
-            if (c->stop && c->queue.empty()) return;
-            // The oldest request picks the net (and temperature); every queued
-            // request of that kind joins, in arrival order, while it fits.
-            int total = 0;
-            const int net = c->queue.front().net;
-            const float T = c->queue.front().temperature;
-            for (auto it = c->queue.begin(); it != c->queue.end();) {
-                const bool same = it->net == net && (net != LG_NET_POLICY || it->temperature == T);
-                if (!same) {
-                    ++it;
-                    continue;
+            if (!have_inflight) c->qcv.wait(lk, [&] { return c->stop || !c->queue.empty(); });
+            if (c->stop && c->queue.empty() && !have_inflight) return;
+            if (!c->queue.empty()) {
+                // The oldest request picks the net (and temperature); every
+                // queued request of that kind joins, in arrival order, while it fits.
+                int total = 0;
+                const int net = c->queue.front().net;
+                const float T = c->queue.front().temperature;
+                for (auto it = c->queue.begin(); it != c->queue.end();) {
+                    const bool same = it->net == net && (net != LG_NET_POLICY || it->temperature == T);
+                    if (!same) {
+                        ++it;
+                        continue;
+                    }
+                    if (total > 0 && total + it->B > c->max_batch) break;
+                    total += it->B;
+                    batch.push_back(*it);
+                    it = c->queue.erase(it);
                 }
-                if (total > 0 && total + it->B > c->max_batch) break;
-                total += it->B;
-                batch.push_back(*it);
-                it = c->queue.erase(it);
             }
         }
-        int net = batch[0].net;
-        Net &n = c->nets[net];
-        size_t per_in = (size_t)n.d.c_in * kPoints;
-        int total = 0;
-        for (auto &r : batch) total += r.B;
-        int bucket = std::min(next_pow2(total), std::max(total, c->max_batch));
-        staging.assign((size_t)bucket * per_in, 0);
-        size_t off = 0;
-        for (auto &r : batch) {
-            std::memcpy(staging.data() + off, r.planes, (size_t)r.B * per_in);
-            off += (size_t)r.B * per_in;
+        // Launch the new batch (if any) into the free slot.
+        int launched = -1;
+        if (!batch.empty()) {
+            const int slot = fl[next_slot].live ? next_slot ^ 1 : next_slot;
+            Flight &f = fl[slot];
+            f.reqs = std::move(batch);
+            f.net = f.reqs[0].net;
+            f.slot = slot;
+            Net &n = c->nets[f.net];
+            const size_t per_in = (size_t)n.d.c_in * kPoints;
+            int total = 0;
+            for (auto &r : f.reqs) total += r.B;
+            const int bucket = std::min(next_pow2(total), std::max(total, c->max_batch));
+            size_t off = 0;
+            for (auto &r : f.reqs) {
+                std::memcpy(c->srv_planes[slot] + off, r.planes, (size_t)r.B * per_in);
+                off += (size_t)r.B * per_in;
+            }
+            std::memset(c->srv_planes[slot] + off, 0, (size_t)(bucket - total) * per_in);
+            {
+                std::lock_guard<std::mutex> g(c->mu);
+                f.rc = server_launch(c, slot, f.net, bucket, f.reqs[0].temperature);
+            }
+            f.live = true;
+            launched = slot;
+            next_slot = slot ^ 1;
+            c->batches++;
         }
-        int per_out = n.d.value_head ? 1 : kPoints;
-        out.resize((size_t)bucket * per_out);
-        int rc;
-        {
-            std::lock_guard<std::mutex> g(c->mu);
-            rc = run_host(c, net, staging.data(), bucket, batch[0].temperature,
-                          n.d.value_head ? nullptr : out.data(), nullptr,
-                          n.d.value_head ? out.data() : nullptr);
+        // Finish the older batch in flight (not the one just launched), or the
+        // only one when nothing new arrived.
+        for (int k = 0; k < 2; ++k) {
+            Flight &f = fl[k];
+            if (!f.live || k == launched) continue;
+            {
+                int rc = f.rc;
+                if (rc == LG_OK) {
+                    std::lock_guard<std::mutex> g(c->mu);
+                    rc = server_finish(c, f.slot);
+                }
+                const int per_out = c->nets[f.net].d.value_head ? 1 : kPoints;
+                size_t o = 0;
+                for (auto &r : f.reqs) {
+                    if (rc == LG_OK)
+                        std::memcpy(r.out, c->srv_out[f.slot] + o, (size_t)r.B * per_out * sizeof(float));
+                    o += (size_t)r.B * per_out;
+                }
+                {
+                    std::lock_guard<std::mutex> lk(c->qmu);
+                    if (rc != LG_OK) c->worker_error = rc;
+                    for (auto &r : f.reqs) c->done.push_back(r.tag);
+                }
+                c->dcv.notify_all();
+                f.live = false;
+                f.reqs.clear();
+            }
         }
-        c->batches++;
-        size_t o = 0;
-        for (auto &r : batch) {
-            if (rc == LG_OK) std::memcpy(r.out, out.data() + o, (size_t)r.B * per_out * sizeof(float));
-            o += (size_t)r.B * per_out;
-        }
-        {
-            std::lock_guard<std::mutex> lk(c->qmu);
-            if (rc != LG_OK) c->worker_error = rc;
-            for (auto &r : batch) c->done.push_back(r.tag);
-        }
-        c->dcv.notify_all();
     }
 }
 
@@ -691,6 +780,11 @@ extern "C" void lg_destroy(lg_ctx *c) {
     if (c->h_planes) cudaFreeHost(c->h_planes);
     if (c->h_out) cudaFreeHost(c->h_out);
     if (c->h_out2) cudaFreeHost(c->h_out2);
+    for (int i = 0; i < 2; ++i) {
+        if (c->srv_planes[i]) cudaFreeHost(c->srv_planes[i]);
+        if (c->srv_out[i]) cudaFreeHost(c->srv_out[i]);
+        if (c->srv_done[i]) cudaEventDestroy(c->srv_done[i]);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -780,6 +874,14 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
         cudaMallocHost(&c->h_out2, mb * kPoints * sizeof(float)) != cudaSuccess) {
         lg_set_error("cudaMallocHost failed");
         return fail(LG_ERR_ALLOC);
+    }
+    for (int i = 0; i < 2; ++i) {
+        if (cudaMallocHost(&c->srv_planes[i], mb * max_c_in * kPoints) != cudaSuccess ||
+            cudaMallocHost(&c->srv_out[i], mb * kPoints * sizeof(float)) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->srv_done[i], cudaEventDisableTiming) != cudaSuccess) {
+            lg_set_error("cudaMallocHost failed");
+            return fail(LG_ERR_ALLOC);
+        }
     }
     if (cudaDeviceSynchronize() != cudaSuccess) {
         lg_set_error("device error after upload");
@@ -1207,5 +1309,83 @@ extern "C" int lg_set_tuning(lg_ctx *c, int B, int variant_3x3, int variant_firs
     c->tc_variant[bl][1] = variant_first;
     for (auto &gr : c->graphs) cudaGraphExecDestroy(gr.second.first);
     c->graphs.clear();
+    return LG_OK;
+}
+
+// ============================================================================
+// 8-symmetry ensemble (AVERAGE_ALL): B positions -> a batch of 8B rotated
+// copies -> one forward -> un-rotate and average on the device.
+// ============================================================================
+
+namespace {
+std::once_flag g_rot_once[64];
+int g_rot_rc[64];
+
+int ensure_rot_tables(lg_ctx *c) {
+    if (c->device < 0 || c->device >= 64) return LG_ERR_ARG;
+    std::call_once(g_rot_once[c->device], [&] { g_rot_rc[c->device] = ensemble_init_tables(); });
+    return g_rot_rc[c->device];
+}
+}  // namespace
+
+extern "C" int lg_policy_avg8_device(lg_ctx *c, const uint8_t *planes, int B, float temperature,
+                                     float *probs, void *stream) {
+    if (!c || !planes || !probs || B < 0 || !(temperature > 0.0f)) {
+        lg_set_error("lg_policy_avg8_device: bad arguments");
+        return LG_ERR_ARG;
+    }
+    Net &n = c->nets[LG_NET_POLICY];
+    if (!n.present) {
+        lg_set_error("no policy net");
+        return LG_ERR_ARG;
+    }
+    if (B == 0) return LG_OK;
+    if (8 * B > c->max_batch) {
+        lg_set_error("lg_policy_avg8_device: 8 x %d positions exceed max_batch %d", B, c->max_batch);
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    LG_CUDA_TRY(cudaSetDevice(c->device));
+    int rc = ensure_rot_tables(c);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_rotate8(planes, B, n.d.c_in, c->d_planes, s);
+    int nl = 0;
+    rc = forward(c, LG_NET_POLICY, c->d_planes, 8 * B, temperature, c->d_probs, nullptr, nullptr, s, &nl,
+                 c->profiling);
+    if (rc) return rc;
+    launch_unrotate_avg8(c->d_probs, B, probs, s);
+    c->launches += nl + 2;
+    LG_CUDA_TRY(cudaGetLastError());
+    return LG_OK;
+}
+
+extern "C" int lg_value_avg8_device(lg_ctx *c, const uint8_t *planes, int B, float *value, void *stream) {
+    if (!c || !planes || !value || B < 0) {
+        lg_set_error("lg_value_avg8_device: bad arguments");
+        return LG_ERR_ARG;
+    }
+    Net &n = c->nets[LG_NET_VALUE];
+    if (!n.present) {
+        lg_set_error("no value net");
+        return LG_ERR_ARG;
+    }
+    if (B == 0) return LG_OK;
+    if (8 * B > c->max_batch) {
+        lg_set_error("lg_value_avg8_device: 8 x %d positions exceed max_batch %d", B, c->max_batch);
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    LG_CUDA_TRY(cudaSetDevice(c->device));
+    int rc = ensure_rot_tables(c);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_rotate8(planes, B, n.d.c_in, c->d_planes, s);
+    int nl = 0;
+    rc = forward(c, LG_NET_VALUE, c->d_planes, 8 * B, 1.0f, nullptr, nullptr, c->d_value, s, &nl, c->profiling);
+    if (rc) return rc;
+    launch_avg8(c->d_value, B, value, s);
+    c->launches += nl + 2;
+    LG_CUDA_TRY(cudaGetLastError());
     return LG_OK;
 }

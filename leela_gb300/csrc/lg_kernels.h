@@ -68,6 +68,12 @@ int tc_init_device();
 // Head kernels for the tensor-core path (logits already produced by the
 // fused epilogue): same softmax / value FC as FP32.
 
+// 8-symmetry ensemble helpers (ensemble.cu).
+int ensemble_init_tables();
+void launch_rotate8(const uint8_t *in, int B, int C, uint8_t *out, cudaStream_t s);
+void launch_unrotate_avg8(const float *probs, int B, float *avg, cudaStream_t s);
+void launch_avg8(const float *v, int B, float *out, cudaStream_t s);
+
 // Tensor-map encoding through the driver entry point (no -lcuda needed).
 int encode_map_2d_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint64_t rows,
                        uint32_t box_inner, uint32_t box_rows, bool swizzle128 = true);

@@ -121,3 +121,36 @@ def test_device_entry_points_match_host(ctx_cfg, positions):
     ctx_cfg.value_device(pv.data_ptr(), 16, d_v.data_ptr(), s.cuda_stream)
     s.synchronize()
     assert np.abs(d_v.cpu().numpy() - ctx_cfg.value(positions["planes_v"][:16, :24])).max() < 1e-6
+
+
+def test_avg8_ensemble_matches_oracle(gpu_lib, weights, positions, oracle_mod):
+    """AVERAGE_ALL (Network.cpp:642-654, 606-615): the device ensemble equals
+    the average of the 8 rotated oracle evaluations, un-rotated."""
+    import torch
+    lg, O = gpu_lib, oracle_mod
+    B = 3
+    pp = np.ascontiguousarray(positions["planes_p"][:B, :24])
+    pv = np.ascontiguousarray(positions["planes_v"][:B, :24])
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1]),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1]), max_batch=32) as c:
+        out = torch.empty((B, 361), device="cuda")
+        val = torch.empty(B, device="cuda")
+        s = torch.cuda.current_stream()
+        c.policy_avg8_device(torch.from_numpy(pp).cuda().data_ptr(), B, out.data_ptr(), 0.75,
+                             s.cuda_stream)
+        c.value_avg8_device(torch.from_numpy(pv).cuda().data_ptr(), B, val.data_ptr(), s.cuda_stream)
+        s.synchronize()
+    O.enable_blas()
+    try:
+        ref = np.zeros((B, 361))
+        vref = np.zeros(B)
+        for r in range(8):
+            rp = np.stack([O.rotate_planes(x, r) for x in pp])
+            pr = O.softmax_f32(O.forward_f32(weights["cfg_p"][0], weights["cfg_p"][1], rp), 0.75)
+            ref += pr[:, lg.REV_ROTATE[r]]
+            rv = np.stack([O.rotate_planes(x, r) for x in pv])
+            vref += O.forward_f32(weights["cfg_v"][0], weights["cfg_v"][1], rv)
+    finally:
+        O.disable_blas()
+    assert np.abs(out.cpu().numpy() - ref / 8).max() < 1e-6
+    assert np.abs(val.cpu().numpy() - vref / 8).max() < 1e-5
