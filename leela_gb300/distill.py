@@ -349,3 +349,19 @@ def _policy_len(shape):
 def _value_part(params, shape):
     trunk = _policy_len(shape) - shape["width"] - 1
     return np.concatenate([params[:trunk], params[trunk + shape["width"] + 1:]])
+
+
+def heldout_loss(student: Student, planes, target_probs, target_value, value_weight=1.0,
+                 batch=256):
+    """Mean policy KL and value MSE of `student` on device tensors (no update)."""
+    N = planes.shape[0]
+    kl = mse = 0.0
+    n = 0
+    for b0 in range(0, N, batch):
+        nb = min(batch, N - b0)
+        (a, b), _ = student.grads(planes[b0].data_ptr(), nb, target_probs[b0].data_ptr(),
+                                  target_value[b0:].data_ptr(), value_weight)
+        kl += a * nb
+        mse += b * nb
+        n += nb
+    return kl / n, mse / n

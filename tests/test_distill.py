@@ -104,3 +104,36 @@ def test_gate_routes_by_entropy(student_mod, gpu_lib, weights, positions):
         assert np.array_equal(p.cpu().numpy(), cf.policy(pp.cpu().numpy()))
         assert np.array_equal(v.cpu().numpy(), cf.value(pv.cpu().numpy()))
     st.close()
+
+
+def test_training_gains_over_the_untrained_student(student_mod, gpu_lib, weights, positions):
+    """What the trained network buys over having none: trained on the
+    config-4 labels (the full FP32 policy net's softmax, 2*mc_owner-1 values)
+    of positions 0..895, the student approximates the full net on the
+    held-out positions 896..1023 far better than the untrained student:
+    lower policy KL to the full net and lower value error."""
+    import os
+
+    import torch
+    lg = gpu_lib
+    from conftest import GOLDEN
+    mc = np.load(os.path.join(GOLDEN, "mcowner_s0.npz"))["mcowner"]
+    pp = np.ascontiguousarray(positions["planes_p"][:, :24])
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1]), max_batch=256) as c:
+        probs = c.policy(pp, 1.0)
+    d_pp = torch.from_numpy(pp).cuda()
+    d_t = torch.from_numpy(probs).cuda()
+    d_v = torch.from_numpy((2 * mc - 1).astype(np.float32)).cuda()
+    tr, te = slice(0, 896), slice(896, 1024)
+    st = student_mod.Student(max_batch=256)
+    st.init_he(0)
+    before = student_mod.heldout_loss(st, d_pp[te].contiguous(), d_t[te].contiguous(),
+                                      d_v[te].contiguous())
+    student_mod.train(st, d_pp[tr].contiguous(), d_t[tr].contiguous(), d_v[tr].contiguous(),
+                      steps=400, batch=128, lr=1e-3, log_every=100)
+    after = student_mod.heldout_loss(st, d_pp[te].contiguous(), d_t[te].contiguous(),
+                                     d_v[te].contiguous())
+    st.close()
+    print("held-out (KL, value MSE) untrained", before, "trained", after)
+    assert after[0] < 0.5 * before[0]
+    assert after[1] < before[1]
