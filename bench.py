@@ -262,6 +262,8 @@ def run_ours(args, world, rank, local):
     nh, msh = ctx.profile_read(lg.PROF_TC_HEAD)
     nf, msf = ctx.profile_read(lg.PROF_TC_FIRST)
     no, mso = ctx.profile_read(lg.PROF_OTHER)
+    ntr, mstr = ctx.profile_read(lg.PROF_TC_TRUNK)
+    tuning = ctx.tuning(BATCH)
     ctx.profile(False)
     ms_max = max_over_ranks(ms, world)
     value = world * POSITIONS * args.steps / (ms_max / 1e3)
@@ -295,9 +297,17 @@ def run_ours(args, world, rank, local):
         ctx.close()
         return
     peak, hbm, peak_kind = read_peaks()
-    avg3 = ms3 / max(n3, 1) / 1e3
-    flop_launch = FLOP_3X3_PER_POS * BATCH
-    achieved = flop_launch / avg3 / 1e12 if n3 else None
+    if ntr:
+        # persistent kernel: all 11 3x3 layers of one net per launch
+        kernel_name = "tc_trunk_kernel (11 x 3x3 128->128 in one launch, batch 256)"
+        n_dom, ms_dom = ntr, mstr
+        flop_launch = 11 * FLOP_3X3_PER_POS * BATCH
+    else:
+        kernel_name = "tc_convT_kernel<2,0,0> (3x3 128->128, batch 256)"
+        n_dom, ms_dom = n3, ms3
+        flop_launch = FLOP_3X3_PER_POS * BATCH
+    avg3 = ms_dom / max(n_dom, 1) / 1e3
+    achieved = flop_launch / avg3 / 1e12 if n_dom else None
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "tc_conv3x3_b256_traffic.json")
     if os.path.exists(tpath):
@@ -317,13 +327,15 @@ def run_ours(args, world, rank, local):
         "e2e": e2e,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "tc_convT_kernel<2,0,0> (3x3 128->128, batch 256)",
+                     "kernel": kernel_name,
                      "peak_source": f"bf16_tflops_sustained ({peak_kind})",
-                     "launches": n3, "avg_launch_us": avg3 * 1e6,
+                     "launches": n_dom, "avg_launch_us": avg3 * 1e6,
                      "flop_per_launch": flop_launch},
         "kernel_time_share": {
-            "tc_3x3": ms3, "tc_3x3_fused_head": msh, "tc_5x5_first": msf, "other": mso,
-            "launches": {"tc_3x3": n3, "tc_head": nh, "tc_first": nf, "other": no}},
+            "tc_3x3": ms3, "tc_3x3_fused_head": msh, "tc_trunk": mstr, "tc_5x5_first": msf,
+            "other": mso,
+            "launches": {"tc_3x3": n3, "tc_head": nh, "tc_trunk": ntr, "tc_first": nf, "other": no}},
+        "kernel_choice_batch256": tuning,
         "clocks": clk,
         "gpu_launches": gpu_launches,
         "pair_flop_rate_tflops": FLOP_PAIR_PER_POS * value / world / 1e12,

@@ -185,9 +185,11 @@ LG_API int lg_policy_device_static(lg_ctx *ctx, const uint8_t *planes, int B, fl
                                    float *probs, float *logits, void *stream);
 
 /* Autotuner.  For every power-of-two batch bucket up to max_batch, times the
- * context's tensor-core nets with each kernel choice for the 3x3 layers and
- * for the first layer (256-row tiles on the transposed kernel, or 128-row
- * tiles, which put twice as many CTAs on a small batch) and keeps the
+ * context's tensor-core nets with each kernel choice for the 3x3 layers
+ * (0: one launch per layer with 256-row tiles on the transposed kernel,
+ * 1: one launch per layer with 128-row tiles, which put twice as many CTAs
+ * on a small batch, 2: all 3x3 layers in one persistent cooperative launch)
+ * and for the first layer (0: 256-row, 1: 128-row tiles) and keeps the
  * fastest.  With a cache path, a table saved for the same device, SM count
  * and net shapes is loaded instead (unless force), and a new table is saved
  * there (written to a temporary file and renamed).  Without tuning every
@@ -197,7 +199,7 @@ LG_API int lg_policy_device_static(lg_ctx *ctx, const uint8_t *planes, int B, fl
  * not, < 0 on error. */
 LG_API int lg_autotune(lg_ctx *ctx, const char *cache_path, int force);
 LG_API int lg_tuning(lg_ctx *ctx, int B, int *variant_3x3, int *variant_first);
-/* Sets the kernel choice of B's bucket by hand (0 or 1 each, as above). */
+/* Sets the kernel choice of B's bucket by hand (3x3: 0-2, first: 0-1). */
 LG_API int lg_set_tuning(lg_ctx *ctx, int B, int variant_3x3, int variant_first);
 
 /* ---------------------------------------------------------------------
@@ -249,7 +251,8 @@ LG_API int lg_student_forward(lg_student *st, const uint8_t *planes, int B, floa
 #define LG_PROF_TC_FIRST 2 /* tensor-core 5x5 first layer */
 #define LG_PROF_FP32_CONV 3 /* FP32 conv (+ split-K reduction) */
 #define LG_PROF_OTHER 4    /* plane packing, head conv, softmax, value FC */
-#define LG_PROF_KINDS 5
+#define LG_PROF_TC_TRUNK 5 /* persistent kernel running all 3x3 layers (incl. the fused head) */
+#define LG_PROF_KINDS 6
 LG_API int lg_profile(lg_ctx *ctx, int enable);
 LG_API int lg_profile_read(lg_ctx *ctx, int kind, long long *launches, double *total_ms);
 

@@ -99,6 +99,9 @@ struct Net {
     // tensor-core path
     std::vector<TcConv> tc;
     float *tc_head_w = nullptr;  // [width]
+    // all 3x3 layers' weights back to back, for the persistent trunk kernel
+    __nv_bfloat16 *trunk_w = nullptr;  // [n3x3][9][2][128][64]
+    float *trunk_bias = nullptr, *trunk_scale = nullptr;
 };
 
 }  // namespace
@@ -122,6 +125,7 @@ struct lg_ctx {
     float *d_logits = nullptr, *d_probs = nullptr, *d_value = nullptr;
     float *d_parts = nullptr;  // fused-head partial sums, [4][max_batch * 361]
     float *d_fcpart = nullptr; // value-head FC partial sums
+    int *d_flags = nullptr;    // per-CTA layer flags of the persistent trunk kernel
     uint8_t *h_planes = nullptr;
     float *h_out = nullptr, *h_out2 = nullptr;
     int planes_c = 0;
@@ -303,6 +307,25 @@ int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
             if (fp8 && (rc = upload(c, &t.scale, scale))) return rc;
             n.tc.push_back(t);
         }
+        // The 3x3 layers again as one array for the persistent trunk kernel.
+        if (d->width == 128 && ntrunk > 1) {
+            const size_t per = (size_t)9 * 2 * 128 * 64;
+            const int nl = ntrunk - 1;
+            rc = dev_alloc(c, &n.trunk_w, per * nl);
+            if (!rc) rc = dev_alloc(c, &n.trunk_bias, (size_t)nl * 128);
+            if (!rc && fp8) rc = dev_alloc(c, &n.trunk_scale, (size_t)nl * 128);
+            if (rc) return rc;
+            for (int l = 1; l < ntrunk; ++l) {
+                const TcConv &t = n.tc[l];
+                LG_CUDA_TRY(cudaMemcpy(n.trunk_w + per * (l - 1), t.w, per * sizeof(__nv_bfloat16),
+                                       cudaMemcpyDeviceToDevice));
+                LG_CUDA_TRY(cudaMemcpy(n.trunk_bias + 128 * (l - 1), t.bias, 128 * sizeof(float),
+                                       cudaMemcpyDeviceToDevice));
+                if (fp8)
+                    LG_CUDA_TRY(cudaMemcpy(n.trunk_scale + 128 * (l - 1), t.scale, 128 * sizeof(float),
+                                           cudaMemcpyDeviceToDevice));
+            }
+        }
         // Fused 1x1 head weights, BF16-rounded as the precision states.
         std::vector<float> hw(Wraw.back());
         for (auto &v : hw) v = __bfloat162float(__float2bfloat16(v));
@@ -432,10 +455,32 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
     int bl = 0;
     while ((1 << bl) < B && bl < 16) ++bl;
     const int var3 = c->tc_variant[bl][0], var1 = c->tc_variant[bl][1];
+    const bool use_trunk = var3 == 2 && n.trunk_w != nullptr;
     int cur = 0;
     for (size_t l = 0; l < n.tc.size(); ++l) {
         const TcConv &t = n.tc[l];
         const bool last = l + 1 == n.tc.size();
+        if (use_trunk && l == 1) {
+            // layers 1 .. end in one persistent launch; layer 0 wrote l3[0]
+            TcTrunk tt{};
+            tt.buf_a = c->l3[0];
+            tt.buf_b = c->l3[1];
+            tt.w = n.trunk_w;
+            tt.bias = n.trunk_bias;
+            tt.scale = n.trunk_scale;
+            tt.head_w = n.tc_head_w;
+            tt.act = d.act;
+            tt.rows = B * kL3Board;
+            tt.nl = (int)n.tc.size() - 1;
+            int rc;
+            {
+                ProfScope ps(c, prof, LG_PROF_TC_TRUNK, s);
+                rc = launch_tc_trunk(tt, c->d_parts, part_stride, c->d_flags, c->d_err, s, c->sm_count);
+            }
+            if (rc) return rc;
+            L += 2;
+            break;
+        }
         TcLayer tl{};
         tl.in = (l == 0) ? (const void *)c->l5 : (const void *)c->l3[cur];
         tl.w = t.w;
@@ -461,7 +506,8 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
     }
     {
         ProfScope ps(c, prof, LG_PROF_OTHER, s);
-        HeadIn h{c->d_parts, tc_head_parts(d.width, var3), part_stride, n.head_b, d.act_head, d.act, lg};
+        HeadIn h{c->d_parts, tc_head_parts(d.width, use_trunk ? 0 : var3), part_stride, n.head_b, d.act_head,
+                 d.act, lg};
         if (!d.value_head)
             launch_softmax(h, B, T, probs, s);
         else
@@ -866,7 +912,8 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
         (rc = dev_alloc(c, &c->d_probs, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)) ||
         (rc = dev_alloc(c, &c->d_parts, 4 * mb * kPoints)) ||
-        (rc = dev_alloc(c, &c->d_fcpart, value_fc_part_floats(max_batch, 4096))))
+        (rc = dev_alloc(c, &c->d_fcpart, value_fc_part_floats(max_batch, 4096))) ||
+        (rc = dev_alloc(c, &c->d_flags, 1024)))
         return fail(rc);
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(LG_ERR_CUDA);
     if (cudaMallocHost(&c->h_planes, mb * max_c_in * kPoints) != cudaSuccess ||
@@ -1182,14 +1229,14 @@ bool load_tuning(lg_ctx *c, const char *path) {
     return true;
 }
 
-int save_tuning(lg_ctx *c, const char *path, const double (*ms)[4]) {
+int save_tuning(lg_ctx *c, const char *path, const double (*ms)[6]) {
     std::string tmp = std::string(path) + ".tmp";
     FILE *f = fopen(tmp.c_str(), "w");
     if (!f) {
         lg_set_error("cannot write %s", tmp.c_str());
         return LG_ERR_ARG;
     }
-    fprintf(f, "{\n \"key\": \"%s\",\n \"order\": \"[3x3 layers, first layer] 0 = 256-row transposed, 1 = 128-row\",\n \"table\": {",
+    fprintf(f, "{\n \"key\": \"%s\",\n \"order\": \"[3x3 layers: 0 = 256-row transposed per layer, 1 = 128-row per layer, 2 = persistent trunk; first layer: 0 = 256-row, 1 = 128-row]; ms_per_forward for (3x3, first) = (0,0) (1,0) (2,0) (0,1) (1,1) (2,1)\",\n \"table\": {",
             tune_key(c).c_str());
     bool first = true;
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16; ++b) {
@@ -1200,8 +1247,8 @@ int save_tuning(lg_ctx *c, const char *path, const double (*ms)[4]) {
     fprintf(f, "\n },\n \"ms_per_forward\": {");
     first = true;
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16; ++b) {
-        fprintf(f, "%s\n  \"%d\": [%.4f, %.4f, %.4f, %.4f]", first ? "" : ",", 1 << b, ms[b][0], ms[b][1],
-                ms[b][2], ms[b][3]);
+        fprintf(f, "%s\n  \"%d\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]", first ? "" : ",", 1 << b, ms[b][0],
+                ms[b][1], ms[b][2], ms[b][3], ms[b][4], ms[b][5]);
         first = false;
     }
     fprintf(f, "\n }\n}\n");
@@ -1235,15 +1282,15 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
     LG_CUDA_TRY(cudaEventCreate(&e0));
     LG_CUDA_TRY(cudaEventCreate(&e1));
     LG_CUDA_TRY(cudaMemsetAsync(c->d_planes, 0, (size_t)c->max_batch * c->planes_c * kPoints, c->stream));
-    double ms[17][4] = {};
+    double ms[17][6] = {};
     int rc = LG_OK;
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16 && rc == LG_OK; ++b) {
         const int B = 1 << b;
         double best = 1e30;
         int best_v = 0;
-        for (int v = 0; v < 4 && rc == LG_OK; ++v) {
-            c->tc_variant[b][0] = v & 1;
-            c->tc_variant[b][1] = v >> 1;
+        for (int v = 0; v < 6 && rc == LG_OK; ++v) {
+            c->tc_variant[b][0] = v % 3;
+            c->tc_variant[b][1] = v / 3;
             const int reps = B >= 64 ? 5 : 20;
             float t = 0.0f;
             for (int it = 0; it < 2 + reps && rc == LG_OK; ++it) {
@@ -1265,8 +1312,8 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
                 best_v = v;
             }
         }
-        c->tc_variant[b][0] = best_v & 1;
-        c->tc_variant[b][1] = best_v >> 1;
+        c->tc_variant[b][0] = best_v % 3;
+        c->tc_variant[b][1] = best_v / 3;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1298,7 +1345,7 @@ extern "C" int lg_tuning(lg_ctx *c, int B, int *variant_3x3, int *variant_first)
 }
 
 extern "C" int lg_set_tuning(lg_ctx *c, int B, int variant_3x3, int variant_first) {
-    if (!c || B < 1 || variant_3x3 < 0 || variant_3x3 > 1 || variant_first < 0 || variant_first > 1) {
+    if (!c || B < 1 || variant_3x3 < 0 || variant_3x3 > 2 || variant_first < 0 || variant_first > 1) {
         lg_set_error("lg_set_tuning: bad arguments");
         return LG_ERR_ARG;
     }

@@ -63,6 +63,23 @@ void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv
 int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *parts, size_t part_stride,
                    int *err, cudaStream_t s, int sm_count);
 int tc_head_parts(int n, int variant = 0);
+
+// All 3x3 128->128 layers of a net in one persistent, cooperative launch
+// (tc_trunk_kernel): layer l reads buf_a when l is even and buf_b when odd,
+// and writes the other; the last layer writes head partial sums (4 parts)
+// when head_w is set.  flags: >= sm_count ints of device scratch.
+struct TcTrunk {
+    const void *buf_a, *buf_b;  // L3 activation buffers [rows][128] BF16
+    const void *w;              // [nl][9][2][128][64] BF16
+    const float *bias;          // [nl][128]
+    const float *scale;         // [nl][128] or null
+    const float *head_w;        // [128] or null
+    int act;
+    int rows;
+    int nl;
+};
+int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
+                    cudaStream_t s, int sm_count);
 size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves);
 int tc_init_device();
 // Head kernels for the tensor-core path (logits already produced by the

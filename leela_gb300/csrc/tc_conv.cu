@@ -351,6 +351,16 @@ __device__ __forceinline__ float warp_transpose_sum(float (&a)[32], int lane) {
     return a[0];
 }
 
+// Kernel T work split: the rows are cut into 32-row blocks, each CTA takes
+// an even contiguous range of blocks and walks it in chunks of up to 256 rows
+// (the MMA's N is the chunk's row count), so that no SM runs a whole extra
+// 256-row tile at the end of the grid.
+__device__ __forceinline__ void cta_row_range(int rows, int &r0, int &r1) {
+    const int nblk = (rows + 31) / 32;
+    r0 = (int)(((long long)nblk * blockIdx.x) / gridDim.x) * 32;
+    r1 = (int)(((long long)nblk * (blockIdx.x + 1)) / gridDim.x) * 32;
+}
+
 template <int HALVES, int KIND, bool HEAD>
 __global__ void __launch_bounds__(kTcThreadsT, 1)
     tc_convT_kernel(const __grid_constant__ CUtensorMap in_map,
@@ -409,8 +419,10 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         // ------------------------------------------------ TMA producer
         if (lane == 0) {
             uint32_t g = 0, wn = 0;
-            for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag; tile += gridDim.x) {
-                const int row0 = tile * C::TP - C::WPRE;
+            int r0, r1;
+            cta_row_range(p.rows, r0, r1);
+            for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP) {
+                const int row0 = cs - C::WPRE;
                 for (int h = 0; h < HALVES; ++h, ++wn) {
                     const int ws = wn % C::NWIN;
                     const uint32_t wk = wn / C::NWIN;
@@ -434,11 +446,13 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_bf16(128, C::TP);
             uint32_t g = 0, wn = 0;
             int local = 0;
-            for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag;
-                 tile += gridDim.x, ++local) {
+            int r0, r1;
+            cta_row_range(p.rows, r0, r1);
+            for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP, ++local) {
+                const int nrows = min(C::TP, r1 - cs);
+                const uint32_t idesc = idesc_bf16(128, nrows);
                 const int acc = local & 1;
                 const uint32_t ak = (uint32_t)(local >> 1);
                 if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(51); break; }
@@ -482,14 +496,21 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         const float scale = p.scale ? __ldg(p.scale + o) : 1.0f;
         const float hw = HEAD ? __ldg(p.head_w + o) : 0.0f;
         int local = 0;
-        for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag; tile += gridDim.x, ++local) {
+        uint32_t uses = 0;  // staging buffer uses of this row group (same for its 4 warps)
+        int r0, r1;
+        cta_row_range(p.rows, r0, r1);
+        for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP, ++local) {
+            const int nrows = min(C::TP, r1 - cs);
+            const int nhalf = max(0, min(2, (nrows - rq * 64) / 32));  // 32-row halves of this group
             const int acc = local & 1;
             const uint32_t ak = (uint32_t)(local >> 1);
             if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(61); break; }
             tc_fence_after();
             const uint32_t t_base = tmem + ((uint32_t)(quarter * 32) << 16) +
                                     (uint32_t)(acc * C::TP + rq * 64);
-            const int q_base = tile * C::TP + rq * 64;
+            const int q_base = cs + rq * 64;
+            // (columns past the chunk are read but unused: the accumulator
+            // holds 256 columns whatever the chunk's N)
             uint32_t v[2][32];
             tmem_ld32(t_base, v[0]);
             tmem_ld32(t_base + 32, v[1]);
@@ -500,6 +521,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
             if (lane == 0) mbar_arrive(&acc_empty[acc]);
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
+                if (c >= nhalf) break;
                 float f[32];
 #pragma unroll
                 for (int j = 0; j < 32; ++j) f[j] = act_apply(fmaf(__uint_as_float(v[c][j]), scale, bias), p.act);
@@ -515,7 +537,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                     // Rows q_base + c*32 .. +31 -> staging buffer of this row
                     // group as [32 rows][128 channels] BF16 (pad rows 0), then
                     // one TMA store by the group's quarter-0 warp.
-                    const uint32_t use = (uint32_t)(local * 2 + c);
+                    const uint32_t use = uses++;
                     uint8_t *buf = stg + rq * C::STG_BYTES;
                     if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) { fail(62); break; }
                     const int row_lane = q_base + c * 32 + lane;
@@ -563,6 +585,286 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
     }
 
     if (C::STAGED && !HEAD && warp >= 2 && (warp & 3) == 0 && lane == 0) bulk_wait0();
+    __syncthreads();
+    if (abort_flag && tid == 0) {
+        for (int i = 0; i < C::NWIN; ++i) {
+            mbar_wait(&win_full[i], 0, 1u << 16);
+            mbar_wait(&win_full[i], 1, 1u << 16);
+        }
+        for (int i = 0; i < C::S; ++i) {
+            mbar_wait(&w_full[i], 0, 1u << 16);
+            mbar_wait(&w_full[i], 1, 1u << 16);
+        }
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) tmem_dealloc(tmem, 512);
+    if (warp == 1) tmem_relinquish();
+}
+
+// ===========================================================================
+// Kernel "trunk": every 3x3 128->128 layer of a net in one persistent
+// launch.  Each CTA owns the same contiguous row range in every layer and
+// runs kernel T's pipeline over it, layer after layer, ping-ponging between
+// two L3 buffers (layer l reads A when l is even, B when odd).  Layer l+1 of
+// CTA k reads rows up to 24 past its range, which CTAs k-1 and k+1 wrote, and
+// overwrites rows its neighbours read for layer l: so CTA k starts layer l+1
+// once CTAs k-1, k, k+1 have finished layer l.  A CTA publishes "layer l done"
+// in flags[k] (release, after its TMA stores completed); the producer polls
+// its neighbours' flags (acquire, bounded) before the first window load of a
+// layer.  The launch is cooperative so that all CTAs are resident.  The last
+// layer can carry the fused 1x1 head.
+// ===========================================================================
+
+struct TrunkParams {
+    const float *bias;    // [nl][128]
+    const float *scale;   // [nl][128] or null
+    const float *head_w;  // [128] (HEAD)
+    int act;
+    int rows;
+    int nl;
+    float *parts;
+    size_t part_stride;
+    int *flags;           // [gridDim.x], zero at launch
+    int *err;
+};
+
+constexpr uint32_t kFlagPolls = 1u << 22;  // x ~64 ns sleep: bounded at ~0.3 s
+
+template <bool HEAD>
+__global__ void __launch_bounds__(kTcThreadsT, 1)
+    tc_trunk_kernel(const __grid_constant__ CUtensorMap in_a, const __grid_constant__ CUtensorMap in_b,
+                    const __grid_constant__ CUtensorMap out_a, const __grid_constant__ CUtensorMap out_b,
+                    const __grid_constant__ CUtensorMap w_map, const TrunkParams p) {
+    using C = TcTCfg<2, 0>;
+    constexpr int HALVES = 2, KIND = 0, NO = 128;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *win = smem;
+    uint8_t *stg = smem + C::NWIN * C::WIN_HALF;
+    uint8_t *wst = stg + C::STG_TOTAL;
+
+    __shared__ uint64_t win_full[C::NWIN], win_empty[C::NWIN], w_full[C::S], w_empty[C::S];
+    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], layer_done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    if (tid == 0) {
+        for (int i = 0; i < C::NWIN; ++i) {
+            mbar_init(&win_full[i], 1);
+            mbar_init(&win_empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], kEpiWarpsT);
+        }
+        for (int i = 0; i < 4; ++i) {
+            mbar_init(&stg_full[i], 4);
+            mbar_init(&stg_empty[i], 1);
+        }
+        for (int i = 0; i < C::S; ++i) {
+            mbar_init(&w_full[i], 1);
+            mbar_init(&w_empty[i], 1);
+        }
+        mbar_init(&layer_done, 4);
+        abort_flag = 0;
+        fence_mbar_init();
+        prefetch_tensormap(&in_a);
+        prefetch_tensormap(&in_b);
+        prefetch_tensormap(&out_a);
+        prefetch_tensormap(&out_b);
+        prefetch_tensormap(&w_map);
+    }
+    if (warp == 1) tmem_alloc(&tmem_base, 512);
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    auto fail = [&](int code) {
+        atomicCAS(p.err, 0, code);
+        atomicExch(&abort_flag, 1);
+    };
+    int r0, r1;
+    cta_row_range(p.rows, r0, r1);
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            uint32_t g = 0, wn = 0;
+            for (int l = 0; l < p.nl && !abort_flag; ++l) {
+                const CUtensorMap *im = (l & 1) ? &in_b : &in_a;
+                if (l > 0) {
+                    // neighbours (and this CTA) finished layer l-1
+                    const int lo = max(0, (int)blockIdx.x - 1), hi = min((int)gridDim.x - 1, (int)blockIdx.x + 1);
+                    for (int j = lo; j <= hi; ++j) {
+                        uint32_t n = 0;
+                        while (ld_acquire_gpu(p.flags + j) < l && ++n < kFlagPolls) __nanosleep(64);
+                        if (n >= kFlagPolls) {
+                            fail(71);
+                            goto done_producer;
+                        }
+                    }
+                    fence_proxy_async_global();
+                }
+                for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP) {
+                    const int row0 = cs - C::WPRE;
+                    for (int h = 0; h < HALVES; ++h, ++wn) {
+                        const int ws = wn % C::NWIN;
+                        const uint32_t wk = wn / C::NWIN;
+                        if (!mbar_wait(&win_empty[ws], (wk & 1) ^ 1, kWaitLimit)) { fail(72); goto done_producer; }
+                        mbar_arrive_expect_tx(&win_full[ws], C::WIN_HALF);
+                        for (int sb = 0; sb < 2; ++sb)
+                            tma_load_2d(win + ws * C::WIN_HALF + sb * C::SUBROWS * 128, im, &win_full[ws],
+                                        h * 64, row0 + sb * C::SUBROWS);
+                        for (int t = 0; t < C::NTAPS; ++t, ++g) {
+                            const int s = g % C::S;
+                            const uint32_t k = g / C::S;
+                            if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(73); goto done_producer; }
+                            mbar_arrive_expect_tx(&w_full[s], C::WST_BYTES);
+                            tma_load_2d(wst + s * C::WST_BYTES, &w_map, &w_full[s], 0,
+                                        ((l * C::NTAPS + t) * HALVES + h) * NO);
+                        }
+                    }
+                }
+            }
+        done_producer:;
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            uint32_t g = 0, wn = 0;
+            int local = 0;
+            for (int l = 0; l < p.nl && !abort_flag; ++l) {
+                for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP, ++local) {
+                    const int nrows = min(C::TP, r1 - cs);
+                    const uint32_t idesc = idesc_bf16(128, nrows);
+                    const int acc = local & 1;
+                    const uint32_t ak = (uint32_t)(local >> 1);
+                    if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(74); goto done_mma; }
+                    tc_fence_after();
+                    const uint32_t d_tmem = tmem + (uint32_t)(acc * C::TP);
+                    bool first = true;
+                    for (int h = 0; h < HALVES; ++h, ++wn) {
+                        const int ws = wn % C::NWIN;
+                        const uint32_t wk = wn / C::NWIN;
+                        if (!mbar_wait(&win_full[ws], wk & 1, kWaitLimit)) { fail(75); goto done_mma; }
+                        tc_fence_after();
+                        const uint32_t win_addr = smem_u32(win + ws * C::WIN_HALF);
+                        for (int t = 0; t < C::NTAPS; ++t, ++g) {
+                            const int s = g % C::S;
+                            const uint32_t k = g / C::S;
+                            if (!mbar_wait(&w_full[s], k & 1, kWaitLimit)) { fail(76); goto done_mma; }
+                            tc_fence_after();
+                            const uint32_t a_base = smem_u32(wst + s * C::WST_BYTES);
+                            const uint32_t b_base = win_addr + (uint32_t)(C::WPRE + tap_shift(KIND, t)) * 128u;
+#pragma unroll
+                            for (int kk = 0; kk < 4; ++kk) {
+                                mma_bf16(d_tmem, sdesc_sw128(a_base + kk * 32), sdesc_sw128(b_base + kk * 32),
+                                         idesc, first ? 0u : 1u);
+                                first = false;
+                            }
+                            mma_commit(&w_empty[s]);
+                        }
+                        mma_commit(&win_empty[ws]);
+                    }
+                    mma_commit(&acc_full[acc]);
+                }
+            }
+        done_mma:;
+        }
+    } else {
+        // ------------------------------------------------ epilogue
+        const int quarter = warp & 3;
+        const int rq = (warp - 2) >> 2;
+        const int o = quarter * 32 + lane;
+        const float hw = HEAD ? __ldg(p.head_w + o) : 0.0f;
+        int local = 0;
+        uint32_t uses = 0;
+        for (int l = 0; l < p.nl && !abort_flag; ++l) {
+            const float bias = __ldg(p.bias + l * NO + o);
+            const float scale = p.scale ? __ldg(p.scale + l * NO + o) : 1.0f;
+            const bool head_layer = HEAD && l == p.nl - 1;
+            const CUtensorMap *om = (l & 1) ? &out_a : &out_b;
+            for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP, ++local) {
+                const int nrows = min(C::TP, r1 - cs);
+                const int nhalf = max(0, min(2, (nrows - rq * 64) / 32));
+                const int acc = local & 1;
+                const uint32_t ak = (uint32_t)(local >> 1);
+                if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(77); break; }
+                tc_fence_after();
+                const uint32_t t_base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * C::TP + rq * 64);
+                const int q_base = cs + rq * 64;
+                uint32_t v[2][32];
+                tmem_ld32(t_base, v[0]);
+                tmem_ld32(t_base + 32, v[1]);
+                tmem_ld_wait();
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[acc]);
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    if (c >= nhalf) break;
+                    float f[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) f[j] = act_apply(fmaf(__uint_as_float(v[c][j]), scale, bias), p.act);
+                    if (head_layer) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) f[j] *= hw;
+                        const float sum = warp_transpose_sum(f, lane);
+                        int orow, point;
+                        bool valid;
+                        row_target<KIND>(q_base + c * 32 + lane, p.rows, orow, valid, point);
+                        if (valid) p.parts[(size_t)quarter * p.part_stride + point] = sum;
+                    } else {
+                        const uint32_t use = uses++;
+                        uint8_t *buf = stg + rq * C::STG_BYTES;
+                        if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) { fail(78); break; }
+                        const int row_lane = q_base + c * 32 + lane;
+                        const int rl = row_lane % kL3Board;
+                        const bool valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
+                        const unsigned vmask = __ballot_sync(0xffffffffu, valid_lane);
+                        __nv_bfloat16 *col = reinterpret_cast<__nv_bfloat16 *>(buf) + o;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            col[j * 128] = __float2bfloat16_rn(((vmask >> j) & 1u) ? f[j] : 0.0f);
+                        fence_proxy_async();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&stg_full[rq]);
+                        if (quarter == 0 && lane == 0) {
+                            if (!mbar_wait(&stg_full[rq], use & 1, kWaitLimit)) {
+                                fail(79);
+                            } else {
+                                tma_store_2d(om, buf, 0, q_base + c * 32);
+                                bulk_commit();
+                                bulk_wait_read0();
+                            }
+                            mbar_arrive(&stg_empty[rq]);
+                        }
+                        __syncwarp();
+                    }
+                }
+            }
+            if (!head_layer) {
+                // Publish "layer l done" once all of this CTA's stores of it
+                // have completed.
+                if (quarter == 0 && lane == 0) {
+                    bulk_wait0();
+                    mbar_arrive(&layer_done);
+                }
+                if (warp == 4 && lane == 0) {
+                    if (!mbar_wait(&layer_done, (uint32_t)(l & 1), kWaitLimit)) {
+                        fail(80);
+                    } else {
+                        fence_proxy_async_global();
+                        __threadfence();
+                        st_release_gpu(p.flags + blockIdx.x, l + 1);
+                    }
+                }
+            }
+        }
+    }
+
     __syncthreads();
     if (abort_flag && tid == 0) {
         for (int i = 0; i < C::NWIN; ++i) {
@@ -656,6 +958,8 @@ int tc_init_device() {
     LG_A(64, 1, 0, false) LG_A(64, 1, 0, true) LG_A(64, 2, 1, false) LG_A(64, 3, 1, false)
     LG_A(128, 3, 1, false) LG_A(128, 2, 0, false) LG_A(128, 2, 0, true) LG_A(128, 2, 1, false)
     LG_T(2, 0, false) LG_T(2, 0, true) LG_T(2, 1, false)
+    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<false>), TcTCfg<2, 0>::SMEM>(tc_trunk_kernel<false>);
+    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<true>), TcTCfg<2, 0>::SMEM>(tc_trunk_kernel<true>);
 #undef LG_A
 #undef LG_T
     return rc;
@@ -686,9 +990,58 @@ static int launch_t(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) 
     if (!rc && Cfg::STAGED && !HEAD)
         rc = encode_map_2d_bf16(&out_map, p.out, 128, (uint64_t)L.rows, 128, 32, /*swizzle=*/false);
     if (rc) return rc;
-    p.ntiles = (L.rows + Cfg::TP - 1) / Cfg::TP;
+    p.ntiles = (L.rows + 31) / 32;  // 32-row blocks, split evenly over the CTAs
     int grid = std::min(p.ntiles, sm_count);
     tc_convT_kernel<HALVES, KIND, HEAD><<<grid, kTcThreadsT, Cfg::SMEM, s>>>(in_map, w_map, out_map, p);
+    return LG_OK;
+}
+
+int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
+                    cudaStream_t s, int sm_count) {
+    using Cfg = TcTCfg<2, 0>;
+    if (T.nl < 1 || T.rows <= 0 || (T.head_w && !parts)) {
+        lg_set_error("launch_tc_trunk: bad arguments");
+        return LG_ERR_ARG;
+    }
+    CUtensorMap in_a, in_b, out_a, out_b, w_map;
+    int rc = encode_map_2d_bf16(&in_a, T.buf_a, 128, (uint64_t)T.rows, 64, Cfg::SUBROWS);
+    if (!rc) rc = encode_map_2d_bf16(&in_b, T.buf_b, 128, (uint64_t)T.rows, 64, Cfg::SUBROWS);
+    if (!rc) rc = encode_map_2d_bf16(&out_a, T.buf_a, 128, (uint64_t)T.rows, 128, 32, false);
+    if (!rc) rc = encode_map_2d_bf16(&out_b, T.buf_b, 128, (uint64_t)T.rows, 128, 32, false);
+    if (!rc) rc = encode_map_2d_bf16(&w_map, T.w, 64, (uint64_t)T.nl * Cfg::NTAPS * 2 * 128, 64, 128);
+    if (rc) return rc;
+    TrunkParams p{};
+    p.bias = T.bias;
+    p.scale = T.scale;
+    p.head_w = T.head_w;
+    p.act = T.act;
+    p.rows = T.rows;
+    p.nl = T.nl;
+    p.parts = parts;
+    p.part_stride = part_stride;
+    p.flags = flags;
+    p.err = err;
+    const int grid = std::min((T.rows + 31) / 32, sm_count);
+    if (cudaMemsetAsync(flags, 0, sizeof(int) * grid, s) != cudaSuccess) {
+        lg_set_error("launch_tc_trunk: flag reset failed");
+        return LG_ERR_CUDA;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kTcThreadsT);
+    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = T.head_w ? cudaLaunchKernelEx(&cfg, tc_trunk_kernel<true>, in_a, in_b, out_a, out_b, w_map, p)
+                             : cudaLaunchKernelEx(&cfg, tc_trunk_kernel<false>, in_a, in_b, out_a, out_b, w_map, p);
+    if (e != cudaSuccess) {
+        lg_set_error("trunk launch: %s", cudaGetErrorString(e));
+        return LG_ERR_CUDA;
+    }
     return LG_OK;
 }
 

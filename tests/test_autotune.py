@@ -24,7 +24,7 @@ def f64(positions, weights, oracle_mod):
     return lp, v
 
 
-@pytest.mark.parametrize("v3,v1", [(0, 0), (1, 0), (0, 1), (1, 1)])
+@pytest.mark.parametrize("v3,v1", [(0, 0), (1, 0), (0, 1), (1, 1), (2, 0), (2, 1)])
 @pytest.mark.parametrize("B", [1, 5, 64])
 def test_every_variant_meets_the_bf16_bars(gpu_lib, weights, positions, f64, v3, v1, B):
     lg = gpu_lib
@@ -59,3 +59,20 @@ def test_autotune_writes_and_reloads_its_cache(gpu_lib, weights, positions, tmp_
     with lg.Context(**kw) as c2:
         c2.autotune(path)  # loads, no timing
         assert {b: c2.tuning(b) for b in table} == table
+
+
+@pytest.mark.parametrize("B", [1, 3, 64])
+def test_fp8_trunk_matches_per_layer_kernels(gpu_lib, weights, positions, B):
+    """The persistent trunk kernel (3x3 choice 2) computes the same layers as
+    the per-layer launches, FP8 weights (per-channel scales) included."""
+    lg = gpu_lib
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "fp8w"),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], "fp8w"), max_batch=64) as c:
+        c.set_tuning(B, 0, 0)
+        p0, l0 = c.policy(positions["planes_p"][:B, :24], 1.0, return_logits=True)
+        v0 = c.value(positions["planes_v"][:B, :24])
+        c.set_tuning(B, 2, 0)
+        p2, l2 = c.policy(positions["planes_p"][:B, :24], 1.0, return_logits=True)
+        v2 = c.value(positions["planes_v"][:B, :24])
+    assert rel_logit_err(l2, l0).max() < 1e-5
+    assert np.abs(v2 - v0).max() < 1e-5
