@@ -260,62 +260,45 @@ __global__ void __launch_bounds__(384) softmax_kernel(const HeadIn h, int B, flo
 // board's partial w2 . hidden over its 64 units; value_final_kernel adds the
 // partials in a fixed order, b2, and applies the value map.  w1t is W1
 // transposed to [361][H].
-constexpr int kFcBM = 16, kFcBN = 64, kFcBK = 32;
+constexpr int kFcBM = 4, kFcBN = 64;
 
+// One CTA = 4 boards x 64 hidden units (thread = one board's hidden unit):
+// the 4 boards' 361 head outputs are formed once in shared memory, then each
+// thread runs the K = 361 dot product with W1t read coalesced across threads.
 __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
                                                         const float *__restrict__ w1t,
                                                         const float *__restrict__ b1,
                                                         const float *__restrict__ w2, int H,
                                                         int act, float *__restrict__ part) {
-    __shared__ float Xs[kFcBK][kFcBM + 1];
-    __shared__ float Ws[kFcBK][kFcBN];
+    __shared__ float Xs[kFcBM][kPoints];
+    __shared__ float red[kFcBM][2];
     const int tid = threadIdx.x;
-    const int tx = tid % 16, ty = tid / 16;  // hidden tx + 16j (j<4), board ty
+    const int n = tid % kFcBN, bb = tid / kFcBN;
     const int b0 = blockIdx.x * kFcBM, n0 = blockIdx.y * kFcBN;
-    float acc[1][4] = {};
-    for (int k0 = 0; k0 < kPoints; k0 += kFcBK) {
-        for (int i = tid; i < kFcBK * kFcBM; i += 256) {
-            const int kk = i % kFcBK, bb = i / kFcBK;  // consecutive threads read consecutive points
-            const int b = b0 + bb, k = k0 + kk;
-            float x = 0.0f;
-            if (b < B && k < kPoints) {
-                x = head_value(h, b, k);
-                if (h.logits_out && blockIdx.y == 0) h.logits_out[(size_t)b * kPoints + k] = x;
-            }
-            Xs[kk][bb] = x;
+    for (int i = tid; i < kFcBM * kPoints; i += 256) {
+        const int bi = i / kPoints, k = i % kPoints;
+        float x = 0.0f;
+        if (b0 + bi < B) {
+            x = head_value(h, b0 + bi, k);
+            if (h.logits_out && blockIdx.y == 0) h.logits_out[(size_t)(b0 + bi) * kPoints + k] = x;
         }
-        for (int i = tid; i < kFcBK * kFcBN; i += 256) {
-            const int kk = i / kFcBN, n = i % kFcBN;
-            const int k = k0 + kk;
-            Ws[kk][n] = (k < kPoints && n0 + n < H) ? w1t[(size_t)k * H + n0 + n] : 0.0f;
-        }
-        __syncthreads();
+        Xs[bi][k] = x;
+    }
+    __syncthreads();
+    const int col = n0 + n;
+    float acc = 0.0f;
+    if (col < H) {
+        const float *w = w1t + col;
 #pragma unroll 8
-        for (int kk = 0; kk < kFcBK; ++kk) {
-            float w[4];
-            const float a = Xs[kk][ty];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) w[j] = Ws[kk][tx + 16 * j];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc[0][j] = fmaf(a, w[j], acc[0][j]);
-        }
-        __syncthreads();
+        for (int k = 0; k < kPoints; ++k) acc = fmaf(Xs[bb][k], w[(size_t)k * H], acc);
     }
-    // Partial second FC over this CTA's hidden units, reduced over the 16
-    // threads (tx) that share a board.
+    float sum = (col < H) ? w2[col] * act_fn(b1[col] + acc, act) : 0.0f;
 #pragma unroll
-    for (int i = 0; i < 1; ++i) {
-        float sum = 0.0f;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int n = n0 + tx + 16 * j;
-            if (n < H) sum = fmaf(w2[n], act_fn(b1[n] + acc[i][j], act), sum);
-        }
-#pragma unroll
-        for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        const int b = b0 + ty + 16 * i;
-        if (tx == 0 && b < B) part[(size_t)b * gridDim.y + blockIdx.y] = sum;
-    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (n % 32 == 0) red[bb][n / 32] = sum;
+    __syncthreads();
+    const int b = b0 + bb;
+    if (n == 0 && b < B) part[(size_t)b * gridDim.y + blockIdx.y] = red[bb][0] + red[bb][1];
 }
 
 __global__ void value_final_kernel(const float *__restrict__ part, int nparts, int B, float b2,

@@ -126,8 +126,11 @@ struct lg_ctx {
     float *d_parts = nullptr;  // fused-head partial sums, [4][max_batch * 361]
     float *d_fcpart = nullptr; // value-head FC partial sums
     int *d_flags = nullptr;    // per-CTA layer flags of the persistent trunk kernel
-    uint8_t *h_planes = nullptr;
-    float *h_out = nullptr, *h_out2 = nullptr;
+    // pinned staging of the blocking calls, two slots so that chunk k+1 is
+    // packed while chunk k runs: planes, outputs, logits, completion events
+    uint8_t *h_planes = nullptr, *h_planes_b = nullptr;
+    float *h_out = nullptr, *h_out2 = nullptr, *h_out_b = nullptr, *h_out2_b = nullptr;
+    cudaEvent_t host_done[2] = {nullptr, nullptr};
     int planes_c = 0;
     std::mutex mu;
     std::map<std::tuple<int, int, uint32_t, int>, std::pair<cudaGraphExec_t, int>> graphs;
@@ -529,6 +532,10 @@ int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *pr
 
 // Host call: copy planes in, run (through a cached CUDA graph of
 // copy-in + forward + copy-out for this batch size), copy results out.
+// Host call: chunks of up to max_batch positions go through a cached CUDA
+// graph of copy-in + forward + copy-out (one graph per chunk size and
+// staging slot).  Two pinned slots alternate, so the host packs chunk k+1
+// while the GPU runs chunk k; chunk k-2's results are handed back first.
 int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
              float *logits, float *value) {
     Net &n = c->nets[net];
@@ -543,36 +550,69 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
     int rc = check_fault(c);
     if (rc) return rc;
     cudaSetDevice(c->device);
-    size_t per_in = (size_t)n.d.c_in * kPoints;
-    for (int b0 = 0; b0 < B; b0 += c->max_batch) {
-        int nb = std::min(c->max_batch, B - b0);
-        std::memcpy(c->h_planes, planes + (size_t)b0 * per_in, (size_t)nb * per_in);
-        uint32_t tbits;
-        std::memcpy(&tbits, &T, 4);
-        bool want_logits = logits != nullptr && !n.d.value_head;
-        auto key = std::make_tuple(net, nb, n.d.value_head ? 0u : tbits, want_logits ? 1 : 0);
+    const size_t per_in = (size_t)n.d.c_in * kPoints;
+    const bool want_logits = logits != nullptr && !n.d.value_head;
+    uint32_t tbits;
+    std::memcpy(&tbits, &T, 4);
+    uint8_t *hp[2] = {c->h_planes, c->h_planes_b};
+    float *ho[2] = {c->h_out, c->h_out_b}, *hl[2] = {c->h_out2, c->h_out2_b};
+    struct Pending {
+        int b0 = 0, nb = 0;
+        bool live = false;
+    } pend[2];
+    auto finish = [&](int slot) -> int {
+        Pending &q = pend[slot];
+        if (!q.live) return LG_OK;
+        q.live = false;
+        LG_CUDA_TRY(cudaEventSynchronize(c->host_done[slot]));
+        int herr = 0;
+        LG_CUDA_TRY(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (herr) {
+            cudaMemset(c->d_err, 0, sizeof(int));
+            lg_set_error("kernel reported error status %d", herr);
+            return LG_ERR_DEVICE;
+        }
+        if (n.d.value_head) {
+            std::memcpy(value + q.b0, ho[slot], (size_t)q.nb * sizeof(float));
+        } else {
+            std::memcpy(probs + (size_t)q.b0 * kPoints, ho[slot], (size_t)q.nb * kPoints * sizeof(float));
+            if (want_logits)
+                std::memcpy(logits + (size_t)q.b0 * kPoints, hl[slot], (size_t)q.nb * kPoints * sizeof(float));
+        }
+        return LG_OK;
+    };
+    int k = 0;
+    for (int b0 = 0; b0 < B; b0 += c->max_batch, ++k) {
+        const int slot = k & 1;
+        const int nb = std::min(c->max_batch, B - b0);
+        if ((rc = finish(slot))) {
+            finish(slot ^ 1);
+            return rc;
+        }
+        std::memcpy(hp[slot], planes + (size_t)b0 * per_in, (size_t)nb * per_in);
+        auto key = std::make_tuple(net, nb, n.d.value_head ? 0u : tbits, (want_logits ? 1 : 0) + 8 * slot);
         auto it = c->graphs.find(key);
         if (it == c->graphs.end()) {
             cudaGraph_t g;
             LG_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            cudaMemcpyAsync(c->d_planes, c->h_planes, (size_t)nb * per_in, cudaMemcpyHostToDevice,
-                            c->stream);
+            cudaMemcpyAsync(c->d_planes, hp[slot], (size_t)nb * per_in, cudaMemcpyHostToDevice, c->stream);
             int nl = 0;
             rc = forward(c, net, c->d_planes, nb, T, c->d_probs, want_logits ? c->d_logits : nullptr,
                          c->d_value, c->stream, &nl);
             if (n.d.value_head) {
-                cudaMemcpyAsync(c->h_out, c->d_value, (size_t)nb * sizeof(float),
-                                cudaMemcpyDeviceToHost, c->stream);
+                cudaMemcpyAsync(ho[slot], c->d_value, (size_t)nb * sizeof(float), cudaMemcpyDeviceToHost,
+                                c->stream);
             } else {
-                cudaMemcpyAsync(c->h_out, c->d_probs, (size_t)nb * kPoints * sizeof(float),
+                cudaMemcpyAsync(ho[slot], c->d_probs, (size_t)nb * kPoints * sizeof(float),
                                 cudaMemcpyDeviceToHost, c->stream);
                 if (want_logits)
-                    cudaMemcpyAsync(c->h_out2, c->d_logits, (size_t)nb * kPoints * sizeof(float),
+                    cudaMemcpyAsync(hl[slot], c->d_logits, (size_t)nb * kPoints * sizeof(float),
                                     cudaMemcpyDeviceToHost, c->stream);
             }
             cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
             if (rc) {
                 if (ce == cudaSuccess) cudaGraphDestroy(g);
+                finish(slot ^ 1);
                 return rc;
             }
             LG_CUDA_TRY(ce);
@@ -583,25 +623,19 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
             it = c->graphs.emplace(key, std::make_pair(ge, nl)).first;
         }
         LG_CUDA_TRY(cudaGraphLaunch(it->second.first, c->stream));
+        LG_CUDA_TRY(cudaEventRecord(c->host_done[slot], c->stream));
         c->launches += it->second.second;
-        LG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-        int herr = 0;
-        LG_CUDA_TRY(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-        if (herr) {
-            cudaMemset(c->d_err, 0, sizeof(int));
-            lg_set_error("kernel reported error status %d", herr);
-            return LG_ERR_DEVICE;
-        }
-        if (n.d.value_head) {
-            std::memcpy(value + b0, c->h_out, (size_t)nb * sizeof(float));
-        } else {
-            std::memcpy(probs + (size_t)b0 * kPoints, c->h_out, (size_t)nb * kPoints * sizeof(float));
-            if (want_logits)
-                std::memcpy(logits + (size_t)b0 * kPoints, c->h_out2,
-                            (size_t)nb * kPoints * sizeof(float));
-        }
+        pend[slot].b0 = b0;
+        pend[slot].nb = nb;
+        pend[slot].live = true;
     }
-    return LG_OK;
+    // hand back the last two chunks in order
+    const int last = (k - 1) & 1;
+    if ((rc = finish(last ^ 1))) {
+        finish(last);
+        return rc;
+    }
+    return finish(last);
 }
 
 int run_device(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
@@ -826,6 +860,11 @@ extern "C" void lg_destroy(lg_ctx *c) {
     if (c->h_planes) cudaFreeHost(c->h_planes);
     if (c->h_out) cudaFreeHost(c->h_out);
     if (c->h_out2) cudaFreeHost(c->h_out2);
+    if (c->h_planes_b) cudaFreeHost(c->h_planes_b);
+    if (c->h_out_b) cudaFreeHost(c->h_out_b);
+    if (c->h_out2_b) cudaFreeHost(c->h_out2_b);
+    for (int i = 0; i < 2; ++i)
+        if (c->host_done[i]) cudaEventDestroy(c->host_done[i]);
     for (int i = 0; i < 2; ++i) {
         if (c->srv_planes[i]) cudaFreeHost(c->srv_planes[i]);
         if (c->srv_out[i]) cudaFreeHost(c->srv_out[i]);
@@ -918,7 +957,12 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(LG_ERR_CUDA);
     if (cudaMallocHost(&c->h_planes, mb * max_c_in * kPoints) != cudaSuccess ||
         cudaMallocHost(&c->h_out, mb * kPoints * sizeof(float)) != cudaSuccess ||
-        cudaMallocHost(&c->h_out2, mb * kPoints * sizeof(float)) != cudaSuccess) {
+        cudaMallocHost(&c->h_out2, mb * kPoints * sizeof(float)) != cudaSuccess ||
+        cudaMallocHost(&c->h_planes_b, mb * max_c_in * kPoints) != cudaSuccess ||
+        cudaMallocHost(&c->h_out_b, mb * kPoints * sizeof(float)) != cudaSuccess ||
+        cudaMallocHost(&c->h_out2_b, mb * kPoints * sizeof(float)) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->host_done[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->host_done[1], cudaEventDisableTiming) != cudaSuccess) {
         lg_set_error("cudaMallocHost failed");
         return fail(LG_ERR_ALLOC);
     }

@@ -892,16 +892,25 @@ constexpr int kPackMaxC = 64;
 __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__restrict__ planes, int B,
                                                              int C, int halves,
                                                              __nv_bfloat16 *__restrict__ out) {
-    __shared__ uint8_t sp[kPackMaxC * kPoints];
+    __shared__ __align__(16) uint8_t sp[kPackMaxC * kPoints];
     const int b = blockIdx.x;
     if (b >= B) return;
     const uint8_t *src = planes + (size_t)b * C * kPoints;
-    for (int i = threadIdx.x; i < C * kPoints; i += blockDim.x) sp[i] = src[i];
+    const int nbytes = C * kPoints;
+    if (((uintptr_t)src & 3) == 0) {
+        for (int i = threadIdx.x; i < nbytes / 4; i += blockDim.x)
+            reinterpret_cast<uint32_t *>(sp)[i] = reinterpret_cast<const uint32_t *>(src)[i];
+        for (int i = (nbytes / 4) * 4 + threadIdx.x; i < nbytes; i += blockDim.x) sp[i] = src[i];
+    } else {
+        for (int i = threadIdx.x; i < nbytes; i += blockDim.x) sp[i] = src[i];
+    }
     __syncthreads();
     const int groups = halves * 8;
     __nv_bfloat16 *dst = out + (size_t)b * kL5Board * groups * 8;
     const bool aligned = (C % 8) == 0;  // then a group of 8 channels shares one dx
-    for (int i = threadIdx.x; i < kL5Board * groups; i += blockDim.x) {
+    const int per = (kL5Board * groups + gridDim.y - 1) / gridDim.y;
+    const int i0 = blockIdx.y * per, i1 = min(kL5Board * groups, i0 + per);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int r = i / groups, g = i % groups;
         const int y = r / kL5Pitch, x = r % kL5Pitch;
         __align__(16) __nv_bfloat16 v[8];
@@ -932,7 +941,8 @@ __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__re
 
 void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv_bfloat16 *out,
                            cudaStream_t s) {
-    pack_planes_l5_kernel<<<B, 256, 0, s>>>(planes, B, C, halves, out);
+    // four CTAs per board, each writing a quarter of its rows
+    pack_planes_l5_kernel<<<dim3(B, 4), 256, 0, s>>>(planes, B, C, halves, out);
 }
 
 // ------------------------------------------------------------------ launch
