@@ -309,10 +309,10 @@ def run_ours(args, world, rank, local):
     avg3 = ms_dom / max(n_dom, 1) / 1e3
     achieved = flop_launch / avg3 / 1e12 if n_dom else None
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "tc_conv3x3_b256_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get("bytes_per_launch")
+            traffic = json.load(f).get("tc_trunk_kernel" if ntr else "tc_convT_kernel<2,0,0>")
     line = {
         "metric": METRIC, "value": value, "unit": "positions/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
