@@ -12,8 +12,12 @@ symmetries = 8192 distinct inputs.  Weights: He-normal, zero biases, seeds 1
 
 Reported (one JSON line on rank 0):
   value       positions/s with inputs resident in HBM (lg_*_device)
-  e2e         positions/s through the host C ABI (lg_policy / lg_value with
-              host buffers; host->device and device->host copies timed)
+  e2e         positions/s through the host C ABI from boards
+              (lg_policy_boards / lg_value_boards: 362 bytes a position in,
+              input planes gathered on the GPU, results out; the copies and
+              the gather timed) -- the counterpart of get_scored_moves /
+              get_value, whose gather runs on the host.  e2e_planes: the same
+              through lg_policy / lg_value with host-gathered planes.
   roofline    the dominant kernel (tensor-core 3x3 conv), CUDA-event timed
               inside the timed region, against the measured BF16 peak
   cpu_baseline  the reference algorithm (im2col + OpenBLAS sgemm, one
@@ -59,6 +63,16 @@ def load_positions():
     P = np.concatenate([pp[..., lg.ROTATE[s]] for s in range(8)])
     V = np.concatenate([pv[..., lg.ROTATE[s]] for s in range(8)])
     return np.ascontiguousarray(P), np.ascontiguousarray(V)
+
+
+def load_boards():
+    """The 1024 fixture boards under the 8 symmetries, in the order of
+    load_positions(): squares [8192][361] int8 and to_move [8192] int8."""
+    d = np.load(os.path.join(ROOT, "tests", "golden", "positions_s0.npz"))
+    import leela_gb300 as lg
+    sq = np.concatenate([d["squares"][:, lg.ROTATE[s]] for s in range(8)])
+    tm = np.tile(d["meta"][:, 0].astype(np.int8), 8)
+    return np.ascontiguousarray(sq, dtype=np.int8), tm
 
 
 def make_weights():
@@ -273,25 +287,42 @@ def run_ours(args, world, rank, local):
             print(json.dumps({"profile_run": True, "value": value}), flush=True)
         return
 
-    # ---------------- e2e: host buffers through lg_policy / lg_value
+    # ---------------- e2e: host boards through lg_policy_boards / lg_value_boards
+    squares, to_move = load_boards()
+    ctx.policy_boards(squares[:BATCH], to_move[:BATCH])
+    ctx.value_boards(squares[:BATCH], to_move[:BATCH])
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        probs = ctx.policy_boards(squares, to_move)
+        vals = ctx.value_boards(squares, to_move)
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": world * POSITIONS * e2e_steps / t_e2e, "unit": "positions/s",
+           "h2d_bytes_per_step": int(2 * (squares.nbytes + to_move.nbytes)),
+           "d2h_bytes_per_step": int(probs.nbytes + vals.nbytes),
+           "call": "lg_policy_boards + lg_value_boards (gather on the GPU)"}
+    # the same with planes gathered on the host (lg_policy / lg_value)
     host_p = np.ascontiguousarray(planes_p)
     host_v = np.ascontiguousarray(planes_v)
     ctx.policy(host_p[:BATCH])
     ctx.value(host_v[:BATCH])
-    e2e_steps = max(1, min(args.steps, 5))
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         probs = ctx.policy(host_p)
         vals = ctx.value(host_v)
-    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
-    e2e = {"value": world * POSITIONS * e2e_steps / t_e2e, "unit": "positions/s",
-           "h2d_bytes_per_step": int(host_p.nbytes + host_v.nbytes),
-           "d2h_bytes_per_step": int(probs.nbytes + vals.nbytes)}
+    t_e2p = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_planes = {"value": world * POSITIONS * e2e_steps / t_e2p, "unit": "positions/s",
+                  "h2d_bytes_per_step": int(host_p.nbytes + host_v.nbytes),
+                  "d2h_bytes_per_step": int(probs.nbytes + vals.nbytes),
+                  "call": "lg_policy + lg_value (planes gathered on the host)"}
 
     extras = {}
     if rank == 0:
         extras = secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp)
+        extras["e2e_planes"] = e2e_planes
+        extras["gather"] = gather_throughput(lg, squares, to_move, dev, sp)
 
     if rank != 0:
         ctx.close()
@@ -511,6 +542,40 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
     out["serving_config3"] = serving_config3(lg, wp, wv, planes_p, planes_v, dev.index)
     out["distill_config4"] = distill_config4(wp, wv, planes_p, planes_v, dev.index)
     return out
+
+
+def gather_throughput(lg, squares, to_move, dev, sp, reps=20):
+    """lg_gather_device alone: 8192 boards -> 24 policy planes and 24 value
+    planes, boards resident in HBM.  Algorithmic bytes per board and set:
+    362 in + 24 * 361 out."""
+    import torch
+    B = squares.shape[0]
+    d_sq = torch.from_numpy(squares).to(dev)
+    d_tm = torch.from_numpy(to_move).to(dev)
+    out_p = torch.empty((B, 24, 361), dtype=torch.uint8, device=dev)
+    out_v = torch.empty((B, 24, 361), dtype=torch.uint8, device=dev)
+
+    def run():
+        lg.gather_device(d_sq.data_ptr(), d_tm.data_ptr(), B, 0, 24, out_p.data_ptr(), sp)
+        lg.gather_device(d_sq.data_ptr(), d_tm.data_ptr(), B, 1, 24, out_v.data_ptr(), sp)
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    per_launch = B * (362 + 24 * 361)
+    _, hbm, _ = read_peaks()
+    gbs = 2 * per_launch / (ms / 1e3) / 1e9
+    return {"boards_per_s_both_sets": B / (ms / 1e3), "us_per_launch": ms * 1e3 / 2,
+            "boards_per_launch": B, "algorithmic_bytes_per_launch": per_launch,
+            "achieved_gbs": gbs, "hbm_peak_gbs": hbm, "frac_of_hbm": gbs / hbm if hbm else None}
 
 
 def distill_config4(wp, wv, planes_p, planes_v, device):

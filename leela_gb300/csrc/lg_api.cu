@@ -122,6 +122,7 @@ struct lg_ctx {
     int *d_err = nullptr;
     // shared
     uint8_t *d_planes = nullptr;
+    int8_t *d_boards = nullptr;  // board-input calls: squares [B][361], then to_move [B]
     float *d_logits = nullptr, *d_probs = nullptr, *d_value = nullptr;
     float *d_parts = nullptr;  // fused-head partial sums, [4][max_batch * 361]
     float *d_fcpart = nullptr; // value-head FC partial sums
@@ -530,21 +531,29 @@ int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *pr
     return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof);
 }
 
-// Host call: copy planes in, run (through a cached CUDA graph of
-// copy-in + forward + copy-out for this batch size), copy results out.
 // Host call: chunks of up to max_batch positions go through a cached CUDA
 // graph of copy-in + forward + copy-out (one graph per chunk size and
 // staging slot).  Two pinned slots alternate, so the host packs chunk k+1
 // while the GPU runs chunk k; chunk k-2's results are handed back first.
+// With `squares` / `to_move` instead of planes, each chunk copies in the
+// boards (362 bytes a position) and the graph gathers the input planes on
+// the GPU before the forward.
 int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
-             float *logits, float *value) {
+             float *logits, float *value, const int8_t *squares = nullptr,
+             const int8_t *to_move = nullptr) {
     Net &n = c->nets[net];
     if (!n.present) {
         lg_set_error("net %d was not created", net);
         return LG_ERR_ARG;
     }
-    if (B < 0 || (B > 0 && !planes)) {
+    const bool boards = squares != nullptr;
+    if (B < 0 || (B > 0 && !planes && !(squares && to_move))) {
         lg_set_error("bad batch");
+        return LG_ERR_ARG;
+    }
+    if (boards && (n.d.c_in > kGatherPlanes || c->planes_c < 2)) {
+        lg_set_error("board input gathers planes 0..%d; the net reads %d planes", kGatherPlanes - 1,
+                     n.d.c_in);
         return LG_ERR_ARG;
     }
     int rc = check_fault(c);
@@ -589,16 +598,33 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
             finish(slot ^ 1);
             return rc;
         }
-        std::memcpy(hp[slot], planes + (size_t)b0 * per_in, (size_t)nb * per_in);
-        auto key = std::make_tuple(net, nb, n.d.value_head ? 0u : tbits, (want_logits ? 1 : 0) + 8 * slot);
+        const size_t in_bytes = boards ? (size_t)nb * (kPoints + 1) : (size_t)nb * per_in;
+        if (boards) {
+            std::memcpy(hp[slot], squares + (size_t)b0 * kPoints, (size_t)nb * kPoints);
+            std::memcpy(hp[slot] + (size_t)nb * kPoints, to_move + b0, (size_t)nb);
+        } else {
+            std::memcpy(hp[slot], planes + (size_t)b0 * per_in, in_bytes);
+        }
+        auto key = std::make_tuple(net, nb, n.d.value_head ? 0u : tbits,
+                                   (want_logits ? 1 : 0) + 8 * slot + (boards ? 16 : 0));
         auto it = c->graphs.find(key);
         if (it == c->graphs.end()) {
             cudaGraph_t g;
             LG_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            cudaMemcpyAsync(c->d_planes, hp[slot], (size_t)nb * per_in, cudaMemcpyHostToDevice, c->stream);
             int nl = 0;
-            rc = forward(c, net, c->d_planes, nb, T, c->d_probs, want_logits ? c->d_logits : nullptr,
-                         c->d_value, c->stream, &nl);
+            if (boards) {
+                cudaMemcpyAsync(c->d_boards, hp[slot], in_bytes, cudaMemcpyHostToDevice, c->stream);
+                rc = launch_gather(c->d_boards, c->d_boards + (size_t)nb * kPoints, nb,
+                                   net == LG_NET_POLICY ? 0 : 1, n.d.c_in, c->d_planes, c->stream);
+                nl = 1;
+            } else {
+                cudaMemcpyAsync(c->d_planes, hp[slot], in_bytes, cudaMemcpyHostToDevice, c->stream);
+            }
+            int nf = 0;
+            if (!rc)
+                rc = forward(c, net, c->d_planes, nb, T, c->d_probs, want_logits ? c->d_logits : nullptr,
+                             c->d_value, c->stream, &nf);
+            nl += nf;
             if (n.d.value_head) {
                 cudaMemcpyAsync(ho[slot], c->d_value, (size_t)nb * sizeof(float), cudaMemcpyDeviceToHost,
                                 c->stream);
@@ -947,6 +973,7 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
     }
     c->planes_c = max_c_in;
     if ((rc = dev_alloc(c, &c->d_planes, mb * max_c_in * kPoints)) ||
+        (rc = dev_alloc(c, &c->d_boards, mb * (kPoints + 1))) ||
         (rc = dev_alloc(c, &c->d_logits, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_probs, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)) ||
@@ -999,6 +1026,26 @@ extern "C" int lg_value(lg_ctx *c, const uint8_t *planes, int B, float *value) {
     }
     std::lock_guard<std::mutex> g(c->mu);
     return run_host(c, LG_NET_VALUE, planes, B, 1.0f, nullptr, nullptr, value);
+}
+
+extern "C" int lg_policy_boards(lg_ctx *c, const int8_t *squares, const int8_t *to_move, int B,
+                                float temperature, float *probs, float *logits) {
+    if (!c || !probs || !(temperature > 0.0f) || (B > 0 && (!squares || !to_move))) {
+        lg_set_error("lg_policy_boards: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    return run_host(c, LG_NET_POLICY, nullptr, B, temperature, probs, logits, nullptr, squares, to_move);
+}
+
+extern "C" int lg_value_boards(lg_ctx *c, const int8_t *squares, const int8_t *to_move, int B,
+                               float *value) {
+    if (!c || !value || (B > 0 && (!squares || !to_move))) {
+        lg_set_error("lg_value_boards: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    return run_host(c, LG_NET_VALUE, nullptr, B, 1.0f, nullptr, nullptr, value, squares, to_move);
 }
 
 extern "C" int lg_policy_device(lg_ctx *c, const uint8_t *planes, int B, float temperature,

@@ -53,6 +53,13 @@ struct TcLayer {
     int variant;          // for n == 128: 0 = 256-row transposed kernel, 1 = 128-row kernel
 };
 
+// Input planes 0..nplanes-1 (nplanes <= kGatherPlanes) of the policy
+// (which = 0) or value (which = 1) set from boards: squares [B][361]
+// (0 black, 1 white, 2 empty), to_move [B]; planes [B][nplanes][361].
+constexpr int kGatherPlanes = 24;
+int launch_gather(const int8_t *squares, const int8_t *to_move, int B, int which, int nplanes,
+                  uint8_t *planes, cudaStream_t s);
+
 // Expanded 5x5 input: planes [B][C][361] bytes -> L5 BF16 rows with
 // halves*64 channels: channel dx*C + c = plane c at (y, x + dx - 2).
 void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv_bfloat16 *out,

@@ -530,3 +530,146 @@ double or_time_pair_f32(const or_net *pol, const float *wp, const or_net *val, c
     clock_gettime(CLOCK_MONOTONIC, &t1);
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }
+
+/* ------------------------------------------------------- input planes */
+
+#define GB_EMPTY 2
+
+static int gb_nbrs(int p, int *out) {
+    int x = p % 19, y = p / 19, n = 0;
+    if (x > 0) out[n++] = p - 1;
+    if (x < 18) out[n++] = p + 1;
+    if (y > 0) out[n++] = p - 19;
+    if (y < 18) out[n++] = p + 19;
+    return n;
+}
+
+/* Flood-fills the string through p; marks its stones in `in` (1) and
+ * returns its liberty count.  Stones go to list[] when it is given. */
+static int gb_string(const int8_t *sq, int p, uint8_t *in, int *list, int *nlist) {
+    int stack[OR_POINTS], sp = 0, n = 0, libs = 0;
+    uint8_t seen_lib[OR_POINTS];
+    memset(seen_lib, 0, sizeof seen_lib);
+    int8_t c = sq[p];
+    in[p] = 1;
+    stack[sp++] = p;
+    while (sp) {
+        int q = stack[--sp], nb[4];
+        if (list) list[n++] = q;
+        int m = gb_nbrs(q, nb);
+        for (int k = 0; k < m; ++k) {
+            int r = nb[k];
+            if (sq[r] == GB_EMPTY) {
+                if (!seen_lib[r]) { seen_lib[r] = 1; ++libs; }
+            } else if (sq[r] == c && !in[r]) {
+                in[r] = 1;
+                stack[sp++] = r;
+            }
+        }
+    }
+    if (nlist) *nlist = n;
+    return libs;
+}
+
+static int gb_libs(const int8_t *sq, int p) {
+    uint8_t in[OR_POINTS];
+    memset(in, 0, sizeof in);
+    return gb_string(sq, p, in, NULL, NULL);
+}
+
+/* Plays `color` at the empty point p on a copy of the board: removes the
+ * opponent strings left without liberties, then returns the liberties of
+ * the string through p, or 0 when that string has none (a suicide). */
+static int gb_after(const int8_t *sq, int color, int p) {
+    int8_t b[OR_POINTS];
+    memcpy(b, sq, sizeof b);
+    b[p] = (int8_t)color;
+    int nb[4], m = gb_nbrs(p, nb);
+    for (int k = 0; k < m; ++k) {
+        int r = nb[k];
+        if (b[r] == 1 - color && gb_libs(b, r) == 0) {
+            uint8_t in[OR_POINTS];
+            int list[OR_POINTS], n;
+            memset(in, 0, sizeof in);
+            gb_string(b, r, in, list, &n);
+            for (int i = 0; i < n; ++i) b[list[i]] = GB_EMPTY;
+        }
+    }
+    return gb_libs(b, p);
+}
+
+void or_gather_planes(const int8_t *squares, int to_move, int which, uint8_t *planes) {
+    memset(planes, 0, 24 * OR_POINTS);
+    int libs_of[OR_POINTS];
+    uint8_t done[OR_POINTS];
+    memset(done, 0, sizeof done);
+    for (int p = 0; p < OR_POINTS; ++p) {
+        if (squares[p] == GB_EMPTY || done[p]) continue;
+        int list[OR_POINTS], n;
+        uint8_t in[OR_POINTS];
+        memset(in, 0, sizeof in);
+        int l = gb_string(squares, p, in, list, &n);
+        for (int i = 0; i < n; ++i) { libs_of[list[i]] = l; done[list[i]] = 1; }
+    }
+    /* policy: own libs 1,2,3,4,5+ at 3..7, opponent's at 8..12, after-move
+     * 1..5,6+ at 13..18, opponent's after-move 1..5 at 19..23 (6+ is plane
+     * 24).  value: libs 1..5,6+ at 3..8 / 9..14, after-move 1..5,6+ at
+     * 15..20, opponent's 1..3 at 21..23 (4.. are planes 24..26). */
+    const int lib_cap = which == 0 ? 5 : 6;
+    const int opp_lib0 = which == 0 ? 8 : 9;
+    const int after0 = which == 0 ? 13 : 15;
+    const int oafter0 = which == 0 ? 19 : 21;
+    const int oafter_max = which == 0 ? 5 : 3;
+    for (int p = 0; p < OR_POINTS; ++p) {
+        int c = squares[p];
+        if (c != GB_EMPTY) {
+            int mine = c == to_move;
+            planes[(mine ? 1 : 2) * OR_POINTS + p] = 1;
+            int l = libs_of[p];
+            if (l >= 1) {
+                int idx = (l >= lib_cap ? lib_cap : l) - 1;
+                planes[((mine ? 3 : opp_lib0) + idx) * OR_POINTS + p] = 1;
+            }
+        } else {
+            planes[p] = 1;
+            int al = gb_after(squares, to_move, p);
+            int at = gb_after(squares, 1 - to_move, p);
+            if (al >= 1) planes[(after0 + (al >= 6 ? 5 : al - 1)) * OR_POINTS + p] = 1;
+            if (at >= 1 && at <= oafter_max) planes[(oafter0 + at - 1) * OR_POINTS + p] = 1;
+        }
+    }
+}
+
+int or_random_board(uint64_t seed, int k, int8_t *squares) {
+    uint64_t s = seed * 0x9E3779B97F4A7C15ull + 0x5851F42D4C957F2Dull;
+    memset(squares, GB_EMPTY, OR_POINTS);
+    int color = 0;
+    for (int mv = 0; mv < k; ++mv) {
+        /* uniform over the legal points: draw empty points without
+         * replacement until one is not a suicide */
+        int cand[OR_POINTS], nc = 0, p = -1;
+        for (int q = 0; q < OR_POINTS; ++q)
+            if (squares[q] == GB_EMPTY) cand[nc++] = q;
+        while (nc > 0) {
+            int j = (int)(splitmix64(&s) % (uint64_t)nc);
+            int q = cand[j];
+            if (gb_after(squares, color, q) > 0) { p = q; break; }
+            cand[j] = cand[--nc];
+        }
+        if (p < 0) break;
+        int nb[4], m = gb_nbrs(p, nb);
+        squares[p] = (int8_t)color;
+        for (int j = 0; j < m; ++j) {
+            int r = nb[j];
+            if (squares[r] == 1 - color && gb_libs(squares, r) == 0) {
+                uint8_t in[OR_POINTS];
+                int list[OR_POINTS], n;
+                memset(in, 0, sizeof in);
+                gb_string(squares, r, in, list, &n);
+                for (int i = 0; i < n; ++i) squares[list[i]] = GB_EMPTY;
+            }
+        }
+        color = 1 - color;
+    }
+    return color;
+}

@@ -125,6 +125,21 @@ double or_time_pair_f32(const or_net *pol, const float *wp, const or_net *val, c
                         const uint8_t *planes_p, const uint8_t *planes_v, int npos, int iters,
                         int nthreads);
 
+/* Input planes 0..23 of the policy (which = 0) or value (which = 1) set,
+ * restating Network::gather_features_policy / gather_features_value
+ * (Network.cpp:883-1046, 1048-1201) for the planes that need no ladder
+ * reader: colours, string liberties (FastBoard::count_rliberties,
+ * FastBoard.cpp:2482-2508) and after-move liberties of both colours
+ * (FastBoard::after_liberties, FastBoard.cpp:2511-2528; 0 for a suicide).
+ * squares[361]: 0 black, 1 white, 2 empty, point y*19+x; planes[24][361]. */
+void or_gather_planes(const int8_t *squares, int to_move, int which, uint8_t *planes);
+
+/* A board reached by k uniformly random legal moves from the empty board
+ * (captures applied, suicide excluded, simple ko ignored), for parity cases
+ * beyond the fixture positions.  Writes squares[361]; returns the side to
+ * move (0 black, 1 white). */
+int or_random_board(uint64_t seed, int k, int8_t *squares);
+
 #ifdef __cplusplus
 }
 #endif

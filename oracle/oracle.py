@@ -114,6 +114,9 @@ def lib():
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int]
             L.or_time_pair_f32.restype = ctypes.c_double
+            L.or_gather_planes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_void_p]
+            L.or_random_board.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]
             _lib = L
     return _lib
 
@@ -225,6 +228,33 @@ def rotate_planes(planes: np.ndarray, sym: int) -> np.ndarray:
     out = np.empty_like(planes)
     lib().or_rotate_planes(_ptr(planes), c, sym, _ptr(out))
     return out
+
+
+def gather_planes(squares: np.ndarray, to_move, which: int) -> np.ndarray:
+    """Planes 0..23 of the policy (which=0) or value (which=1) input set for
+    boards squares [B][361] (0 black, 1 white, 2 empty) -> [B][24][361] u8.
+    Restates Network::gather_features_policy / gather_features_value
+    (Network.cpp:883-1201) for the planes without ladders."""
+    sq = np.ascontiguousarray(squares, dtype=np.int8).reshape(-1, POINTS)
+    tm = np.broadcast_to(np.asarray(to_move, dtype=np.int64), (sq.shape[0],))
+    out = np.empty((sq.shape[0], 24, POINTS), dtype=np.uint8)
+    L = lib()
+    for b in range(sq.shape[0]):
+        L.or_gather_planes(_ptr(sq[b]), int(tm[b]), which, _ptr(out[b]))
+    return out
+
+
+def random_boards(n: int, seed: int, kmax: int = 300):
+    """n boards after k ~ U[0, kmax] random legal moves (captures applied):
+    (squares [n][361] int8, to_move [n] int8)."""
+    rng = np.random.default_rng(seed)
+    ks = rng.integers(0, kmax + 1, size=n)
+    sq = np.empty((n, POINTS), dtype=np.int8)
+    tm = np.empty(n, dtype=np.int8)
+    L = lib()
+    for i in range(n):
+        tm[i] = L.or_random_board(seed * 1000003 + i, int(ks[i]), _ptr(sq[i]))
+    return sq, tm
 
 
 def e4m3_round(x: float) -> float:

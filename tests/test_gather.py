@@ -1,0 +1,113 @@
+"""GPU input-plane gather (lg_gather_device) and the board-input evaluation
+calls (lg_policy_boards / lg_value_boards).
+
+Bit-exact: the gathered planes equal the reference gather's planes 0..23 on
+the 1024 fixture positions, and the oracle's on random boards (dense ones,
+with captures) and hand-built edge cases.  The board-input calls return
+exactly what the plane-input calls return on the gathered planes."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+POINTS = 361
+
+
+def _gather(lg, squares, to_move, which, nplanes=24):
+    import torch
+    sq = torch.from_numpy(np.ascontiguousarray(squares, dtype=np.int8).reshape(-1, POINTS)).cuda()
+    B = sq.shape[0]
+    tm = torch.from_numpy(np.ascontiguousarray(
+        np.broadcast_to(np.asarray(to_move, dtype=np.int8), (B,)))).cuda()
+    out = torch.full((max(B, 1), nplanes, POINTS), 7, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    lg.gather_device(sq.data_ptr(), tm.data_ptr(), B, which, nplanes, out.data_ptr(), s)
+    torch.cuda.synchronize()
+    return out[:B].cpu().numpy()
+
+
+@pytest.mark.parametrize("which,key", [(0, "planes_p"), (1, "planes_v")])
+def test_gather_matches_reference_planes(gpu_lib, positions, which, key):
+    got = _gather(gpu_lib, positions["squares"], positions["meta"][:, 0], which)
+    ref = positions[key][:, :24]
+    bad = np.argwhere(got != ref)
+    assert bad.size == 0, bad[:5]
+
+
+@pytest.mark.parametrize("seed,kmax", [(1, 250), (2, 400), (3, 600)])
+def test_gather_matches_oracle_on_random_boards(gpu_lib, oracle_mod, seed, kmax):
+    sq, tm = oracle_mod.random_boards(256, seed, kmax=kmax)
+    for which in (0, 1):
+        got = _gather(gpu_lib, sq, tm, which)
+        ref = oracle_mod.gather_planes(sq, tm, which)
+        assert (got == ref).all(), np.argwhere(got != ref)[:5]
+
+
+def _edge_boards():
+    boards = []
+    boards.append(np.full(POINTS, 2, np.int8))                      # empty board
+    b = np.full(POINTS, 2, np.int8); b[0] = 0; boards.append(b)     # one corner stone
+    b = np.full(POINTS, 0, np.int8); b[[0, 200]] = 2; boards.append(b)  # one string, 2 liberties
+    b = np.full(POINTS, 0, np.int8); b[180] = 2; boards.append(b)   # one string, 1 liberty
+    # a white stone in atari inside black: capture and after-move planes
+    b = np.full(POINTS, 2, np.int8)
+    b[[20 - 1, 20 + 1, 20 - 19]] = 0; b[20] = 1; boards.append(b)
+    # a large white string with 1 liberty next to a black eye
+    b = np.full(POINTS, 1, np.int8); b[0:19] = 0; b[19:38] = 1; b[5] = 2; b[360] = 2
+    boards.append(b)
+    # alternate rows of black and white with one gap each (long strings)
+    b = np.empty(POINTS, np.int8)
+    for y in range(19):
+        b[y * 19:(y + 1) * 19] = y % 2
+        b[y * 19 + (y * 7) % 19] = 2
+    boards.append(b)
+    return np.stack(boards)
+
+
+def test_gather_edge_cases(gpu_lib, oracle_mod):
+    sq = _edge_boards()
+    for tm in (0, 1):
+        for which in (0, 1):
+            got = _gather(gpu_lib, sq, tm, which)
+            ref = oracle_mod.gather_planes(sq, np.full(len(sq), tm), which)
+            assert (got == ref).all(), (tm, which, np.argwhere(got != ref)[:5])
+
+
+def test_gather_prefix_and_arguments(gpu_lib, positions):
+    lg = gpu_lib
+    sq, tm = positions["squares"][:8], positions["meta"][:8, 0]
+    got = _gather(lg, sq, tm, 0, nplanes=18)
+    assert (got == positions["planes_p"][:8, :18]).all()
+    _gather(lg, sq[:0], tm[:0], 0)   # B = 0 is a no-op
+    import torch
+    dsq = torch.from_numpy(np.ascontiguousarray(sq)).cuda()
+    dtm = torch.from_numpy(np.ascontiguousarray(tm.astype(np.int8))).cuda()
+    out = torch.zeros((8, 32, POINTS), dtype=torch.uint8, device="cuda")
+    for which, nplanes in ((0, 25), (0, 0), (2, 24)):
+        with pytest.raises(lg.LeelaGPUError):
+            lg.gather_device(dsq.data_ptr(), dtm.data_ptr(), 8, which, nplanes, out.data_ptr(), None)
+    with pytest.raises(lg.LeelaGPUError):
+        lg.gather_device(0, 0, 4, 0, 24, 0, None)
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_board_calls_equal_plane_calls(gpu_lib, positions, weights, prec):
+    lg = gpu_lib
+    n = 160  # more than max_batch: two chunks plus a ragged one
+    sq, tm = positions["squares"][:n], positions["meta"][:n, 0]
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], prec),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], prec), max_batch=64) as c:
+        pb, lb = c.policy_boards(sq, tm, 1.0, return_logits=True)
+        vb = c.value_boards(sq, tm)
+        pp, lp = c.policy(positions["planes_p"][:n, :24], 1.0, return_logits=True)
+        vp = c.value(positions["planes_v"][:n, :24])
+    assert np.array_equal(pb, pp) and np.array_equal(lb, lp) and np.array_equal(vb, vp)
+
+
+def test_board_calls_reject_wide_inputs(gpu_lib, weights, positions):
+    """A net reading more than 24 planes cannot take board input."""
+    lg = gpu_lib
+    with lg.Context(policy=lg.NetDesc.reference_policy(weights["ref_p"][1]), max_batch=8) as c:
+        with pytest.raises(lg.LeelaGPUError):
+            c.policy_boards(positions["squares"][:2], positions["meta"][:2, 0])
