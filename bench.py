@@ -277,6 +277,8 @@ def run_ours(args, world, rank, local):
     nf, msf = ctx.profile_read(lg.PROF_TC_FIRST)
     no, mso = ctx.profile_read(lg.PROF_OTHER)
     ntr, mstr = ctx.profile_read(lg.PROF_TC_TRUNK)
+    npk, mspk = ctx.profile_read(lg.PROF_PACK)
+    ntl, mstl = ctx.profile_read(lg.PROF_TAIL)
     tuning = ctx.tuning(BATCH)
     ctx.profile(False)
     ms_max = max_over_ranks(ms, world)
@@ -364,8 +366,9 @@ def run_ours(args, world, rank, local):
                      "flop_per_launch": flop_launch},
         "kernel_time_share": {
             "tc_3x3": ms3, "tc_3x3_fused_head": msh, "tc_trunk": mstr, "tc_5x5_first": msf,
-            "other": mso,
-            "launches": {"tc_3x3": n3, "tc_head": nh, "tc_trunk": ntr, "tc_first": nf, "other": no}},
+            "pack_planes": mspk, "softmax_value_fc": mstl, "other": mso,
+            "launches": {"tc_3x3": n3, "tc_head": nh, "tc_trunk": ntr, "tc_first": nf,
+                         "pack_planes": npk, "softmax_value_fc": ntl, "other": no}},
         "kernel_choice_batch256": tuning,
         "clocks": clk,
         "gpu_launches": gpu_launches,

@@ -277,9 +277,11 @@ LG_API int lg_student_forward(lg_student *st, const uint8_t *planes, int B, floa
 #define LG_PROF_TC_HEAD 1  /* tensor-core 3x3 conv with the fused 1x1 head */
 #define LG_PROF_TC_FIRST 2 /* tensor-core 5x5 first layer */
 #define LG_PROF_FP32_CONV 3 /* FP32 conv (+ split-K reduction) */
-#define LG_PROF_OTHER 4    /* plane packing, head conv, softmax, value FC */
+#define LG_PROF_OTHER 4    /* FP32 plane packing and head conv */
 #define LG_PROF_TC_TRUNK 5 /* persistent kernel running all 3x3 layers (incl. the fused head) */
-#define LG_PROF_KINDS 6
+#define LG_PROF_PACK 6     /* tensor-core plane packing (planes -> expanded BF16 rows) */
+#define LG_PROF_TAIL 7     /* softmax, value FC1 + final */
+#define LG_PROF_KINDS 8
 LG_API int lg_profile(lg_ctx *ctx, int enable);
 LG_API int lg_profile_read(lg_ctx *ctx, int kind, long long *launches, double *total_ms);
 

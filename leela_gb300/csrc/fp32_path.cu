@@ -253,62 +253,105 @@ __global__ void __launch_bounds__(384) softmax_kernel(const HeadIn h, int B, flo
 }
 
 // innerproduct<361,H> (+act) then innerproduct<H,1>, then tanh or (1+tanh)/2
-// (Network.cpp:395-423, 733-737), as a small tiled GEMM over boards:
-// value_fc1_kernel computes hidden = act(b1 + x361 . W1^T) for a tile of 32
-// boards x 64 hidden units (K = 361 staged through shared memory, the 361
-// head outputs formed on the fly from the head partial sums) and writes each
-// board's partial w2 . hidden over its 64 units; value_final_kernel adds the
-// partials in a fixed order, b2, and applies the value map.  w1t is W1
-// transposed to [361][H].
-constexpr int kFcBM = 4, kFcBN = 64;
+// (Network.cpp:395-423, 733-737), as a tiled GEMM over boards.
+// value_fc1_kernel: one CTA = 32 boards x 64 hidden units x one of
+// kFcSplit fixed K ranges of the 361 inputs.  The 32 boards' head outputs
+// for the range are formed in shared memory from the head partial sums, the
+// W1 slice for the range is one contiguous block (W1 is stored sliced,
+// w1s[H/64][361][64], zero-padded past H), and each thread accumulates a
+// 4-board x 2-unit register tile.  It writes pre-activation partial sums
+// pre[split][b][unit].  value_final_kernel adds the kFcSplit partials in a
+// fixed order plus b1, applies the activation, reduces w2 . hidden over the
+// block in a fixed order, adds b2 and applies the value map.  The split does
+// not depend on B, so a board's value does not depend on its batch.
+constexpr int kFcBoards = 32, kFcUnits = 64, kFcSplit = 4;
+constexpr int kFcK = (kPoints + kFcSplit - 1) / kFcSplit;  // 91
+constexpr int kFcXPitch = 36;  // floats; rows 16-byte aligned, 4-way store conflicts at most
 
-// One CTA = 4 boards x 64 hidden units (thread = one board's hidden unit):
-// the 4 boards' 361 head outputs are formed once in shared memory, then each
-// thread runs the K = 361 dot product with W1t read coalesced across threads.
 __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
-                                                        const float *__restrict__ w1t,
-                                                        const float *__restrict__ b1,
-                                                        const float *__restrict__ w2, int H,
-                                                        int act, float *__restrict__ part) {
-    __shared__ float Xs[kFcBM][kPoints];
-    __shared__ float red[kFcBM][2];
+                                                        const float *__restrict__ w1s, int Hp,
+                                                        float *__restrict__ pre) {
+    __shared__ __align__(16) float Xs[kFcK][kFcXPitch];
+    __shared__ __align__(16) float Ws[kFcK][kFcUnits];
     const int tid = threadIdx.x;
-    const int n = tid % kFcBN, bb = tid / kFcBN;
-    const int b0 = blockIdx.x * kFcBM, n0 = blockIdx.y * kFcBN;
-    for (int i = tid; i < kFcBM * kPoints; i += 256) {
-        const int bi = i / kPoints, k = i % kPoints;
-        float x = 0.0f;
-        if (b0 + bi < B) {
-            x = head_value(h, b0 + bi, k);
-            if (h.logits_out && blockIdx.y == 0) h.logits_out[(size_t)(b0 + bi) * kPoints + k] = x;
-        }
-        Xs[bi][k] = x;
-    }
-    __syncthreads();
-    const int col = n0 + n;
-    float acc = 0.0f;
-    if (col < H) {
-        const float *w = w1t + col;
-#pragma unroll 8
-        for (int k = 0; k < kPoints; ++k) acc = fmaf(Xs[bb][k], w[(size_t)k * H], acc);
-    }
-    float sum = (col < H) ? w2[col] * act_fn(b1[col] + acc, act) : 0.0f;
+    const int b0 = blockIdx.x * kFcBoards, slice = blockIdx.y, ks = blockIdx.z;
+    const int k0 = ks * kFcK, nk = min(kPoints, k0 + kFcK) - k0;
+    // W1 slice rows k0 .. k0+nk-1: contiguous, float4 loads
+    const float4 *wsrc = reinterpret_cast<const float4 *>(w1s + ((size_t)slice * kPoints + k0) * kFcUnits);
+    constexpr int kWPer = (kFcK * kFcUnits / 4 + 255) / 256;  // 6
+    float4 wv[kWPer];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if (n % 32 == 0) red[bb][n / 32] = sum;
+    for (int j = 0; j < kWPer; ++j) {
+        const int i = tid + 256 * j;
+        if (i < nk * (kFcUnits / 4)) wv[j] = wsrc[i];
+    }
+#pragma unroll
+    for (int j = 0; j < kWPer; ++j) {
+        const int i = tid + 256 * j;
+        if (i < nk * (kFcUnits / 4)) reinterpret_cast<float4 *>(&Ws[0][0])[i] = wv[j];
+    }
+    // head outputs, read along k for each board: every load of the thread is
+    // issued before the first store, so the loop waits out one round trip
+    constexpr int kPer = (kFcBoards * kFcK + 255) / 256;  // 12
+    float xv[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        const int i = tid + 256 * j;
+        const int bi = i / nk, kk = i - bi * nk, b = b0 + bi;
+        xv[j] = (i < kFcBoards * nk && b < B) ? head_value(h, b, k0 + kk) : 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        const int i = tid + 256 * j;
+        if (i < kFcBoards * nk) {
+            const int bi = i / nk, kk = i - bi * nk, b = b0 + bi;
+            Xs[kk][bi] = xv[j];
+            if (h.logits_out && slice == 0 && b < B) h.logits_out[(size_t)b * kPoints + k0 + kk] = xv[j];
+        }
+    }
     __syncthreads();
-    const int b = b0 + bb;
-    if (n == 0 && b < B) part[(size_t)b * gridDim.y + blockIdx.y] = red[bb][0] + red[bb][1];
+    const int up = tid % 32, bq = tid / 32;  // units 2up, 2up+1; boards 4bq .. 4bq+3
+    float acc[4][2] = {};
+    for (int kk = 0; kk < nk; ++kk) {
+        const float4 x = *reinterpret_cast<const float4 *>(&Xs[kk][4 * bq]);
+        const float2 w = *reinterpret_cast<const float2 *>(&Ws[kk][2 * up]);
+        acc[0][0] = fmaf(x.x, w.x, acc[0][0]);
+        acc[0][1] = fmaf(x.x, w.y, acc[0][1]);
+        acc[1][0] = fmaf(x.y, w.x, acc[1][0]);
+        acc[1][1] = fmaf(x.y, w.y, acc[1][1]);
+        acc[2][0] = fmaf(x.z, w.x, acc[2][0]);
+        acc[2][1] = fmaf(x.z, w.y, acc[2][1]);
+        acc[3][0] = fmaf(x.w, w.x, acc[3][0]);
+        acc[3][1] = fmaf(x.w, w.y, acc[3][1]);
+    }
+    const int u = slice * kFcUnits + 2 * up;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int b = b0 + 4 * bq + j;
+        if (b < B)
+            *reinterpret_cast<float2 *>(pre + ((size_t)ks * B + b) * Hp + u) = make_float2(acc[j][0], acc[j][1]);
+    }
 }
 
-__global__ void value_final_kernel(const float *__restrict__ part, int nparts, int B, float b2,
-                                   int value_map, float *__restrict__ value) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) value_final_kernel(const float *__restrict__ pre, int B, int H, int Hp,
+                                                          const float *__restrict__ b1,
+                                                          const float *__restrict__ w2, float b2, int act,
+                                                          int value_map, float *__restrict__ value) {
+    __shared__ float red[32];
+    const int b = blockIdx.x;
     if (b >= B) return;
     float s = 0.0f;
-    for (int k = 0; k < nparts; ++k) s += part[(size_t)b * nparts + k];
-    const float t = tanhf(b2 + s);
-    value[b] = value_map ? (1.0f + t) / 2.0f : t;
+    for (int u = threadIdx.x; u < H; u += 256) {
+        float z = b1[u];
+#pragma unroll
+        for (int k = 0; k < kFcSplit; ++k) z += pre[((size_t)k * B + b) * Hp + u];
+        s = fmaf(w2[u], act_fn(z, act), s);
+    }
+    s = block_reduce<256>(s, false, red);
+    if (threadIdx.x == 0) {
+        const float t = tanhf(b2 + s);
+        value[b] = value_map ? (1.0f + t) / 2.0f : t;
+    }
 }
 
 // ------------------------------------------------------------ host launchers
@@ -371,14 +414,19 @@ void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cud
     softmax_kernel<<<B, 384, 0, s>>>(h, B, temperature, probs);
 }
 
-void launch_value_fc(const HeadIn &h, int B, const float *w1t, const float *b1, const float *w2,
+void launch_value_fc(const HeadIn &h, int B, const float *w1s, const float *b1, const float *w2,
                      float b2, int H, int act, int value_map, float *value, float *part,
                      cudaStream_t s) {
-    dim3 grid((B + kFcBM - 1) / kFcBM, (H + kFcBN - 1) / kFcBN);
-    value_fc1_kernel<<<grid, 256, 0, s>>>(h, B, w1t, b1, w2, H, act, part);
-    value_final_kernel<<<(B + 127) / 128, 128, 0, s>>>(part, (int)grid.y, B, b2, value_map, value);
+    const int slices = (H + kFcUnits - 1) / kFcUnits;
+    dim3 grid((B + kFcBoards - 1) / kFcBoards, slices, kFcSplit);
+    value_fc1_kernel<<<grid, 256, 0, s>>>(h, B, w1s, slices * kFcUnits, part);
+    value_final_kernel<<<B, 256, 0, s>>>(part, B, H, slices * kFcUnits, b1, w2, b2, act, value_map, value);
 }
 
-size_t value_fc_part_floats(int B, int H) { return (size_t)B * ((H + kFcBN - 1) / kFcBN); }
+size_t value_fc_part_floats(int B, int H) {
+    return (size_t)kFcSplit * B * (((H + kFcUnits - 1) / kFcUnits) * kFcUnits);
+}
+
+int value_fc_slice_units() { return kFcUnits; }
 
 }  // namespace lg

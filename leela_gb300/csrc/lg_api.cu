@@ -94,7 +94,7 @@ struct Net {
     std::vector<float *> bias;
     float *head_w = nullptr;     // [k*k][cin]
     float head_b = 0.0f;
-    float *w1t = nullptr, *b1 = nullptr, *w2 = nullptr;
+    float *w1s = nullptr, *b1 = nullptr, *w2 = nullptr;
     float b2 = 0.0f;
     // tensor-core path
     std::vector<TcConv> tc;
@@ -126,7 +126,7 @@ struct lg_ctx {
     float *d_logits = nullptr, *d_probs = nullptr, *d_value = nullptr;
     float *d_parts = nullptr;  // fused-head partial sums, [4][max_batch * 361]
     float *d_fcpart = nullptr; // value-head FC partial sums
-    int *d_flags = nullptr;    // per-CTA layer flags of the persistent trunk kernel
+    int *d_flags = nullptr;    // chunk flags and item counter of the persistent trunk kernel
     // pinned staging of the blocking calls, two slots so that chunk k+1 is
     // packed while chunk k runs: planes, outputs, logits, completion events
     uint8_t *h_planes = nullptr, *h_planes_b = nullptr;
@@ -339,20 +339,23 @@ int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
     if (d->value_head) {
         int H = d->fc_hidden;
         const float *W1 = w + off;
-        std::vector<float> w1t((size_t)kPoints * H), b1(W1 + (size_t)H * kPoints,
-                                                       W1 + (size_t)H * kPoints + H);
+        // W1 [H][361] stored sliced by hidden units: [H/U][361][U], U = 64,
+        // zero-padded past H, so one FC1 tile's weights are one block.
+        const int U = value_fc_slice_units(), slices = (H + U - 1) / U;
+        std::vector<float> w1s((size_t)slices * kPoints * U, 0.0f), b1(W1 + (size_t)H * kPoints,
+                                                                      W1 + (size_t)H * kPoints + H);
         std::vector<float> w2(W1 + (size_t)H * kPoints + H, W1 + (size_t)H * kPoints + 2 * H);
         bool lowp = d->precision != LG_FP32;
         for (int o = 0; o < H; ++o)
             for (int i = 0; i < kPoints; ++i) {
                 float v = W1[(size_t)o * kPoints + i];
                 if (lowp) v = __bfloat162float(__float2bfloat16(v));
-                w1t[(size_t)i * H + o] = v;
+                w1s[((size_t)(o / U) * kPoints + i) * U + o % U] = v;
             }
         if (lowp)
             for (auto &v : w2) v = __bfloat162float(__float2bfloat16(v));
         n.b2 = W1[(size_t)H * kPoints + 2 * H];
-        if ((rc = upload(c, &n.w1t, w1t)) || (rc = upload(c, &n.b1, b1)) ||
+        if ((rc = upload(c, &n.w1s, w1s)) || (rc = upload(c, &n.b1, b1)) ||
             (rc = upload(c, &n.w2, w2)))
             return rc;
     }
@@ -431,12 +434,12 @@ int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float
     }
     ++L;
     {
-        ProfScope ps(c, prof, LG_PROF_OTHER, s);
+        ProfScope ps(c, prof, LG_PROF_TAIL, s);
         HeadIn h{lg, 1, 0, 0.0f, 0, d.act, nullptr};
         if (!d.value_head)
             launch_softmax(h, B, T, probs, s);
         else
-            launch_value_fc(h, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
+            launch_value_fc(h, B, n.w1s, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
                             c->d_fcpart, s);
     }
     L += d.value_head ? 2 : 1;
@@ -450,7 +453,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
     int L = 0;
     const TcConv &first = n.tc[0];
     {
-        ProfScope ps(c, prof, LG_PROF_OTHER, s);
+        ProfScope ps(c, prof, LG_PROF_PACK, s);
         launch_pack_planes_l5(planes, B, d.c_in, first.halves, c->l5, s);
     }
     ++L;
@@ -509,13 +512,13 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
         if (l > 0) cur ^= 1;
     }
     {
-        ProfScope ps(c, prof, LG_PROF_OTHER, s);
+        ProfScope ps(c, prof, LG_PROF_TAIL, s);
         HeadIn h{c->d_parts, tc_head_parts(d.width, use_trunk ? 0 : var3), part_stride, n.head_b, d.act_head,
                  d.act, lg};
         if (!d.value_head)
             launch_softmax(h, B, T, probs, s);
         else
-            launch_value_fc(h, B, n.w1t, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
+            launch_value_fc(h, B, n.w1s, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
                             c->d_fcpart, s);
     }
     L += d.value_head ? 2 : 1;
@@ -934,12 +937,13 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
         return fail(LG_ERR_CUDA);
     const lg_net_desc *descs[2] = {policy, value};
     size_t max_act = 0, max_partial = 0, max_tc_l3 = 0, max_tc_l5 = 0;
-    int max_c_in = 0;
+    int max_c_in = 0, max_fc = 0;
     for (int i = 0; i < 2; ++i) {
         if (!descs[i]) continue;
         if ((rc = build_net(c, c->nets[i], descs[i]))) return fail(rc);
         Net &n = c->nets[i];
         max_c_in = std::max(max_c_in, n.d.c_in);
+        if (n.d.value_head) max_fc = std::max(max_fc, n.d.fc_hidden);
         if (n.d.precision == LG_FP32) {
             for (auto &s : n.shapes) {
                 max_act = std::max(max_act, (size_t)std::max(s.cin, s.cout));
@@ -978,8 +982,8 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
         (rc = dev_alloc(c, &c->d_probs, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)) ||
         (rc = dev_alloc(c, &c->d_parts, 4 * mb * kPoints)) ||
-        (rc = dev_alloc(c, &c->d_fcpart, value_fc_part_floats(max_batch, 4096))) ||
-        (rc = dev_alloc(c, &c->d_flags, 1024)))
+        (rc = dev_alloc(c, &c->d_fcpart, value_fc_part_floats(max_batch, std::max(max_fc, 1)))) ||
+        (rc = dev_alloc(c, &c->d_flags, std::max<size_t>(1024, trunk_flag_ints(max_batch * kL3Board)))))
         return fail(rc);
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(LG_ERR_CUDA);
     if (cudaMallocHost(&c->h_planes, mb * max_c_in * kPoints) != cudaSuccess ||

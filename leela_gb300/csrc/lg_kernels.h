@@ -26,12 +26,15 @@ struct HeadIn {
     float *logits_out;
 };
 void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s);
-// Value head: two launches (tiled FC1 + partial FC2, then a fixed-order sum
-// and the value map); `part` holds value_fc_part_floats(B, H) floats.
-void launch_value_fc(const HeadIn &h, int B, const float *w1t, const float *b1, const float *w2,
+// Value head: two launches (tiled split-K FC1 pre-activations, then a
+// fixed-order sum, b1, activation, FC2 and the value map); `part` holds
+// value_fc_part_floats(B, H) floats.  w1s is W1 sliced by
+// value_fc_slice_units() hidden units: [ceil(H/64)][361][64], zero-padded.
+void launch_value_fc(const HeadIn &h, int B, const float *w1s, const float *b1, const float *w2,
                      float b2, int H, int act, int value_map, float *value, float *part,
                      cudaStream_t s);
 size_t value_fc_part_floats(int B, int H);
+int value_fc_slice_units();
 
 // ------------------------------------------------- tensor-core (tcgen05) path
 //
@@ -72,9 +75,10 @@ int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *parts, size_t
 int tc_head_parts(int n, int variant = 0);
 
 // All 3x3 128->128 layers of a net in one persistent, cooperative launch
-// (tc_trunk_kernel): layer l reads buf_a when l is even and buf_b when odd,
-// and writes the other; the last layer writes head partial sums (4 parts)
-// when head_w is set.  flags: >= sm_count ints of device scratch.
+// (tc_trunk_kernel), scheduled as (layer, 256-row chunk) items claimed in
+// order: layer l reads buf_a when l is even and buf_b when odd, and writes
+// the other; the last layer writes head partial sums (4 parts) when head_w
+// is set.
 struct TcTrunk {
     const void *buf_a, *buf_b;  // L3 activation buffers [rows][128] BF16
     const void *w;              // [nl][9][2][128][64] BF16
@@ -85,8 +89,10 @@ struct TcTrunk {
     int rows;
     int nl;
 };
+// flags: trunk_flag_ints(rows) ints of device scratch (reset by the launch).
 int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
                     cudaStream_t s, int sm_count);
+size_t trunk_flag_ints(int rows);
 size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves);
 int tc_init_device();
 // Head kernels for the tensor-core path (logits already produced by the

@@ -604,16 +604,19 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
 
 // ===========================================================================
 // Kernel "trunk": every 3x3 128->128 layer of a net in one persistent
-// launch.  Each CTA owns the same contiguous row range in every layer and
-// runs kernel T's pipeline over it, layer after layer, ping-ponging between
-// two L3 buffers (layer l reads A when l is even, B when odd).  Layer l+1 of
-// CTA k reads rows up to 24 past its range, which CTAs k-1 and k+1 wrote, and
-// overwrites rows its neighbours read for layer l: so CTA k starts layer l+1
-// once CTAs k-1, k, k+1 have finished layer l.  A CTA publishes "layer l done"
-// in flags[k] (release, after its TMA stores completed); the producer polls
-// its neighbours' flags (acquire, bounded) before the first window load of a
-// layer.  The launch is cooperative so that all CTAs are resident.  The last
-// layer can carry the fused 1x1 head.
+// launch, scheduled as work items (layer l, chunk j) of 256 rows.  The
+// producer of each CTA claims items from a global counter in (layer, chunk)
+// order and runs kernel T's pipeline over each (its windows, weight stages,
+// MMAs, epilogue), ping-ponging between two L3 buffers (layer l reads A when
+// l is even, B when odd).  Item (l, j) reads rows [256j - 24, 256j + 280) of
+// layer l-1's output, written by items (l-1, j-1 .. j+1), and overwrites rows
+// that only those items read for layer l-1: so it starts once flags[j-1 ..
+// j+1] >= l.  flags[j] = number of layers whose chunk-j rows are stored
+// (published with release after the item's TMA stores completed; the
+// producer polls with acquire, bounded).  Items are claimed in order, so an
+// item's dependencies were claimed earlier by CTAs that are running: there
+// is no layer-wide barrier, faster SMs take more items, and every item but a
+// layer's last runs at N = 256.  The last layer can carry the fused 1x1 head.
 // ===========================================================================
 
 struct TrunkParams {
@@ -625,11 +628,12 @@ struct TrunkParams {
     int nl;
     float *parts;
     size_t part_stride;
-    int *flags;           // [gridDim.x], zero at launch
+    int *flags;           // [nchunks] chunk flags, then the item counter; zero at launch
     int *err;
 };
 
 constexpr uint32_t kFlagPolls = 1u << 22;  // x ~64 ns sleep: bounded at ~0.3 s
+constexpr int kItemRing = 4;               // item descriptors in flight per CTA
 
 template <bool HEAD>
 __global__ void __launch_bounds__(kTcThreadsT, 1)
@@ -645,11 +649,15 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
     uint8_t *wst = stg + C::STG_TOTAL;
 
     __shared__ uint64_t win_full[C::NWIN], win_empty[C::NWIN], w_full[C::S], w_empty[C::S];
-    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], layer_done;
+    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], item_done;
+    __shared__ uint64_t item_full[kItemRing], item_empty[kItemRing];
+    __shared__ int item_id[kItemRing];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    const int nchunks = (p.rows + C::TP - 1) / C::TP;
+    const int nitems = p.nl * nchunks;
     if (tid == 0) {
         for (int i = 0; i < C::NWIN; ++i) {
             mbar_init(&win_full[i], 1);
@@ -667,7 +675,11 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
             mbar_init(&w_full[i], 1);
             mbar_init(&w_empty[i], 1);
         }
-        mbar_init(&layer_done, 4);
+        for (int i = 0; i < kItemRing; ++i) {
+            mbar_init(&item_full[i], 1);
+            mbar_init(&item_empty[i], 1 + kEpiWarpsT);  // the MMA issuer and every epilogue warp
+        }
+        mbar_init(&item_done, 4);
         abort_flag = 0;
         fence_mbar_init();
         prefetch_tensormap(&in_a);
@@ -685,21 +697,36 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         atomicCAS(p.err, 0, code);
         atomicExch(&abort_flag, 1);
     };
-    int r0, r1;
-    cta_row_range(p.rows, r0, r1);
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
         if (lane == 0) {
             uint32_t g = 0, wn = 0;
-            for (int l = 0; l < p.nl && !abort_flag; ++l) {
-                const CUtensorMap *im = (l & 1) ? &in_b : &in_a;
+            for (int q = 0;; ++q) {
+                const int slot = q % kItemRing;
+                const uint32_t qk = (uint32_t)(q / kItemRing);
+                // Claim only once the item ring and the next window slot are
+                // free, so that a claimed item is worked on at once.
+                bool ok = mbar_wait(&item_empty[slot], (qk & 1) ^ 1, kWaitLimit);
+                const int ws0 = wn % C::NWIN;
+                ok = ok && mbar_wait(&win_empty[ws0], ((wn / C::NWIN) & 1) ^ 1, kWaitLimit);
+                int it = -1;
+                if (ok && !abort_flag) {
+                    it = atomicAdd(p.flags + nchunks, 1);
+                    if (it >= nitems) it = -1;
+                } else if (!ok) {
+                    fail(72);
+                }
+                item_id[slot] = it;
+                mbar_arrive(&item_full[slot]);  // releases item_id[slot]
+                if (it < 0) break;
+                const int l = it / nchunks, j = it - l * nchunks;
                 if (l > 0) {
-                    // neighbours (and this CTA) finished layer l-1
-                    const int lo = max(0, (int)blockIdx.x - 1), hi = min((int)gridDim.x - 1, (int)blockIdx.x + 1);
-                    for (int j = lo; j <= hi; ++j) {
+                    // layer l-1 of chunks j-1 .. j+1 is stored
+                    const int lo = max(0, j - 1), hi = min(nchunks - 1, j + 1);
+                    for (int jj = lo; jj <= hi; ++jj) {
                         uint32_t n = 0;
-                        while (ld_acquire_gpu(p.flags + j) < l && ++n < kFlagPolls) __nanosleep(64);
+                        while (ld_acquire_gpu(p.flags + jj) < l && ++n < kFlagPolls) __nanosleep(64);
                         if (n >= kFlagPolls) {
                             fail(71);
                             goto done_producer;
@@ -707,24 +734,24 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                     }
                     fence_proxy_async_global();
                 }
-                for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP) {
-                    const int row0 = cs - C::WPRE;
-                    for (int h = 0; h < HALVES; ++h, ++wn) {
-                        const int ws = wn % C::NWIN;
-                        const uint32_t wk = wn / C::NWIN;
-                        if (!mbar_wait(&win_empty[ws], (wk & 1) ^ 1, kWaitLimit)) { fail(72); goto done_producer; }
-                        mbar_arrive_expect_tx(&win_full[ws], C::WIN_HALF);
-                        for (int sb = 0; sb < 2; ++sb)
-                            tma_load_2d(win + ws * C::WIN_HALF + sb * C::SUBROWS * 128, im, &win_full[ws],
-                                        h * 64, row0 + sb * C::SUBROWS);
-                        for (int t = 0; t < C::NTAPS; ++t, ++g) {
-                            const int s = g % C::S;
-                            const uint32_t k = g / C::S;
-                            if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(73); goto done_producer; }
-                            mbar_arrive_expect_tx(&w_full[s], C::WST_BYTES);
-                            tma_load_2d(wst + s * C::WST_BYTES, &w_map, &w_full[s], 0,
-                                        ((l * C::NTAPS + t) * HALVES + h) * NO);
-                        }
+                const CUtensorMap *im = (l & 1) ? &in_b : &in_a;
+                const int row0 = j * C::TP - C::WPRE;
+                for (int h = 0; h < HALVES; ++h, ++wn) {
+                    const int ws = wn % C::NWIN;
+                    const uint32_t wk = wn / C::NWIN;
+                    // (the first half's slot was waited for before the claim)
+                    if (h > 0 && !mbar_wait(&win_empty[ws], (wk & 1) ^ 1, kWaitLimit)) { fail(73); goto done_producer; }
+                    mbar_arrive_expect_tx(&win_full[ws], C::WIN_HALF);
+                    for (int sb = 0; sb < 2; ++sb)
+                        tma_load_2d(win + ws * C::WIN_HALF + sb * C::SUBROWS * 128, im, &win_full[ws],
+                                    h * 64, row0 + sb * C::SUBROWS);
+                    for (int t = 0; t < C::NTAPS; ++t, ++g) {
+                        const int s = g % C::S;
+                        const uint32_t k = g / C::S;
+                        if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(74); goto done_producer; }
+                        mbar_arrive_expect_tx(&w_full[s], C::WST_BYTES);
+                        tma_load_2d(wst + s * C::WST_BYTES, &w_map, &w_full[s], 0,
+                                    ((l * C::NTAPS + t) * HALVES + h) * NO);
                     }
                 }
             }
@@ -734,42 +761,45 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             uint32_t g = 0, wn = 0;
-            int local = 0;
-            for (int l = 0; l < p.nl && !abort_flag; ++l) {
-                for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP, ++local) {
-                    const int nrows = min(C::TP, r1 - cs);
-                    const uint32_t idesc = idesc_bf16(128, nrows);
-                    const int acc = local & 1;
-                    const uint32_t ak = (uint32_t)(local >> 1);
-                    if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(74); goto done_mma; }
+            for (int q = 0;; ++q) {
+                const int slot = q % kItemRing;
+                if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, kWaitLimit)) { fail(75); break; }
+                const int it = item_id[slot];
+                mbar_arrive(&item_empty[slot]);
+                if (it < 0) break;
+                const int j = it % nchunks;
+                const int nrows = min(C::TP, p.rows - j * C::TP);
+                const uint32_t idesc = idesc_bf16(128, nrows);
+                const int acc = q & 1;
+                const uint32_t ak = (uint32_t)(q >> 1);
+                if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(76); break; }
+                tc_fence_after();
+                const uint32_t d_tmem = tmem + (uint32_t)(acc * C::TP);
+                bool first = true;
+                for (int h = 0; h < HALVES; ++h, ++wn) {
+                    const int ws = wn % C::NWIN;
+                    const uint32_t wk = wn / C::NWIN;
+                    if (!mbar_wait(&win_full[ws], wk & 1, kWaitLimit)) { fail(77); goto done_mma; }
                     tc_fence_after();
-                    const uint32_t d_tmem = tmem + (uint32_t)(acc * C::TP);
-                    bool first = true;
-                    for (int h = 0; h < HALVES; ++h, ++wn) {
-                        const int ws = wn % C::NWIN;
-                        const uint32_t wk = wn / C::NWIN;
-                        if (!mbar_wait(&win_full[ws], wk & 1, kWaitLimit)) { fail(75); goto done_mma; }
+                    const uint32_t win_addr = smem_u32(win + ws * C::WIN_HALF);
+                    for (int t = 0; t < C::NTAPS; ++t, ++g) {
+                        const int s = g % C::S;
+                        const uint32_t k = g / C::S;
+                        if (!mbar_wait(&w_full[s], k & 1, kWaitLimit)) { fail(78); goto done_mma; }
                         tc_fence_after();
-                        const uint32_t win_addr = smem_u32(win + ws * C::WIN_HALF);
-                        for (int t = 0; t < C::NTAPS; ++t, ++g) {
-                            const int s = g % C::S;
-                            const uint32_t k = g / C::S;
-                            if (!mbar_wait(&w_full[s], k & 1, kWaitLimit)) { fail(76); goto done_mma; }
-                            tc_fence_after();
-                            const uint32_t a_base = smem_u32(wst + s * C::WST_BYTES);
-                            const uint32_t b_base = win_addr + (uint32_t)(C::WPRE + tap_shift(KIND, t)) * 128u;
+                        const uint32_t a_base = smem_u32(wst + s * C::WST_BYTES);
+                        const uint32_t b_base = win_addr + (uint32_t)(C::WPRE + tap_shift(KIND, t)) * 128u;
 #pragma unroll
-                            for (int kk = 0; kk < 4; ++kk) {
-                                mma_bf16(d_tmem, sdesc_sw128(a_base + kk * 32), sdesc_sw128(b_base + kk * 32),
-                                         idesc, first ? 0u : 1u);
-                                first = false;
-                            }
-                            mma_commit(&w_empty[s]);
+                        for (int kk = 0; kk < 4; ++kk) {
+                            mma_bf16(d_tmem, sdesc_sw128(a_base + kk * 32), sdesc_sw128(b_base + kk * 32),
+                                     idesc, first ? 0u : 1u);
+                            first = false;
                         }
-                        mma_commit(&win_empty[ws]);
+                        mma_commit(&w_empty[s]);
                     }
-                    mma_commit(&acc_full[acc]);
+                    mma_commit(&win_empty[ws]);
                 }
+                mma_commit(&acc_full[acc]);
             }
         done_mma:;
         }
@@ -779,88 +809,94 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         const int rq = (warp - 2) >> 2;
         const int o = quarter * 32 + lane;
         const float hw = HEAD ? __ldg(p.head_w + o) : 0.0f;
-        int local = 0;
-        uint32_t uses = 0;
-        for (int l = 0; l < p.nl && !abort_flag; ++l) {
+        uint32_t uses = 0, done_n = 0;
+        for (int q = 0;; ++q) {
+            const int slot = q % kItemRing;
+            if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, kWaitLimit)) { fail(79); break; }
+            const int it = item_id[slot];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&item_empty[slot]);
+            if (it < 0) break;
+            const int l = it / nchunks, j = it - l * nchunks;
+            const int cs = j * C::TP;
             const float bias = __ldg(p.bias + l * NO + o);
             const float scale = p.scale ? __ldg(p.scale + l * NO + o) : 1.0f;
             const bool head_layer = HEAD && l == p.nl - 1;
             const CUtensorMap *om = (l & 1) ? &out_a : &out_b;
-            for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP, ++local) {
-                const int nrows = min(C::TP, r1 - cs);
-                const int nhalf = max(0, min(2, (nrows - rq * 64) / 32));
-                const int acc = local & 1;
-                const uint32_t ak = (uint32_t)(local >> 1);
-                if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(77); break; }
-                tc_fence_after();
-                const uint32_t t_base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * C::TP + rq * 64);
-                const int q_base = cs + rq * 64;
-                uint32_t v[2][32];
-                tmem_ld32(t_base, v[0]);
-                tmem_ld32(t_base + 32, v[1]);
-                tmem_ld_wait();
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&acc_empty[acc]);
+            const int nrows = min(C::TP, p.rows - cs);
+            const int nhalf = max(0, min(2, (nrows - rq * 64) / 32));
+            const int acc = q & 1;
+            const uint32_t ak = (uint32_t)(q >> 1);
+            if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(80); break; }
+            tc_fence_after();
+            const uint32_t t_base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * C::TP + rq * 64);
+            const int q_base = cs + rq * 64;
+            uint32_t v[2][32];
+            tmem_ld32(t_base, v[0]);
+            tmem_ld32(t_base + 32, v[1]);
+            tmem_ld_wait();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[acc]);
 #pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    if (c >= nhalf) break;
-                    float f[32];
+            for (int c = 0; c < 2; ++c) {
+                if (c >= nhalf) break;
+                float f[32];
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) f[j] = act_apply(fmaf(__uint_as_float(v[c][j]), scale, bias), p.act);
-                    if (head_layer) {
+                for (int jj = 0; jj < 32; ++jj) f[jj] = act_apply(fmaf(__uint_as_float(v[c][jj]), scale, bias), p.act);
+                if (head_layer) {
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) f[j] *= hw;
-                        const float sum = warp_transpose_sum(f, lane);
-                        int orow, point;
-                        bool valid;
-                        row_target<KIND>(q_base + c * 32 + lane, p.rows, orow, valid, point);
-                        if (valid) p.parts[(size_t)quarter * p.part_stride + point] = sum;
-                    } else {
-                        const uint32_t use = uses++;
-                        uint8_t *buf = stg + rq * C::STG_BYTES;
-                        if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) { fail(78); break; }
-                        const int row_lane = q_base + c * 32 + lane;
-                        const int rl = row_lane % kL3Board;
-                        const bool valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
-                        const unsigned vmask = __ballot_sync(0xffffffffu, valid_lane);
-                        __nv_bfloat16 *col = reinterpret_cast<__nv_bfloat16 *>(buf) + o;
+                    for (int jj = 0; jj < 32; ++jj) f[jj] *= hw;
+                    const float sum = warp_transpose_sum(f, lane);
+                    int orow, point;
+                    bool valid;
+                    row_target<KIND>(q_base + c * 32 + lane, p.rows, orow, valid, point);
+                    if (valid) p.parts[(size_t)quarter * p.part_stride + point] = sum;
+                } else {
+                    const uint32_t use = uses++;
+                    uint8_t *buf = stg + rq * C::STG_BYTES;
+                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) { fail(81); break; }
+                    const int row_lane = q_base + c * 32 + lane;
+                    const int rl = row_lane % kL3Board;
+                    const bool valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
+                    const unsigned vmask = __ballot_sync(0xffffffffu, valid_lane);
+                    __nv_bfloat16 *col = reinterpret_cast<__nv_bfloat16 *>(buf) + o;
 #pragma unroll
-                        for (int j = 0; j < 32; ++j)
-                            col[j * 128] = __float2bfloat16_rn(((vmask >> j) & 1u) ? f[j] : 0.0f);
-                        fence_proxy_async();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(&stg_full[rq]);
-                        if (quarter == 0 && lane == 0) {
-                            if (!mbar_wait(&stg_full[rq], use & 1, kWaitLimit)) {
-                                fail(79);
-                            } else {
-                                tma_store_2d(om, buf, 0, q_base + c * 32);
-                                bulk_commit();
-                                bulk_wait_read0();
-                            }
-                            mbar_arrive(&stg_empty[rq]);
+                    for (int jj = 0; jj < 32; ++jj)
+                        col[jj * 128] = __float2bfloat16_rn(((vmask >> jj) & 1u) ? f[jj] : 0.0f);
+                    fence_proxy_async();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&stg_full[rq]);
+                    if (quarter == 0 && lane == 0) {
+                        if (!mbar_wait(&stg_full[rq], use & 1, kWaitLimit)) {
+                            fail(82);
+                        } else {
+                            tma_store_2d(om, buf, 0, q_base + c * 32);
+                            bulk_commit();
+                            bulk_wait_read0();
                         }
-                        __syncwarp();
+                        mbar_arrive(&stg_empty[rq]);
                     }
+                    __syncwarp();
                 }
             }
             if (!head_layer) {
-                // Publish "layer l done" once all of this CTA's stores of it
-                // have completed.
+                // Publish "layer l of chunk j stored" once all four row
+                // groups' stores of this item have completed.
                 if (quarter == 0 && lane == 0) {
                     bulk_wait0();
-                    mbar_arrive(&layer_done);
+                    mbar_arrive(&item_done);
                 }
                 if (warp == 4 && lane == 0) {
-                    if (!mbar_wait(&layer_done, (uint32_t)(l & 1), kWaitLimit)) {
-                        fail(80);
+                    if (!mbar_wait(&item_done, done_n & 1, kWaitLimit)) {
+                        fail(83);
                     } else {
                         fence_proxy_async_global();
                         __threadfence();
-                        st_release_gpu(p.flags + blockIdx.x, l + 1);
+                        st_release_gpu(p.flags + j, l + 1);
                     }
                 }
+                ++done_n;
             }
         }
     }
@@ -897,10 +933,25 @@ __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__re
     if (b >= B) return;
     const uint8_t *src = planes + (size_t)b * C * kPoints;
     const int nbytes = C * kPoints;
-    if (((uintptr_t)src & 3) == 0) {
-        for (int i = threadIdx.x; i < nbytes / 4; i += blockDim.x)
-            reinterpret_cast<uint32_t *>(sp)[i] = reinterpret_cast<const uint32_t *>(src)[i];
-        for (int i = (nbytes / 4) * 4 + threadIdx.x; i < nbytes; i += blockDim.x) sp[i] = src[i];
+    if (((uintptr_t)src & 7) == 0) {
+        // 8-byte words, four loads in flight per thread before the stores
+        const int n8 = nbytes / 8;
+        const uint2 *s8 = reinterpret_cast<const uint2 *>(src);
+        uint2 *d8 = reinterpret_cast<uint2 *>(sp);
+        for (int base = 0; base < n8; base += 4 * 256) {
+            uint2 r[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int i = base + j * 256 + (int)threadIdx.x;
+                if (i < n8) r[j] = s8[i];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int i = base + j * 256 + (int)threadIdx.x;
+                if (i < n8) d8[i] = r[j];
+            }
+        }
+        for (int i = n8 * 8 + threadIdx.x; i < nbytes; i += blockDim.x) sp[i] = src[i];
     } else {
         for (int i = threadIdx.x; i < nbytes; i += blockDim.x) sp[i] = src[i];
     }
@@ -977,6 +1028,8 @@ int tc_init_device() {
 
 int tc_head_parts(int n, int variant) { return (n == 128 && variant == 0) ? 4 : 1; }
 
+size_t trunk_flag_ints(int rows) { return (size_t)(rows + TcTCfg<2, 0>::TP - 1) / TcTCfg<2, 0>::TP + 1; }
+
 template <int N, int HALVES, int KIND, bool HEAD>
 static int launch_a(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) {
     using Cfg = TcCfg<N, HALVES, KIND>;
@@ -1031,8 +1084,9 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     p.part_stride = part_stride;
     p.flags = flags;
     p.err = err;
-    const int grid = std::min((T.rows + 31) / 32, sm_count);
-    if (cudaMemsetAsync(flags, 0, sizeof(int) * grid, s) != cudaSuccess) {
+    const int nchunks = (T.rows + Cfg::TP - 1) / Cfg::TP;
+    const int grid = std::min(T.nl * nchunks, sm_count);
+    if (cudaMemsetAsync(flags, 0, sizeof(int) * (nchunks + 1), s) != cudaSuccess) {
         lg_set_error("launch_tc_trunk: flag reset failed");
         return LG_ERR_CUDA;
     }
