@@ -40,6 +40,9 @@ constexpr int kTcThreads = 320;
 constexpr int kEpiWarps = 8;
 // Kernel T: 2 control warps + 16 epilogue warps (4 per TMEM lane quarter).
 constexpr int kTcThreadsT = 576;
+// Kernel "trunk": + one window-producer warp (18).  19 warps put 5 on one of
+// the SM's four sub-partitions (16,384 registers each): at most 96 a thread.
+constexpr int kTrunkThreads = 608;
 constexpr int kEpiWarpsT = 16;
 constexpr uint32_t kWaitLimit = 1u << 26;
 
@@ -636,7 +639,7 @@ constexpr uint32_t kFlagPolls = 1u << 22;  // x ~64 ns sleep: bounded at ~0.3 s
 constexpr int kItemRing = 4;               // item descriptors in flight per CTA
 
 template <bool HEAD>
-__global__ void __launch_bounds__(kTcThreadsT, 1)
+__global__ void __maxnreg__(96)
     tc_trunk_kernel(const __grid_constant__ CUtensorMap in_a, const __grid_constant__ CUtensorMap in_b,
                     const __grid_constant__ CUtensorMap out_a, const __grid_constant__ CUtensorMap out_b,
                     const __grid_constant__ CUtensorMap w_map, const TrunkParams p) {
@@ -677,7 +680,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         }
         for (int i = 0; i < kItemRing; ++i) {
             mbar_init(&item_full[i], 1);
-            mbar_init(&item_empty[i], 1 + kEpiWarpsT);  // the MMA issuer and every epilogue warp
+            mbar_init(&item_empty[i], 2 + kEpiWarpsT);  // weight producer, MMA issuer, epilogue warps
         }
         mbar_init(&item_done, 4);
         abort_flag = 0;
@@ -698,10 +701,10 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
         atomicExch(&abort_flag, 1);
     };
 
-    if (warp == 0) {
-        // ------------------------------------------------ TMA producer
+    if (warp == kEpiWarpsT + 2) {
+        // ------------------------------------------------ item claims + windows
         if (lane == 0) {
-            uint32_t g = 0, wn = 0;
+            uint32_t wn = 0;
             for (int q = 0;; ++q) {
                 const int slot = q % kItemRing;
                 const uint32_t qk = (uint32_t)(q / kItemRing);
@@ -729,7 +732,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                         while (ld_acquire_gpu(p.flags + jj) < l && ++n < kFlagPolls) __nanosleep(64);
                         if (n >= kFlagPolls) {
                             fail(71);
-                            goto done_producer;
+                            goto done_windows;
                         }
                     }
                     fence_proxy_async_global();
@@ -740,22 +743,38 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                     const int ws = wn % C::NWIN;
                     const uint32_t wk = wn / C::NWIN;
                     // (the first half's slot was waited for before the claim)
-                    if (h > 0 && !mbar_wait(&win_empty[ws], (wk & 1) ^ 1, kWaitLimit)) { fail(73); goto done_producer; }
+                    if (h > 0 && !mbar_wait(&win_empty[ws], (wk & 1) ^ 1, kWaitLimit)) { fail(73); goto done_windows; }
                     mbar_arrive_expect_tx(&win_full[ws], C::WIN_HALF);
                     for (int sb = 0; sb < 2; ++sb)
                         tma_load_2d(win + ws * C::WIN_HALF + sb * C::SUBROWS * 128, im, &win_full[ws],
                                     h * 64, row0 + sb * C::SUBROWS);
+                }
+            }
+        done_windows:;
+        }
+    } else if (warp == 0) {
+        // ------------------------------------------------ weight stages
+        if (lane == 0) {
+            uint32_t g = 0;
+            for (int q = 0;; ++q) {
+                const int slot = q % kItemRing;
+                if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, kWaitLimit)) { fail(70); break; }
+                const int it = item_id[slot];
+                mbar_arrive(&item_empty[slot]);
+                if (it < 0) break;
+                const int l = it / nchunks;
+                for (int h = 0; h < HALVES; ++h) {
                     for (int t = 0; t < C::NTAPS; ++t, ++g) {
                         const int s = g % C::S;
                         const uint32_t k = g / C::S;
-                        if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(74); goto done_producer; }
+                        if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(74); goto done_weights; }
                         mbar_arrive_expect_tx(&w_full[s], C::WST_BYTES);
                         tma_load_2d(wst + s * C::WST_BYTES, &w_map, &w_full[s], 0,
                                     ((l * C::NTAPS + t) * HALVES + h) * NO);
                     }
                 }
             }
-        done_producer:;
+        done_weights:;
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
@@ -1092,7 +1111,7 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     }
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kTcThreadsT);
+    cfg.blockDim = dim3(kTrunkThreads);
     cfg.dynamicSmemBytes = Cfg::SMEM;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
