@@ -51,6 +51,8 @@ BATCH = 256
 POSITIONS = 8192
 # Algorithmic FLOPs of one 3x3 128->128 conv per position: 2 * 361 * 128 * 1152.
 FLOP_3X3_PER_POS = 2 * 361 * 128 * 1152
+# ... of the 5x5 24->128 first layer: 2 * 361 * 128 * 600.
+FLOP_5X5_PER_POS = 2 * 361 * 128 * 600
 # Policy (1,226,637,568) + value (1,226,822,912) FLOP per position.
 FLOP_PAIR_PER_POS = 2_453_460_480
 
@@ -330,7 +332,12 @@ def run_ours(args, world, rank, local):
         ctx.close()
         return
     peak, hbm, peak_kind = read_peaks()
-    if ntr:
+    if ntr and tuning.get("conv3x3") == 3:
+        # persistent kernel: the 5x5 first layer and all 11 3x3 layers of one net
+        kernel_name = "tc_trunk_kernel (5x5 24->128 + 11 x 3x3 128->128 in one launch, batch 256)"
+        n_dom, ms_dom = ntr, mstr
+        flop_launch = (11 * FLOP_3X3_PER_POS + FLOP_5X5_PER_POS) * BATCH
+    elif ntr:
         # persistent kernel: all 11 3x3 layers of one net per launch
         kernel_name = "tc_trunk_kernel (11 x 3x3 128->128 in one launch, batch 256)"
         n_dom, ms_dom = ntr, mstr

@@ -215,8 +215,9 @@ LG_API int lg_policy_device_static(lg_ctx *ctx, const uint8_t *planes, int B, fl
  * context's tensor-core nets with each kernel choice for the 3x3 layers
  * (0: one launch per layer with 256-row tiles on the transposed kernel,
  * 1: one launch per layer with 128-row tiles, which put twice as many CTAs
- * on a small batch, 2: all 3x3 layers in one persistent cooperative launch)
- * and for the first layer (0: 256-row, 1: 128-row tiles) and keeps the
+ * on a small batch, 2: all 3x3 layers in one persistent cooperative launch,
+ * 3: as 2 with the 5x5 first layer in the same launch) and for the first
+ * layer (0: 256-row, 1: 128-row tiles; unused by choice 3) and keeps the
  * fastest.  With a cache path, a table saved for the same device, SM count
  * and net shapes is loaded instead (unless force), and a new table is saved
  * there (written to a temporary file and renamed).  Without tuning every

@@ -462,14 +462,24 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
     int bl = 0;
     while ((1 << bl) < B && bl < 16) ++bl;
     const int var3 = c->tc_variant[bl][0], var1 = c->tc_variant[bl][1];
-    const bool use_trunk = var3 == 2 && n.trunk_w != nullptr;
+    const bool use_trunk = (var3 == 2 || var3 == 3) && n.trunk_w != nullptr;
+    // choice 3: the 5x5 first layer runs inside the trunk launch too
+    const bool fuse_first = use_trunk && var3 == 3 && first.k == 5 && first.halves == 2 && first.cout == 128;
     int cur = 0;
-    for (size_t l = 0; l < n.tc.size(); ++l) {
+    for (size_t l = fuse_first ? 1 : 0; l < n.tc.size(); ++l) {
         const TcConv &t = n.tc[l];
         const bool last = l + 1 == n.tc.size();
         if (use_trunk && l == 1) {
             // layers 1 .. end in one persistent launch; layer 0 wrote l3[0]
+            // (or runs as the launch's first items)
             TcTrunk tt{};
+            if (fuse_first) {
+                tt.buf5 = c->l5;
+                tt.rows5 = B * kL5Board;
+                tt.w0 = first.w;
+                tt.bias0 = first.bias;
+                tt.scale0 = first.scale;
+            }
             tt.buf_a = c->l3[0];
             tt.buf_b = c->l3[1];
             tt.w = n.trunk_w;
@@ -983,7 +993,7 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
         (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)) ||
         (rc = dev_alloc(c, &c->d_parts, 4 * mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_fcpart, value_fc_part_floats(max_batch, std::max(max_fc, 1)))) ||
-        (rc = dev_alloc(c, &c->d_flags, std::max<size_t>(1024, trunk_flag_ints(max_batch * kL3Board)))))
+        (rc = dev_alloc(c, &c->d_flags, std::max<size_t>(1024, trunk_flag_ints(max_batch * kL3Board, max_batch * kL5Board)))))
         return fail(rc);
     if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(LG_ERR_CUDA);
     if (cudaMallocHost(&c->h_planes, mb * max_c_in * kPoints) != cudaSuccess ||
@@ -1317,6 +1327,7 @@ bool load_tuning(lg_ctx *c, const char *path) {
         if (pos == std::string::npos) continue;
         int a = 0, d = 0;
         if (sscanf(text.c_str() + pos + strlen(pat), "%d, %d", &a, &d) != 2) return false;
+        if (a < 0 || a > 3 || d < 0 || d > 1) return false;
         table[b][0] = a;
         table[b][1] = d;
     }
@@ -1324,14 +1335,14 @@ bool load_tuning(lg_ctx *c, const char *path) {
     return true;
 }
 
-int save_tuning(lg_ctx *c, const char *path, const double (*ms)[6]) {
+int save_tuning(lg_ctx *c, const char *path, const double (*ms)[7]) {
     std::string tmp = std::string(path) + ".tmp";
     FILE *f = fopen(tmp.c_str(), "w");
     if (!f) {
         lg_set_error("cannot write %s", tmp.c_str());
         return LG_ERR_ARG;
     }
-    fprintf(f, "{\n \"key\": \"%s\",\n \"order\": \"[3x3 layers: 0 = 256-row transposed per layer, 1 = 128-row per layer, 2 = persistent trunk; first layer: 0 = 256-row, 1 = 128-row]; ms_per_forward for (3x3, first) = (0,0) (1,0) (2,0) (0,1) (1,1) (2,1)\",\n \"table\": {",
+    fprintf(f, "{\n \"key\": \"%s\",\n \"order\": \"[3x3 layers: 0 = 256-row transposed per layer, 1 = 128-row per layer, 2 = persistent trunk, 3 = persistent trunk with the first layer in it; first layer: 0 = 256-row, 1 = 128-row]; ms_per_forward for (3x3, first) = (0,0) (1,0) (2,0) (0,1) (1,1) (2,1) (3,0)\",\n \"table\": {",
             tune_key(c).c_str());
     bool first = true;
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16; ++b) {
@@ -1342,8 +1353,8 @@ int save_tuning(lg_ctx *c, const char *path, const double (*ms)[6]) {
     fprintf(f, "\n },\n \"ms_per_forward\": {");
     first = true;
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16; ++b) {
-        fprintf(f, "%s\n  \"%d\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]", first ? "" : ",", 1 << b, ms[b][0],
-                ms[b][1], ms[b][2], ms[b][3], ms[b][4], ms[b][5]);
+        fprintf(f, "%s\n  \"%d\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f, %.4f]", first ? "" : ",", 1 << b,
+                ms[b][0], ms[b][1], ms[b][2], ms[b][3], ms[b][4], ms[b][5], ms[b][6]);
         first = false;
     }
     fprintf(f, "\n }\n}\n");
@@ -1377,15 +1388,15 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
     LG_CUDA_TRY(cudaEventCreate(&e0));
     LG_CUDA_TRY(cudaEventCreate(&e1));
     LG_CUDA_TRY(cudaMemsetAsync(c->d_planes, 0, (size_t)c->max_batch * c->planes_c * kPoints, c->stream));
-    double ms[17][6] = {};
+    double ms[17][7] = {};
     int rc = LG_OK;
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16 && rc == LG_OK; ++b) {
         const int B = 1 << b;
         double best = 1e30;
         int best_v = 0;
-        for (int v = 0; v < 6 && rc == LG_OK; ++v) {
-            c->tc_variant[b][0] = v % 3;
-            c->tc_variant[b][1] = v / 3;
+        for (int v = 0; v < 7 && rc == LG_OK; ++v) {
+            c->tc_variant[b][0] = v < 6 ? v % 3 : 3;
+            c->tc_variant[b][1] = v < 6 ? v / 3 : 0;
             const int reps = B >= 64 ? 5 : 20;
             float t = 0.0f;
             for (int it = 0; it < 2 + reps && rc == LG_OK; ++it) {
@@ -1407,8 +1418,8 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
                 best_v = v;
             }
         }
-        c->tc_variant[b][0] = best_v % 3;
-        c->tc_variant[b][1] = best_v / 3;
+        c->tc_variant[b][0] = best_v < 6 ? best_v % 3 : 3;
+        c->tc_variant[b][1] = best_v < 6 ? best_v / 3 : 0;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1440,7 +1451,7 @@ extern "C" int lg_tuning(lg_ctx *c, int B, int *variant_3x3, int *variant_first)
 }
 
 extern "C" int lg_set_tuning(lg_ctx *c, int B, int variant_3x3, int variant_first) {
-    if (!c || B < 1 || variant_3x3 < 0 || variant_3x3 > 2 || variant_first < 0 || variant_first > 1) {
+    if (!c || B < 1 || variant_3x3 < 0 || variant_3x3 > 3 || variant_first < 0 || variant_first > 1) {
         lg_set_error("lg_set_tuning: bad arguments");
         return LG_ERR_ARG;
     }

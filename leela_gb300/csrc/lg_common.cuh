@@ -129,6 +129,14 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void 
         "r"(smem_u32(smem_src)), "r"(x), "r"(y)
         : "memory");
 }
+// Plain bulk copy shared -> global (no tensor map): both addresses 16-byte
+// aligned, bytes a multiple of 16; completes through the bulk groups below.
+__device__ __forceinline__ void bulk_store(void *gdst, const void *smem_src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(
+                     reinterpret_cast<uint64_t>(gdst)),
+                 "r"(smem_u32(smem_src)), "r"(bytes)
+                 : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 // Wait until the shared-memory sources of all committed bulk stores have been read.
 __device__ __forceinline__ void bulk_wait_read0() {

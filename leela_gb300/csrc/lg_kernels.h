@@ -79,6 +79,9 @@ int tc_head_parts(int n, int variant = 0);
 // order: layer l reads buf_a when l is even and buf_b when odd, and writes
 // the other; the last layer writes head partial sums (4 parts) when head_w
 // is set.
+// With buf5 set, the 5x5 first layer (L5 input rows5 = B * 399, weights
+// [5][2][128][64]) runs in the same launch as its own work items and writes
+// buf_a.
 struct TcTrunk {
     const void *buf_a, *buf_b;  // L3 activation buffers [rows][128] BF16
     const void *w;              // [nl][9][2][128][64] BF16
@@ -88,11 +91,15 @@ struct TcTrunk {
     int act;
     int rows;
     int nl;
+    const void *buf5 = nullptr;  // fused first layer: L5 rows [rows5][128] BF16
+    const void *w0 = nullptr;    // [5][2][128][64] BF16
+    const float *bias0 = nullptr, *scale0 = nullptr;
+    int rows5 = 0;
 };
-// flags: trunk_flag_ints(rows) ints of device scratch (reset by the launch).
+// flags: trunk_flag_ints(rows, rows5) ints of device scratch (reset by the launch).
 int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
                     cudaStream_t s, int sm_count);
-size_t trunk_flag_ints(int rows);
+size_t trunk_flag_ints(int rows, int rows5);
 size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves);
 int tc_init_device();
 // Head kernels for the tensor-core path (logits already produced by the

@@ -623,32 +623,64 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
 // ===========================================================================
 
 struct TrunkParams {
-    const float *bias;    // [nl][128]
+    const float *bias;    // [nl][128], the 3x3 layers
     const float *scale;   // [nl][128] or null
+    const float *bias0;   // [128]: the fused 5x5 first layer (rows5 > 0)
+    const float *scale0;  // [128] or null
     const float *head_w;  // [128] (HEAD)
+    __nv_bfloat16 *out0;  // the first layer's output rows (buffer A)
     int act;
-    int rows;
-    int nl;
+    int rows;             // L3 rows, B * 400
+    int rows5;            // L5 rows of the fused first layer, B * 399; 0 = none
+    int nl;               // 3x3 layers
     float *parts;
     size_t part_stride;
-    int *flags;           // [nchunks] chunk flags, then the item counter; zero at launch
+    int *flags;           // [n3] chunk flags, the item counter, [n5] first-layer chunk flags
     int *err;
+};
+
+// Shared memory of kernel "trunk": window slots sized for the first layer's
+// taller windows (5 taps of pitch 19) and used by both kinds of item.
+struct TrunkCfg {
+    using C0 = TcTCfg<2, 0>;
+    using C1 = TcTCfg<2, 1>;
+    static constexpr int TP = 256;
+    static constexpr int NWIN = 3;
+    static constexpr int WIN_SLOT = C1::WIN_HALF > C0::WIN_HALF ? C1::WIN_HALF : C0::WIN_HALF;
+    static constexpr int S = 4;
+    static constexpr int WST_BYTES = C0::WST_BYTES;
+    static constexpr int STG_BYTES = C0::STG_BYTES;
+    static constexpr int STG_TOTAL = 4 * STG_BYTES;
+    static constexpr int SMEM = 1024 + NWIN * WIN_SLOT + STG_TOTAL + S * WST_BYTES;
+    static_assert(C0::TP == TP && C1::TP == TP, "item rows");
+    static_assert(WIN_SLOT % 1024 == 0 && (C0::SUBROWS * 128) % 1024 == 0 && (C1::SUBROWS * 128) % 1024 == 0,
+                  "window boxes keep the 1024-byte swizzle alignment");
+    static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
 constexpr uint32_t kFlagPolls = 1u << 22;  // x ~64 ns sleep: bounded at ~0.3 s
 constexpr int kItemRing = 4;               // item descriptors in flight per CTA
 
+__device__ __forceinline__ bool poll_flag(const int *f, int want) {
+    uint32_t n = 0;
+    while (ld_acquire_gpu(f) < want && ++n < kFlagPolls) __nanosleep(64);
+    return n < kFlagPolls;
+}
+
 template <bool HEAD>
 __global__ void __maxnreg__(96)
     tc_trunk_kernel(const __grid_constant__ CUtensorMap in_a, const __grid_constant__ CUtensorMap in_b,
                     const __grid_constant__ CUtensorMap out_a, const __grid_constant__ CUtensorMap out_b,
-                    const __grid_constant__ CUtensorMap w_map, const TrunkParams p) {
-    using C = TcTCfg<2, 0>;
-    constexpr int HALVES = 2, KIND = 0, NO = 128;
+                    const __grid_constant__ CUtensorMap w_map, const __grid_constant__ CUtensorMap in5,
+                    const __grid_constant__ CUtensorMap w0_map, const TrunkParams p) {
+    using C = TrunkCfg;
+    using C0 = TrunkCfg::C0;
+    using C1 = TrunkCfg::C1;
+    constexpr int HALVES = 2, NO = 128;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *win = smem;
-    uint8_t *stg = smem + C::NWIN * C::WIN_HALF;
+    uint8_t *stg = smem + C::NWIN * C::WIN_SLOT;
     uint8_t *wst = stg + C::STG_TOTAL;
 
     __shared__ uint64_t win_full[C::NWIN], win_empty[C::NWIN], w_full[C::S], w_empty[C::S];
@@ -659,8 +691,22 @@ __global__ void __maxnreg__(96)
     __shared__ int abort_flag;
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    const int nchunks = (p.rows + C::TP - 1) / C::TP;
-    const int nitems = p.nl * nchunks;
+    const int n3 = (p.rows + C::TP - 1) / C::TP;
+    const int n5 = p.rows5 > 0 ? (p.rows5 + C::TP - 1) / C::TP : 0;
+    const int first = n5 > 0 ? 1 : 0;
+    const int nitems = n5 + p.nl * n3;
+    int *const flags0 = p.flags + n3 + 1;
+    // item -> (layer l, chunk j); layer 0 is the first layer when fused
+    auto decode = [&](int it, int &l, int &j) {
+        if (it < n5) {
+            l = 0;
+            j = it;
+        } else {
+            const int r = it - n5;
+            l = first + r / n3;
+            j = r - (r / n3) * n3;
+        }
+    };
     if (tid == 0) {
         for (int i = 0; i < C::NWIN; ++i) {
             mbar_init(&win_full[i], 1);
@@ -682,7 +728,7 @@ __global__ void __maxnreg__(96)
             mbar_init(&item_full[i], 1);
             mbar_init(&item_empty[i], 2 + kEpiWarpsT);  // weight producer, MMA issuer, epilogue warps
         }
-        mbar_init(&item_done, 4);
+        mbar_init(&item_done, kEpiWarpsT);
         abort_flag = 0;
         fence_mbar_init();
         prefetch_tensormap(&in_a);
@@ -690,6 +736,10 @@ __global__ void __maxnreg__(96)
         prefetch_tensormap(&out_a);
         prefetch_tensormap(&out_b);
         prefetch_tensormap(&w_map);
+        if (first) {
+            prefetch_tensormap(&in5);
+            prefetch_tensormap(&w0_map);
+        }
     }
     if (warp == 1) tmem_alloc(&tmem_base, 512);
     __syncthreads();
@@ -715,7 +765,7 @@ __global__ void __maxnreg__(96)
                 ok = ok && mbar_wait(&win_empty[ws0], ((wn / C::NWIN) & 1) ^ 1, kWaitLimit);
                 int it = -1;
                 if (ok && !abort_flag) {
-                    it = atomicAdd(p.flags + nchunks, 1);
+                    it = atomicAdd(p.flags + n3, 1);
                     if (it >= nitems) it = -1;
                 } else if (!ok) {
                     fail(72);
@@ -723,31 +773,47 @@ __global__ void __maxnreg__(96)
                 item_id[slot] = it;
                 mbar_arrive(&item_full[slot]);  // releases item_id[slot]
                 if (it < 0) break;
-                const int l = it / nchunks, j = it - l * nchunks;
-                if (l > 0) {
-                    // layer l-1 of chunks j-1 .. j+1 is stored
-                    const int lo = max(0, j - 1), hi = min(nchunks - 1, j + 1);
-                    for (int jj = lo; jj <= hi; ++jj) {
-                        uint32_t n = 0;
-                        while (ld_acquire_gpu(p.flags + jj) < l && ++n < kFlagPolls) __nanosleep(64);
-                        if (n >= kFlagPolls) {
+                int l, j;
+                decode(it, l, j);
+                const bool fl = first && l == 0;
+                const int k = l - first;  // 3x3 layer index
+                if (!fl && k == 0 && first) {
+                    // the first layer's chunks whose L5 rows feed L3 rows
+                    // [256j - 24, 256j + 280): an L5 row is the L3 row minus
+                    // (board + y), board + y <= rows / 400 + 19
+                    const int lo3 = max(0, j * C::TP - C0::WPRE);
+                    const int hi3 = min(p.rows, j * C::TP + C::TP + C0::WPRE);
+                    const int lo5 = max(0, lo3 - (hi3 - 1) / kL3Board - kBoard);
+                    const int hi5 = min(p.rows5 - 1, hi3 - 1);
+                    for (int jj = lo5 / C::TP; jj <= hi5 / C::TP; ++jj)
+                        if (!poll_flag(flags0 + jj, 1)) {
                             fail(71);
                             goto done_windows;
                         }
-                    }
+                    fence_proxy_async_global();
+                } else if (!fl && k > 0) {
+                    // layer k-1 of chunks j-1 .. j+1 is stored
+                    const int lo = max(0, j - 1), hi = min(n3 - 1, j + 1);
+                    for (int jj = lo; jj <= hi; ++jj)
+                        if (!poll_flag(p.flags + jj, k)) {
+                            fail(71);
+                            goto done_windows;
+                        }
                     fence_proxy_async_global();
                 }
-                const CUtensorMap *im = (l & 1) ? &in_b : &in_a;
-                const int row0 = j * C::TP - C::WPRE;
+                const CUtensorMap *im = fl ? &in5 : ((k & 1) ? &in_b : &in_a);
+                const int sub = fl ? C1::SUBROWS : C0::SUBROWS;
+                const uint32_t bytes = fl ? C1::WIN_HALF : C0::WIN_HALF;
+                const int row0 = j * C::TP - (fl ? C1::WPRE : C0::WPRE);
                 for (int h = 0; h < HALVES; ++h, ++wn) {
                     const int ws = wn % C::NWIN;
                     const uint32_t wk = wn / C::NWIN;
                     // (the first half's slot was waited for before the claim)
                     if (h > 0 && !mbar_wait(&win_empty[ws], (wk & 1) ^ 1, kWaitLimit)) { fail(73); goto done_windows; }
-                    mbar_arrive_expect_tx(&win_full[ws], C::WIN_HALF);
+                    mbar_arrive_expect_tx(&win_full[ws], bytes);
                     for (int sb = 0; sb < 2; ++sb)
-                        tma_load_2d(win + ws * C::WIN_HALF + sb * C::SUBROWS * 128, im, &win_full[ws],
-                                    h * 64, row0 + sb * C::SUBROWS);
+                        tma_load_2d(win + ws * C::WIN_SLOT + sb * sub * 128, im, &win_full[ws], h * 64,
+                                    row0 + sb * sub);
                 }
             }
         done_windows:;
@@ -762,15 +828,19 @@ __global__ void __maxnreg__(96)
                 const int it = item_id[slot];
                 mbar_arrive(&item_empty[slot]);
                 if (it < 0) break;
-                const int l = it / nchunks;
+                int l, j;
+                decode(it, l, j);
+                const bool fl = first && l == 0;
+                const int ntaps = fl ? C1::NTAPS : C0::NTAPS;
+                const CUtensorMap *wm = fl ? &w0_map : &w_map;
+                const int wl = fl ? 0 : l - first;
                 for (int h = 0; h < HALVES; ++h) {
-                    for (int t = 0; t < C::NTAPS; ++t, ++g) {
+                    for (int t = 0; t < ntaps; ++t, ++g) {
                         const int s = g % C::S;
                         const uint32_t k = g / C::S;
                         if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(74); goto done_weights; }
                         mbar_arrive_expect_tx(&w_full[s], C::WST_BYTES);
-                        tma_load_2d(wst + s * C::WST_BYTES, &w_map, &w_full[s], 0,
-                                    ((l * C::NTAPS + t) * HALVES + h) * NO);
+                        tma_load_2d(wst + s * C::WST_BYTES, wm, &w_full[s], 0, ((wl * ntaps + t) * HALVES + h) * NO);
                     }
                 }
             }
@@ -786,33 +856,39 @@ __global__ void __maxnreg__(96)
                 const int it = item_id[slot];
                 mbar_arrive(&item_empty[slot]);
                 if (it < 0) break;
-                const int j = it % nchunks;
-                const int nrows = min(C::TP, p.rows - j * C::TP);
+                int l, j;
+                decode(it, l, j);
+                const bool fl = first && l == 0;
+                const int ntaps = fl ? C1::NTAPS : C0::NTAPS;
+                // N: the item's rows, rounded up to the MMA's multiple of 16
+                // (rows past the tensor are zero-filled and not stored)
+                const int nrows = fl ? min(C::TP, (p.rows5 - j * C::TP + 15) / 16 * 16) : min(C::TP, p.rows - j * C::TP);
                 const uint32_t idesc = idesc_bf16(128, nrows);
                 const int acc = q & 1;
                 const uint32_t ak = (uint32_t)(q >> 1);
                 if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(76); break; }
                 tc_fence_after();
                 const uint32_t d_tmem = tmem + (uint32_t)(acc * C::TP);
-                bool first = true;
+                bool first_mma = true;
                 for (int h = 0; h < HALVES; ++h, ++wn) {
                     const int ws = wn % C::NWIN;
                     const uint32_t wk = wn / C::NWIN;
                     if (!mbar_wait(&win_full[ws], wk & 1, kWaitLimit)) { fail(77); goto done_mma; }
                     tc_fence_after();
-                    const uint32_t win_addr = smem_u32(win + ws * C::WIN_HALF);
-                    for (int t = 0; t < C::NTAPS; ++t, ++g) {
+                    const uint32_t win_addr = smem_u32(win + ws * C::WIN_SLOT);
+                    for (int t = 0; t < ntaps; ++t, ++g) {
                         const int s = g % C::S;
                         const uint32_t k = g / C::S;
                         if (!mbar_wait(&w_full[s], k & 1, kWaitLimit)) { fail(78); goto done_mma; }
                         tc_fence_after();
                         const uint32_t a_base = smem_u32(wst + s * C::WST_BYTES);
-                        const uint32_t b_base = win_addr + (uint32_t)(C::WPRE + tap_shift(KIND, t)) * 128u;
+                        const int brow = fl ? C1::WPRE + tap_shift(1, t) : C0::WPRE + tap_shift(0, t);
+                        const uint32_t b_base = win_addr + (uint32_t)brow * 128u;
 #pragma unroll
                         for (int kk = 0; kk < 4; ++kk) {
                             mma_bf16(d_tmem, sdesc_sw128(a_base + kk * 32), sdesc_sw128(b_base + kk * 32),
-                                     idesc, first ? 0u : 1u);
-                            first = false;
+                                     idesc, first_mma ? 0u : 1u);
+                            first_mma = false;
                         }
                         mma_commit(&w_empty[s]);
                     }
@@ -836,48 +912,72 @@ __global__ void __maxnreg__(96)
             __syncwarp();
             if (lane == 0) mbar_arrive(&item_empty[slot]);
             if (it < 0) break;
-            const int l = it / nchunks, j = it - l * nchunks;
+            int l, j;
+            decode(it, l, j);
+            const bool fl = first && l == 0;
+            const int k = l - first;
             const int cs = j * C::TP;
-            const float bias = __ldg(p.bias + l * NO + o);
-            const float scale = p.scale ? __ldg(p.scale + l * NO + o) : 1.0f;
-            const bool head_layer = HEAD && l == p.nl - 1;
-            const CUtensorMap *om = (l & 1) ? &out_a : &out_b;
-            const int nrows = min(C::TP, p.rows - cs);
-            const int nhalf = max(0, min(2, (nrows - rq * 64) / 32));
+            const float bias = fl ? __ldg(p.bias0 + o) : __ldg(p.bias + k * NO + o);
+            const float scale = fl ? (p.scale0 ? __ldg(p.scale0 + o) : 1.0f)
+                                   : (p.scale ? __ldg(p.scale + k * NO + o) : 1.0f);
+            const bool head_layer = HEAD && !fl && k == p.nl - 1;
+            const CUtensorMap *om = (k & 1) ? &out_a : &out_b;
+            const int rows_l = fl ? p.rows5 : p.rows;
+            const int nrows = min(C::TP, rows_l - cs);
+            const int nhalf = max(0, min(2, (nrows - rq * 64 + 31) / 32));
             const int acc = q & 1;
             const uint32_t ak = (uint32_t)(q >> 1);
             if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(80); break; }
             tc_fence_after();
             const uint32_t t_base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * C::TP + rq * 64);
             const int q_base = cs + rq * 64;
-            uint32_t v[2][32];
-            tmem_ld32(t_base, v[0]);
-            tmem_ld32(t_base + 32, v[1]);
-            tmem_ld_wait();
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_empty[acc]);
+            bool bad = false;
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
-                if (c >= nhalf) break;
+                // One 32-row half at a time (32 registers); the accumulator is
+                // released after the second half's load, which the MMA issuer
+                // needs again only one item later.
+                uint32_t v[32];
+                tmem_ld32(t_base + 32 * c, v);
+                tmem_ld_wait();
+                if (c == 1) {
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&acc_empty[acc]);
+                }
+                if (c >= nhalf || bad) continue;
                 float f[32];
 #pragma unroll
-                for (int jj = 0; jj < 32; ++jj) f[jj] = act_apply(fmaf(__uint_as_float(v[c][jj]), scale, bias), p.act);
+                for (int jj = 0; jj < 32; ++jj) f[jj] = act_apply(fmaf(__uint_as_float(v[jj]), scale, bias), p.act);
                 if (head_layer) {
 #pragma unroll
                     for (int jj = 0; jj < 32; ++jj) f[jj] *= hw;
                     const float sum = warp_transpose_sum(f, lane);
                     int orow, point;
                     bool valid;
-                    row_target<KIND>(q_base + c * 32 + lane, p.rows, orow, valid, point);
+                    row_target<0>(q_base + c * 32 + lane, p.rows, orow, valid, point);
                     if (valid) p.parts[(size_t)quarter * p.part_stride + point] = sum;
                 } else {
                     const uint32_t use = uses++;
                     uint8_t *buf = stg + rq * C::STG_BYTES;
-                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) { fail(81); break; }
+                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) {
+                        fail(81);
+                        bad = true;
+                        continue;
+                    }
                     const int row_lane = q_base + c * 32 + lane;
-                    const int rl = row_lane % kL3Board;
-                    const bool valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
+                    // 3x3 items: L3 rows, pad rows written as zeros.  First-
+                    // layer items: L5 rows; lane's L3 row (-1: pad row y =
+                    // 19, 20 or past the last board, not stored).
+                    int orow = -1;
+                    bool valid_lane;
+                    if (fl) {
+                        int point;
+                        row_target<1>(row_lane, p.rows5, orow, valid_lane, point);
+                    } else {
+                        const int rl = row_lane % kL3Board;
+                        valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
+                    }
                     const unsigned vmask = __ballot_sync(0xffffffffu, valid_lane);
                     __nv_bfloat16 *col = reinterpret_cast<__nv_bfloat16 *>(buf) + o;
 #pragma unroll
@@ -886,33 +986,60 @@ __global__ void __maxnreg__(96)
                     fence_proxy_async();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&stg_full[rq]);
-                    if (quarter == 0 && lane == 0) {
-                        if (!mbar_wait(&stg_full[rq], use & 1, kWaitLimit)) {
-                            fail(82);
+                    if (quarter == 0) {
+                        // every lane of the warp holds its row's target; lane 0 stores
+                        const bool ok = lane != 0 || mbar_wait(&stg_full[rq], use & 1, kWaitLimit);
+                        if (!ok) fail(82);
+                        if (!fl) {
+                            if (lane == 0 && ok) tma_store_2d(om, buf, 0, q_base + c * 32);
                         } else {
-                            tma_store_2d(om, buf, 0, q_base + c * 32);
-                            bulk_commit();
-                            bulk_wait_read0();
+                            // runs of rows whose L3 rows are consecutive: one
+                            // plain bulk copy each (at most 3 per 32 rows)
+                            const int prev = __shfl_up_sync(0xffffffffu, orow, 1);
+                            const bool starts = orow >= 0 && (lane == 0 || prev != orow - 1);
+                            unsigned smask = __ballot_sync(0xffffffffu, starts);
+                            const unsigned vm = __ballot_sync(0xffffffffu, orow >= 0);
+                            while (smask) {
+                                const int a = __ffs(smask) - 1;
+                                smask &= smask - 1;
+                                // run ends before the next start or the next non-stored row
+                                const unsigned gaps = ~vm & ~((2u << a) - 1u);  // lanes > a not stored
+                                const int nxt_start = smask ? __ffs(smask) - 1 : 32;
+                                const int nxt_gap = gaps ? __ffs(gaps) - 1 : 32;
+                                const int e = min(nxt_start, nxt_gap);
+                                const int r0 = __shfl_sync(0xffffffffu, orow, a);
+                                if (lane == 0 && ok)
+                                    bulk_store(p.out0 + (size_t)r0 * NO, buf + a * 256, (uint32_t)(e - a) * 256u);
+                            }
                         }
-                        mbar_arrive(&stg_empty[rq]);
+                        if (lane == 0) {
+                            if (ok) {
+                                bulk_commit();
+                                bulk_wait_read0();
+                            }
+                            mbar_arrive(&stg_empty[rq]);
+                        }
                     }
                     __syncwarp();
                 }
             }
             if (!head_layer) {
-                // Publish "layer l of chunk j stored" once all four row
-                // groups' stores of this item have completed.
-                if (quarter == 0 && lane == 0) {
-                    bulk_wait0();
-                    mbar_arrive(&item_done);
-                }
+                // Publish "chunk j of layer l stored" once every epilogue
+                // warp's stores of this item are complete (the quarter-0
+                // warps' bulk stores).
+                if (quarter == 0 && lane == 0) bulk_wait0();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&item_done);
                 if (warp == 4 && lane == 0) {
                     if (!mbar_wait(&item_done, done_n & 1, kWaitLimit)) {
                         fail(83);
                     } else {
                         fence_proxy_async_global();
                         __threadfence();
-                        st_release_gpu(p.flags + j, l + 1);
+                        if (fl)
+                            st_release_gpu(flags0 + j, 1);
+                        else
+                            st_release_gpu(p.flags + j, k + 1);
                     }
                 }
                 ++done_n;
@@ -1038,8 +1165,8 @@ int tc_init_device() {
     LG_A(64, 1, 0, false) LG_A(64, 1, 0, true) LG_A(64, 2, 1, false) LG_A(64, 3, 1, false)
     LG_A(128, 3, 1, false) LG_A(128, 2, 0, false) LG_A(128, 2, 0, true) LG_A(128, 2, 1, false)
     LG_T(2, 0, false) LG_T(2, 0, true) LG_T(2, 1, false)
-    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<false>), TcTCfg<2, 0>::SMEM>(tc_trunk_kernel<false>);
-    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<true>), TcTCfg<2, 0>::SMEM>(tc_trunk_kernel<true>);
+    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<false>), TrunkCfg::SMEM>(tc_trunk_kernel<false>);
+    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<true>), TrunkCfg::SMEM>(tc_trunk_kernel<true>);
 #undef LG_A
 #undef LG_T
     return rc;
@@ -1047,7 +1174,9 @@ int tc_init_device() {
 
 int tc_head_parts(int n, int variant) { return (n == 128 && variant == 0) ? 4 : 1; }
 
-size_t trunk_flag_ints(int rows) { return (size_t)(rows + TcTCfg<2, 0>::TP - 1) / TcTCfg<2, 0>::TP + 1; }
+size_t trunk_flag_ints(int rows, int rows5) {
+    return (size_t)(rows + TrunkCfg::TP - 1) / TrunkCfg::TP + 1 + (size_t)(rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP;
+}
 
 template <int N, int HALVES, int KIND, bool HEAD>
 static int launch_a(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) {
@@ -1080,47 +1209,63 @@ static int launch_t(const TcLayer &L, TcParams p, cudaStream_t s, int sm_count) 
 
 int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
                     cudaStream_t s, int sm_count) {
-    using Cfg = TcTCfg<2, 0>;
-    if (T.nl < 1 || T.rows <= 0 || (T.head_w && !parts)) {
+    using C0 = TrunkCfg::C0;
+    using C1 = TrunkCfg::C1;
+    const bool fused = T.buf5 != nullptr;
+    if (T.nl < 1 || T.rows <= 0 || (T.head_w && !parts) || (fused && (T.rows5 <= 0 || !T.w0 || !T.bias0))) {
         lg_set_error("launch_tc_trunk: bad arguments");
         return LG_ERR_ARG;
     }
-    CUtensorMap in_a, in_b, out_a, out_b, w_map;
-    int rc = encode_map_2d_bf16(&in_a, T.buf_a, 128, (uint64_t)T.rows, 64, Cfg::SUBROWS);
-    if (!rc) rc = encode_map_2d_bf16(&in_b, T.buf_b, 128, (uint64_t)T.rows, 64, Cfg::SUBROWS);
+    CUtensorMap in_a, in_b, out_a, out_b, w_map, in5, w0_map;
+    int rc = encode_map_2d_bf16(&in_a, T.buf_a, 128, (uint64_t)T.rows, 64, C0::SUBROWS);
+    if (!rc) rc = encode_map_2d_bf16(&in_b, T.buf_b, 128, (uint64_t)T.rows, 64, C0::SUBROWS);
     if (!rc) rc = encode_map_2d_bf16(&out_a, T.buf_a, 128, (uint64_t)T.rows, 128, 32, false);
     if (!rc) rc = encode_map_2d_bf16(&out_b, T.buf_b, 128, (uint64_t)T.rows, 128, 32, false);
-    if (!rc) rc = encode_map_2d_bf16(&w_map, T.w, 64, (uint64_t)T.nl * Cfg::NTAPS * 2 * 128, 64, 128);
+    if (!rc) rc = encode_map_2d_bf16(&w_map, T.w, 64, (uint64_t)T.nl * C0::NTAPS * 2 * 128, 64, 128);
+    if (fused) {
+        if (!rc) rc = encode_map_2d_bf16(&in5, T.buf5, 128, (uint64_t)T.rows5, 64, C1::SUBROWS);
+        if (!rc) rc = encode_map_2d_bf16(&w0_map, T.w0, 64, (uint64_t)C1::NTAPS * 2 * 128, 64, 128);
+    } else {
+        in5 = in_a;  // unused
+        w0_map = w_map;
+    }
     if (rc) return rc;
     TrunkParams p{};
     p.bias = T.bias;
     p.scale = T.scale;
+    p.bias0 = T.bias0;
+    p.scale0 = T.scale0;
     p.head_w = T.head_w;
+    p.out0 = (__nv_bfloat16 *)T.buf_a;
     p.act = T.act;
     p.rows = T.rows;
+    p.rows5 = fused ? T.rows5 : 0;
     p.nl = T.nl;
     p.parts = parts;
     p.part_stride = part_stride;
     p.flags = flags;
     p.err = err;
-    const int nchunks = (T.rows + Cfg::TP - 1) / Cfg::TP;
-    const int grid = std::min(T.nl * nchunks, sm_count);
-    if (cudaMemsetAsync(flags, 0, sizeof(int) * (nchunks + 1), s) != cudaSuccess) {
+    const int n3 = (T.rows + TrunkCfg::TP - 1) / TrunkCfg::TP;
+    const int n5 = fused ? (T.rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP : 0;
+    const int grid = std::min(n5 + T.nl * n3, sm_count);
+    if (cudaMemsetAsync(flags, 0, sizeof(int) * (n3 + 1 + n5), s) != cudaSuccess) {
         lg_set_error("launch_tc_trunk: flag reset failed");
         return LG_ERR_CUDA;
     }
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kTrunkThreads);
-    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.dynamicSmemBytes = TrunkCfg::SMEM;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = T.head_w ? cudaLaunchKernelEx(&cfg, tc_trunk_kernel<true>, in_a, in_b, out_a, out_b, w_map, p)
-                             : cudaLaunchKernelEx(&cfg, tc_trunk_kernel<false>, in_a, in_b, out_a, out_b, w_map, p);
+    cudaError_t e = T.head_w ? cudaLaunchKernelEx(&cfg, tc_trunk_kernel<true>, in_a, in_b, out_a, out_b, w_map, in5,
+                                                  w0_map, p)
+                             : cudaLaunchKernelEx(&cfg, tc_trunk_kernel<false>, in_a, in_b, out_a, out_b, w_map, in5,
+                                                  w0_map, p);
     if (e != cudaSuccess) {
         lg_set_error("trunk launch: %s", cudaGetErrorString(e));
         return LG_ERR_CUDA;

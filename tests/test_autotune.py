@@ -24,7 +24,7 @@ def f64(positions, weights, oracle_mod):
     return lp, v
 
 
-@pytest.mark.parametrize("v3,v1", [(0, 0), (1, 0), (0, 1), (1, 1), (2, 0), (2, 1)])
+@pytest.mark.parametrize("v3,v1", [(0, 0), (1, 0), (0, 1), (1, 1), (2, 0), (2, 1), (3, 0)])
 @pytest.mark.parametrize("B", [1, 5, 64])
 def test_every_variant_meets_the_bf16_bars(gpu_lib, weights, positions, f64, v3, v1, B):
     lg = gpu_lib
@@ -62,17 +62,38 @@ def test_autotune_writes_and_reloads_its_cache(gpu_lib, weights, positions, tmp_
 
 
 @pytest.mark.parametrize("B", [1, 3, 64])
-def test_fp8_trunk_matches_per_layer_kernels(gpu_lib, weights, positions, B):
-    """The persistent trunk kernel (3x3 choice 2) computes the same layers as
-    the per-layer launches, FP8 weights (per-channel scales) included."""
+@pytest.mark.parametrize("v3", [2, 3])
+def test_fp8_trunk_matches_per_layer_kernels(gpu_lib, weights, positions, B, v3):
+    """The persistent trunk kernel (3x3 choice 2; choice 3 with the first
+    layer in the same launch) computes the same layers as the per-layer
+    launches, FP8 weights (per-channel scales) included."""
     lg = gpu_lib
     with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "fp8w"),
                     value=lg.NetDesc.config1_value(weights["cfg_v"][1], "fp8w"), max_batch=64) as c:
         c.set_tuning(B, 0, 0)
         p0, l0 = c.policy(positions["planes_p"][:B, :24], 1.0, return_logits=True)
         v0 = c.value(positions["planes_v"][:B, :24])
-        c.set_tuning(B, 2, 0)
+        c.set_tuning(B, v3, 0)
         p2, l2 = c.policy(positions["planes_p"][:B, :24], 1.0, return_logits=True)
         v2 = c.value(positions["planes_v"][:B, :24])
     assert rel_logit_err(l2, l0).max() < 1e-5
     assert np.abs(v2 - v0).max() < 1e-5
+
+
+@pytest.mark.parametrize("B", [1, 7, 64, 256])
+def test_fused_first_layer_trunk_equals_separate_first_layer(gpu_lib, weights, positions, B):
+    """Choice 3 (first layer as work items of the trunk launch) and choice 2
+    (first layer in its own launch, same 256-row tiles and K order) give the
+    same BF16 results; B = 7 leaves a ragged last L5 chunk (2793 rows)."""
+    lg = gpu_lib
+    idx = np.arange(B) % 1024
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"), max_batch=256) as c:
+        c.set_tuning(B, 2, 0)
+        _, l2 = c.policy(positions["planes_p"][idx, :24], 1.0, return_logits=True)
+        v2 = c.value(positions["planes_v"][idx, :24])
+        c.set_tuning(B, 3, 0)
+        _, l3 = c.policy(positions["planes_p"][idx, :24], 1.0, return_logits=True)
+        v3 = c.value(positions["planes_v"][idx, :24])
+    assert rel_logit_err(l3, l2).max() < 1e-5
+    assert np.abs(v3 - v2).max() < 1e-5
