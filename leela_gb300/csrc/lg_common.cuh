@@ -129,6 +129,11 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void 
         "r"(smem_u32(smem_src)), "r"(x), "r"(y)
         : "memory");
 }
+// Named barrier `id` (1..15) over `nthreads` threads (a multiple of 32).
+__device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // Plain bulk copy shared -> global (no tensor map): both addresses 16-byte
 // aligned, bytes a multiple of 16; completes through the bulk groups below.
 __device__ __forceinline__ void bulk_store(void *gdst, const void *smem_src, uint32_t bytes) {

@@ -67,9 +67,9 @@ int launch_gather(const int8_t *squares, const int8_t *to_move, int B, int which
 // halves*64 channels: channel dx*C + c = plane c at (y, x + dx - 2).
 void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv_bfloat16 *out,
                            cudaStream_t s);
-// Writes the layer output (L3 rows) or, for the fused head, head partial sums
-// into parts ([tc_head_parts(n)][boards*361]).  Returns LG_ERR_ARG if no
-// kernel covers the shape.
+// Writes the layer output (L3 rows) or, for the fused head, the head output
+// before its bias into parts[boards*361] (tc_head_parts() = 1 array).
+// Returns LG_ERR_ARG if no kernel covers the shape.
 int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *parts, size_t part_stride,
                    int *err, cudaStream_t s, int sm_count);
 int tc_head_parts(int n, int variant = 0);

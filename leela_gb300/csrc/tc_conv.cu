@@ -354,6 +354,26 @@ __device__ __forceinline__ float warp_transpose_sum(float (&a)[32], int lane) {
     return a[0];
 }
 
+// Fused 1x1 head: each of a row group's four epilogue warps (warps
+// 2 + 4 rq .. 5 + 4 rq, one 32-channel quarter each) holds its partial sum for
+// the group's 32 rows (lane = row); they are added in quarter order 0..3 in
+// shared memory (red: 128 floats of this group) and quarter 0 writes the
+// head output of each board point.  All four warps must call it.
+template <int KIND>
+__device__ __forceinline__ void head_store(float sum, float *red, int rq, int quarter, int lane, int row, int rows,
+                                           float *parts) {
+    red[quarter * 32 + lane] = sum;
+    named_bar_sync(1 + rq, 128);
+    if (quarter == 0) {
+        const float tot = ((red[lane] + red[32 + lane]) + red[64 + lane]) + red[96 + lane];
+        int orow, point;
+        bool valid;
+        row_target<KIND>(row, rows, orow, valid, point);
+        if (valid) parts[point] = tot;
+    }
+    named_bar_sync(1 + rq, 128);
+}
+
 // Kernel T work split: the rows are cut into 32-row blocks, each CTA takes
 // an even contiguous range of blocks and walks it in chunks of up to 256 rows
 // (the MMA's N is the chunk's row count), so that no SM runs a whole extra
@@ -381,6 +401,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
     __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
+    __shared__ float head_red[HEAD ? 4 * 128 : 1];
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     if (tid == 0) {
@@ -531,11 +552,8 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                 if (HEAD) {
 #pragma unroll
                     for (int j = 0; j < 32; ++j) f[j] *= hw;
-                    const float sum = warp_transpose_sum(f, lane);
-                    int orow, point;
-                    bool valid;
-                    row_target<KIND>(q_base + c * 32 + lane, p.rows, orow, valid, point);
-                    if (valid) p.parts[(size_t)quarter * p.part_stride + point] = sum;
+                    head_store<KIND>(warp_transpose_sum(f, lane), head_red + rq * 128, rq, quarter, lane,
+                                     q_base + c * 32 + lane, p.rows, p.parts);
                 } else if (C::STAGED) {
                     // Rows q_base + c*32 .. +31 -> staging buffer of this row
                     // group as [32 rows][128 channels] BF16 (pad rows 0), then
@@ -689,6 +707,7 @@ __global__ void __maxnreg__(96)
     __shared__ int item_id[kItemRing];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
+    __shared__ float head_red[HEAD ? 4 * 128 : 1];
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     const int n3 = (p.rows + C::TP - 1) / C::TP;
@@ -952,11 +971,8 @@ __global__ void __maxnreg__(96)
                 if (head_layer) {
 #pragma unroll
                     for (int jj = 0; jj < 32; ++jj) f[jj] *= hw;
-                    const float sum = warp_transpose_sum(f, lane);
-                    int orow, point;
-                    bool valid;
-                    row_target<0>(q_base + c * 32 + lane, p.rows, orow, valid, point);
-                    if (valid) p.parts[(size_t)quarter * p.part_stride + point] = sum;
+                    head_store<0>(warp_transpose_sum(f, lane), head_red + rq * 128, rq, quarter, lane,
+                                  q_base + c * 32 + lane, p.rows, p.parts);
                 } else {
                     const uint32_t use = uses++;
                     uint8_t *buf = stg + rq * C::STG_BYTES;
@@ -1172,7 +1188,7 @@ int tc_init_device() {
     return rc;
 }
 
-int tc_head_parts(int n, int variant) { return (n == 128 && variant == 0) ? 4 : 1; }
+int tc_head_parts(int n, int variant) { return 1; }
 
 size_t trunk_flag_ints(int rows, int rows5) {
     return (size_t)(rows + TrunkCfg::TP - 1) / TrunkCfg::TP + 1 + (size_t)(rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP;
