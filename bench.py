@@ -507,12 +507,15 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
         dev_rate = n / (e0.elapsed_time(e1) / 1e3)
     out["fp32_plain_batch1"] = {"host_api_positions_per_s": host_rate,
                                 "device_positions_per_s": dev_rate}
-    # BF16 at the other configured batch sizes (device-resident inputs).
+    # BF16 at the other configured batch sizes (device-resident inputs),
+    # autotuned as a user's context would be.
+    import tempfile
     by_batch = {}
     for b in (1, 8, 64, 256):
         with lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"),
                         value=lg.NetDesc.config1_value(wv, "bf16"), device=dev.index,
                         max_batch=b) as cb:
+            cb.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{b}.json"))
             probs = torch.empty((b, 361), device=dev)
             val = torch.empty(b, device=dev)
             reps = max(4, min(200, 4096 // b))

@@ -273,6 +273,9 @@ def run_config4(planes_p, planes_v, position_index, mc_winrate, wp, wv, device=0
             Context(policy=NetDesc.config1_policy(wp, "bf16"),
                     value=NetDesc.config1_value(wv, "bf16"), device=device,
                     max_batch=batch) as cf:
+        # both nets with their kernel choices tuned, as a serving context runs
+        cs.autotune()
+        cf.autotune()
         sp = torch.empty((T, 361), device=dev)
         fp = torch.empty((T, 361), device=dev)
         fv = torch.empty(T, device=dev)

@@ -2,7 +2,9 @@
 // FP32 accumulate, M=128, K=16) with both operands resident in shared memory,
 // one CTA per SM: N in {64,128,256}; the A start row aligned (mode 0), shifted
 // by 3 rows (mode 1), or cycling through the nine 3x3 tap shifts of the L3
-// layout (mode 2).  Build and run on a GB300:
+// layout (mode 2); the B start row (N rows) cycling through the nine tap
+// shifts (mode 3, the conv kernels' case) or through nine multiples of 8
+// rows (mode 4).  Build and run on a GB300:
 //   nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 \
 //        -o tc_mma_rate leela_gb300/microbench/tc_mma_rate.cu && ./tc_mma_rate
 #include <cstdio>
@@ -14,31 +16,40 @@ using namespace lg::ptx;
 
 __device__ __forceinline__ uint32_t idesc_n(int N) { return idesc_bf16(128, N); }
 
-// mode: 0 = aligned A, 1 = A shifted by 3 rows, 2 = A cycling 9 tap shifts
-template <int N>
-__global__ void __launch_bounds__(128, 1) bench(int iters, int mode, unsigned long long *cycles, int *err) {
+// MODE: 0 = aligned, 1 = A shifted by 3 rows, 2 = A cycling 9 tap shifts,
+// 3 = B cycling 9 tap shifts, 4 = B cycling 9 multiples of 8 rows.  The 36
+// (tap, K step) descriptors of one round are compile-time offsets of two base
+// descriptors (the start-address field is addr >> 4 in the low 14 bits and
+// never carries), so the one issuing thread spends a few instructions per MMA.
+template <int N, int MODE>
+__global__ void __launch_bounds__(128, 1) bench(int rounds, unsigned long long *cycles, int *err) {
     extern __shared__ __align__(1024) uint8_t raw[];
     uint8_t *sm = (uint8_t *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
     uint8_t *A = sm;                 // 256 rows x 128 B
-    uint8_t *Bm = sm + 256 * 128;    // 256 rows x 128 B
+    uint8_t *Bm = sm + 256 * 128;    // 256 + 64 rows x 128 B
     __shared__ uint64_t bar;
     __shared__ uint32_t tb;
     int tid = threadIdx.x, warp = tid / 32;
-    for (int i = tid; i < 512 * 128 / 16; i += 128) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < 576 * 128 / 16; i += 128) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
     fence_proxy_async();
     if (tid == 0) { mbar_init(&bar, 1); fence_mbar_init(); }
     if (warp == 0) tmem_alloc(&tb, 256);
     __syncthreads();
     tc_fence_after();
     if (tid == 0) {
-        const int shifts[9] = {3, 4, 5, 23, 24, 25, 43, 44, 45};
-        uint32_t id = idesc_n(N);
+        constexpr uint32_t id = idesc_bf16(128, N);
+        const uint64_t a0 = sdesc_sw128(smem_u32(A)), b0 = sdesc_sw128(smem_u32(Bm));
         unsigned long long t0 = clock64();
-        for (int i = 0; i < iters; ++i) {
-            int r = mode == 0 ? 0 : (mode == 1 ? 3 : shifts[(i >> 2) % 9]);
-            uint64_t ad = sdesc_sw128(smem_u32(A + r * 128 + (i & 3) * 32));
-            uint64_t bd = sdesc_sw128(smem_u32(Bm + (i & 3) * 32));
-            mma_bf16(tb, ad, bd, id, i > 0);
+        for (int r = 0; r < rounds; ++r) {
+#pragma unroll
+            for (int u = 0; u < 36; ++u) {
+                const int t9 = u / 4, kk = u % 4;
+                const int tap = 3 + (t9 / 3) * 20 + t9 % 3;  // the 3x3 tap shifts 3,4,5,23,..,45 (L3 pitch 20)
+                const int ra = MODE == 1 ? 3 : (MODE == 2 ? tap : 0);
+                const int rb = MODE == 3 ? tap : (MODE == 4 ? 8 * t9 : 0);
+                mma_bf16(tb, a0 + (uint64_t)((ra * 128 + kk * 32) >> 4), b0 + (uint64_t)((rb * 128 + kk * 32) >> 4), id,
+                         (r > 0 || u > 0) ? 1u : 0u);
+            }
         }
         mma_commit(&bar);
         if (!mbar_wait(&bar, 0, 1u << 28)) atomicExch(err, 1);
@@ -50,33 +61,38 @@ __global__ void __launch_bounds__(128, 1) bench(int iters, int mode, unsigned lo
     if (warp == 0) { tmem_dealloc(tb, 256); tmem_relinquish(); }
 }
 
+template <int N, int MODE>
+void run(int sms, int smem, int rounds, unsigned long long *dc, int *de) {
+    cudaFuncSetAttribute(bench<N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    std::vector<unsigned long long> h(sms);
+    for (int grid : {1, sms}) {
+        cudaEvent_t a, b; cudaEventCreate(&a); cudaEventCreate(&b);
+        cudaEventRecord(a);
+        bench<N, MODE><<<grid, 128, smem>>>(rounds, dc, de);
+        cudaEventRecord(b);
+        cudaError_t e = cudaEventSynchronize(b);
+        float ms; cudaEventElapsedTime(&ms, a, b);
+        cudaMemcpy(h.data(), dc, grid * 8, cudaMemcpyDeviceToHost);
+        unsigned long long mx = 0; for (int i = 0; i < grid; ++i) mx = h[i] > mx ? h[i] : mx;
+        double macs = 128.0 * N * 16 * 36 * rounds;
+        printf("N=%3d mode=%d grid=%3d: %8llu clk  %.0f MAC/clk/SM  %.1f TFLOP/s total (%.3f ms) %s\n", N, MODE, grid, mx,
+               macs / mx, 2 * macs * grid / (ms * 1e-3) / 1e12, ms, cudaGetErrorString(e));
+    }
+}
+
 int main() {
     int sms; cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     unsigned long long *dc; int *de;
     cudaMalloc(&dc, sms * 8); cudaMalloc(&de, 4); cudaMemset(de, 0, 4);
-    int smem = 1024 + 512 * 128;
-    cudaFuncSetAttribute(bench<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(bench<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(bench<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    std::vector<unsigned long long> h(sms);
-    const int iters = 4096;
-    for (int n : {64, 128, 256})
-        for (int mode = 0; mode < 3; ++mode)
-            for (int grid : {1, sms}) {
-                cudaEvent_t a, b; cudaEventCreate(&a); cudaEventCreate(&b);
-                cudaEventRecord(a);
-                if (n == 64) bench<64><<<grid, 128, smem>>>(iters, mode, dc, de);
-                if (n == 128) bench<128><<<grid, 128, smem>>>(iters, mode, dc, de);
-                if (n == 256) bench<256><<<grid, 128, smem>>>(iters, mode, dc, de);
-                cudaEventRecord(b);
-                cudaError_t e = cudaEventSynchronize(b);
-                float ms; cudaEventElapsedTime(&ms, a, b);
-                cudaMemcpy(h.data(), dc, grid * 8, cudaMemcpyDeviceToHost);
-                unsigned long long mx = 0; for (int i = 0; i < grid; ++i) mx = h[i] > mx ? h[i] : mx;
-                double macs = 128.0 * n * 16 * iters;
-                printf("N=%3d mode=%d grid=%3d: %8llu clk  %.0f MAC/clk/SM  %.1f TFLOP/s total (%.3f ms) %s\n", n, mode, grid, mx,
-                       macs / mx, 2 * macs * grid / (ms * 1e-3) / 1e12, ms, cudaGetErrorString(e));
-            }
+    const int smem = 1024 + 576 * 128, rounds = 114;  // 4104 MMAs per CTA
+    run<64, 0>(sms, smem, rounds, dc, de);
+    run<128, 0>(sms, smem, rounds, dc, de);
+    run<256, 0>(sms, smem, rounds, dc, de);
+    run<256, 1>(sms, smem, rounds, dc, de);
+    run<256, 2>(sms, smem, rounds, dc, de);
+    run<256, 3>(sms, smem, rounds, dc, de);
+    run<256, 4>(sms, smem, rounds, dc, de);
+    run<128, 3>(sms, smem, rounds, dc, de);
     int he; cudaMemcpy(&he, de, 4, cudaMemcpyDeviceToHost);
     printf("err=%d\n", he);
     return 0;
