@@ -135,30 +135,34 @@ LG_API int lg_value_device(lg_ctx *ctx, const uint8_t *planes, int B, float *val
 
 /* Input planes from boards, on the GPU.  squares [B][361] (0 black, 1 white,
  * 2 empty; point y*19+x, the order the planes use), to_move [B] (0 black,
- * 1 white); planes [B][nplanes][361] bytes, nplanes <= 24.  which = 0 writes
+ * 1 white); planes [B][nplanes][361] bytes, nplanes <= 32.  which = 0 writes
  * planes 0..nplanes-1 of the policy set, which = 1 of the value set: stone
- * colours, liberties of each string and the liberties a stone of either
- * colour would have on each empty point after its captures (0 for a
- * suicide), bit-exact with the reference gather.  Planes 24..31 (ladders,
- * ko, move history, komi, third line) are not produced.  Device pointers,
+ * colours, liberties of each string, the liberties a stone of either colour
+ * would have on each empty point after its captures (0 for a suicide), the
+ * ladder reader's "ladder" and "ladder win" planes, the ko point, the last
+ * two moves (policy set), white's komi and the third line -- bit-exact with
+ * the reference gather.  moves [B][4] int32 (last move, the move before it,
+ * ko point: point indices, -1 for none; white-has-komi flag 0/1) is read only
+ * for planes 24..31 and may be NULL when nplanes <= 24.  Device pointers,
  * enqueued on `stream`; needs no context.
- * Replaces: planes 0..23 of Network::gather_features_policy
- * (Network.cpp:883-1046) and Network::gather_features_value
- * (Network.cpp:1048-1201), which run on the host. */
-LG_API int lg_gather_device(const int8_t *squares, const int8_t *to_move, int B, int which, int nplanes,
-                            uint8_t *planes, void *stream);
+ * Replaces: Network::gather_features_policy (Network.cpp:883-1046) and
+ * Network::gather_features_value (Network.cpp:1048-1201), which run on the
+ * host. */
+LG_API int lg_gather_device(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B,
+                            int which, int nplanes, uint8_t *planes, void *stream);
 
 /* Host-buffer policy / value evaluation from boards (same encoding as
- * lg_gather_device): copies 362 bytes a position to the device, gathers the
- * net's input planes there (the net must read at most 24 planes), then runs
- * the forward; results as lg_policy / lg_value.
+ * lg_gather_device): copies 362 bytes a position to the device (378 with
+ * moves), gathers the net's input planes there, then runs the forward;
+ * results as lg_policy / lg_value.  moves may be NULL when the net reads at
+ * most 24 planes.
  * Replaces: Network::get_scored_moves (Network.cpp:624-674) and
  * Network::get_value (Network.cpp:590-622) at the DIRECT rotation, gather
  * included. */
-LG_API int lg_policy_boards(lg_ctx *ctx, const int8_t *squares, const int8_t *to_move, int B,
-                            float temperature, float *probs, float *logits);
-LG_API int lg_value_boards(lg_ctx *ctx, const int8_t *squares, const int8_t *to_move, int B,
-                           float *value);
+LG_API int lg_policy_boards(lg_ctx *ctx, const int8_t *squares, const int8_t *to_move, const int32_t *moves,
+                            int B, float temperature, float *probs, float *logits);
+LG_API int lg_value_boards(lg_ctx *ctx, const int8_t *squares, const int8_t *to_move, const int32_t *moves,
+                           int B, float *value);
 
 /* 8-symmetry ensemble, device pointers, enqueued on `stream`: each of the B
  * positions (planes [B][c_in][361], unrotated) is evaluated under all 8

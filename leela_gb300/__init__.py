@@ -98,9 +98,9 @@ def library():
                                           ctypes.c_size_t, P(ctypes.c_size_t)]
             L.lg_value_avg8_device.argtypes = [vp, vp, i32, vp, vp]
             L.lg_profile_read.argtypes = [vp, i32, P(ctypes.c_longlong), P(ctypes.c_double)]
-            L.lg_gather_device.argtypes = [vp, vp, i32, i32, i32, vp, vp]
-            L.lg_policy_boards.argtypes = [vp, vp, vp, i32, f32, vp, vp]
-            L.lg_value_boards.argtypes = [vp, vp, vp, i32, vp]
+            L.lg_gather_device.argtypes = [vp, vp, vp, i32, i32, i32, vp, vp]
+            L.lg_policy_boards.argtypes = [vp, vp, vp, vp, i32, f32, vp, vp]
+            L.lg_value_boards.argtypes = [vp, vp, vp, vp, i32, vp]
             _lib = L
     return _lib
 
@@ -210,25 +210,27 @@ class Context:
         return out
 
     def policy_boards(self, squares, to_move, temperature: float = 1.0,
-                      return_logits: bool = False):
+                      return_logits: bool = False, moves=None):
         """lg_policy_boards: boards in (squares [B][361], 0 black / 1 white /
-        2 empty; to_move [B]), input planes gathered on the GPU."""
-        squares = np.ascontiguousarray(squares, dtype=np.int8).reshape(-1, POINTS)
+        2 empty; to_move [B]; moves [B][4] = last move, the move before it,
+        ko point (-1 none), white-has-komi flag, needed by nets reading
+        planes 24..31), input planes gathered on the GPU."""
+        squares, to_move, moves = _boards(squares, to_move, moves)
         B = squares.shape[0]
-        to_move = np.ascontiguousarray(np.broadcast_to(np.asarray(to_move, dtype=np.int8), (B,)))
         probs = np.empty((B, POINTS), dtype=np.float32)
         logits = np.empty((B, POINTS), dtype=np.float32) if return_logits else None
-        _check(library().lg_policy_boards(self._h, squares.ctypes.data, to_move.ctypes.data, B,
+        _check(library().lg_policy_boards(self._h, squares.ctypes.data, to_move.ctypes.data,
+                                          moves.ctypes.data if moves is not None else None, B,
                                           temperature, probs.ctypes.data,
                                           logits.ctypes.data if logits is not None else None))
         return (probs, logits) if return_logits else probs
 
-    def value_boards(self, squares, to_move):
-        squares = np.ascontiguousarray(squares, dtype=np.int8).reshape(-1, POINTS)
+    def value_boards(self, squares, to_move, moves=None):
+        squares, to_move, moves = _boards(squares, to_move, moves)
         B = squares.shape[0]
-        to_move = np.ascontiguousarray(np.broadcast_to(np.asarray(to_move, dtype=np.int8), (B,)))
         out = np.empty(B, dtype=np.float32)
-        _check(library().lg_value_boards(self._h, squares.ctypes.data, to_move.ctypes.data, B,
+        _check(library().lg_value_boards(self._h, squares.ctypes.data, to_move.ctypes.data,
+                                         moves.ctypes.data if moves is not None else None, B,
                                          out.ctypes.data))
         return out
 
@@ -327,12 +329,22 @@ REV_ROTATE = np.array([[rev_rotate_nn_idx(i, s) for i in range(POINTS)] for s in
                       dtype=np.int64)
 
 
+def _boards(squares, to_move, moves):
+    squares = np.ascontiguousarray(squares, dtype=np.int8).reshape(-1, POINTS)
+    B = squares.shape[0]
+    to_move = np.ascontiguousarray(np.broadcast_to(np.asarray(to_move, dtype=np.int8), (B,)))
+    if moves is not None:
+        moves = np.ascontiguousarray(moves, dtype=np.int32).reshape(B, 4)
+    return squares, to_move, moves
+
+
 def gather_device(squares_ptr: int, to_move_ptr: int, B: int, which: int, nplanes: int,
-                  planes_ptr: int, stream: int | None = None):
-    """lg_gather_device: input planes 0..nplanes-1 of the policy (which=0) or
-    value (which=1) set from boards, device pointers, on `stream`."""
-    _check(library().lg_gather_device(squares_ptr, to_move_ptr, B, which, nplanes, planes_ptr,
-                                      stream))
+                  planes_ptr: int, stream: int | None = None, moves_ptr: int | None = None):
+    """lg_gather_device: input planes 0..nplanes-1 (<= 32) of the policy
+    (which=0) or value (which=1) set from boards, device pointers, on
+    `stream`; moves_ptr ([B][4] int32) is needed for planes 24..31."""
+    _check(library().lg_gather_device(squares_ptr, to_move_ptr, moves_ptr, B, which, nplanes,
+                                      planes_ptr, stream))
 
 
 def rotate_planes(planes: np.ndarray, symmetry: int) -> np.ndarray:

@@ -2,13 +2,13 @@
 //
 // Reference: Network::gather_features_policy / gather_features_value
 // (Network.cpp:883-1046, 1048-1201) build 32 planes per position on the host
-// from FastBoard queries; planes 0..23 of both sets -- the ones the
-// benchmark nets read -- need only stone colours, the liberty count of each
-// string (FastBoard::count_rliberties, FastBoard.cpp:2482-2508) and, for
-// each empty point, the liberties of the string a stone of either colour
-// would form there after its captures, 0 for a suicide
-// (FastBoard::after_liberties, FastBoard.cpp:2511-2528).  Planes 24..31
-// (ladders, ko, move history, komi, third line) are not produced here.
+// from FastBoard queries: stone colours, the liberty count of each string
+// (FastBoard::count_rliberties, FastBoard.cpp:2482-2508), for each empty
+// point the liberties of the string a stone of either colour would form
+// there after its captures, 0 for a suicide (FastBoard::after_liberties,
+// FastBoard.cpp:2511-2528), the ladder reader's two planes (ladder.cuh), the
+// ko point, the last two moves, white's komi and the third line.  Planes
+// 0..23 -- the benchmark nets' inputs -- need only the board.
 //
 // One CTA per board, one thread per point.  Strings are labelled by
 // propagating the minimum point index over same-coloured neighbours; every
@@ -20,9 +20,17 @@
 // where the captured strings are the opponent strings next to p with one
 // liberty.
 //
+// Planes 24..31: the ladder reader runs only where it can answer "yes" --
+// an empty point with two empty neighbours next to an own string in atari
+// (ladder), or next to an opponent string of two liberties (ladder win) --
+// one thread per such point on a bitboard copy of the position.
+//
 // Input: squares [B][361] (0 black, 1 white, 2 empty; point y*19+x), to_move
-// [B] (0 black, 1 white).  Output: planes [B][nplanes][361] bytes (0/1).
+// [B] (0 black, 1 white), and for planes 24..31 moves [B][4] (last move, the
+// move before it, ko point: point indices, -1 none; white-has-komi flag).
+// Output: planes [B][nplanes][361] bytes (0/1).
 #include "lg_kernels.h"
+#include "ladder.cuh"
 
 namespace lg {
 
@@ -38,10 +46,15 @@ __device__ __forceinline__ int nbr(int p, int k) {
     }
 }
 
-template <int WHICH>  // 0 = policy planes, 1 = value planes
+// WHICH: 0 = policy planes, 1 = value planes; EXTRA: planes 24..31 wanted
+// (the ladder reader's registers and stack stay out of the 24-plane kernel)
+template <int WHICH, bool EXTRA>
 __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ squares,
-                                                     const int8_t *__restrict__ to_move, int B,
+                                                     const int8_t *__restrict__ to_move,
+                                                     const int32_t *__restrict__ moves, int B,
                                                      int nplanes, uint8_t *__restrict__ planes) {
+    __shared__ lad::Masks masks;
+    __shared__ lad::Board board;
     __shared__ int8_t sq[kPoints];
     __shared__ short lab[kPoints];
     __shared__ uint32_t stones[kPoints][kWords];
@@ -64,6 +77,19 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
         }
     }
     if (p < kWords) empty[p] = 0;
+    constexpr bool extra = EXTRA;
+    if (extra && p < 3 * kWords) {
+        // board, x != 0, x != 18 masks (bit q = point q)
+        const int kind = p / kWords, w = p % kWords;
+        uint32_t m = 0;
+        for (int j = 0; j < 32; ++j) {
+            const int q = w * 32 + j, x = q % kBoard;
+            const bool in = q < kPoints && (kind == 0 || (kind == 1 ? x != 0 : x != kBoard - 1));
+            m |= (uint32_t)in << j;
+        }
+        (kind == 0 ? masks.board : kind == 1 ? masks.notx0 : masks.notx18)[w] = m;
+    }
+    if (extra && p < 2 * kWords) board.c[p / kWords][p % kWords] = 0;
     __syncthreads();
     // string labels: minimum point index of the string
     for (int it = 0; it < 2 * kPoints; ++it) {
@@ -86,6 +112,7 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
         if (c == 2) {
             atomicOr(&empty[p >> 5], 1u << (p & 31));
         } else {
+            if (extra && (c == 0 || c == 1)) atomicOr(&board.c[c][p >> 5], 1u << (p & 31));
             const int r = lab[p];
             atomicOr(&stones[r][p >> 5], 1u << (p & 31));
             for (int k = 0; k < 4; ++k) {
@@ -103,15 +130,26 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
     __syncthreads();
     if (!on) return;
     uint32_t bits = 0;  // bit i = plane i at this point
+    // policy: own libs 1,2,3,4,5+ at 3..7, opponent's at 8..12, after-move
+    // 1..5,6+ at 13..18, opponent's after-move 1..5,6+ at 19..24, ladder 25,
+    // ladder win 26, ko 27, last move 28, the move before 29, white's komi 30,
+    // third line 31.  value: libs 1..5,6+ at 3..8 / 9..14, after-move 1..5,6+
+    // at 15..20 / 21..26, ladder 27, ladder win 28, komi 29, third line 30,
+    // ko 31.
+    constexpr int kLibCap = WHICH == 0 ? 5 : 6, kOppLib0 = WHICH == 0 ? 8 : 9;
+    constexpr int kAfter0 = WHICH == 0 ? 13 : 15, kOAfter0 = WHICH == 0 ? 19 : 21;
+    constexpr int kLadder = WHICH == 0 ? 25 : 27, kWin = WHICH == 0 ? 26 : 28;
+    constexpr int kKomi = WHICH == 0 ? 30 : 29, kLine3 = WHICH == 0 ? 31 : 30, kKo = WHICH == 0 ? 27 : 31;
+    {
+        const int x = p % kBoard, y = p / kBoard;
+        if (x == 2 || x == 16 || y == 2 || y == 16) bits |= 1u << kLine3;
+    }
     if (c != 2) {
         const bool mine = c == tomove;
         bits |= mine ? 2u : 4u;
+        if (extra && c == 1 && moves[(size_t)b * 4 + 3]) bits |= 1u << kKomi;
         const int l = libs[lab[p]];
-        if (WHICH == 0) {  // policy: 1, 2, 3, 4, 5+ ; own at 3.., opponent at 8..
-            if (l >= 1) bits |= 1u << ((mine ? 3 : 8) + (l >= 5 ? 4 : l - 1));
-        } else {           // value: 1, 2, 3, 4, 5, 6+ ; own at 3.., opponent at 9..
-            if (l >= 1) bits |= 1u << ((mine ? 3 : 9) + (l >= 6 ? 5 : l - 1));
-        }
+        if (l >= 1) bits |= 1u << ((mine ? 3 : kOppLib0) + (l >= kLibCap ? kLibCap : l) - 1);
     } else {
         bits |= 1u;
         int nb[4];
@@ -151,41 +189,69 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
             after[side] = n;
         }
         const int al = after[0], at = after[1];
-        if (WHICH == 0) {  // after 1..6+ at 13..18, opponent 1..5 at 19..23
-            if (al >= 1) bits |= 1u << (13 + (al >= 6 ? 5 : al - 1));
-            if (at >= 1 && at <= 5) bits |= 1u << (19 + at - 1);
-        } else {           // after 1..6+ at 15..20, opponent 1..3 at 21..23
-            if (al >= 1) bits |= 1u << (15 + (al >= 6 ? 5 : al - 1));
-            if (at >= 1 && at <= 3) bits |= 1u << (21 + at - 1);
+        if (al >= 1) bits |= 1u << (kAfter0 + (al >= 6 ? 5 : al - 1));
+        if (at >= 1) bits |= 1u << (kOAfter0 + (at >= 6 ? 5 : at - 1));
+        if (extra && (tomove == 0 || tomove == 1)) {
+            int n_empty = 0;
+            bool own_atari = false, opp_two = false;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int q = nb[k];
+                if (q < 0) continue;
+                const int cq = sq[q];
+                if (cq == 2) {
+                    ++n_empty;
+                } else if (cq == 0 || cq == 1) {
+                    const int lq = libs[lab[q]];
+                    own_atari |= cq == tomove && lq == 1;
+                    opp_two |= cq != tomove && lq == 2;
+                }
+            }
+            // ladder: two empty neighbours, an own string in atari next to it
+            // (its saving move then is no self-atari)
+            if (n_empty == 2 && own_atari && lad::losing_ladder(board, tomove, p, masks)) bits |= 1u << kLadder;
+            if (opp_two && lad::winning_ladder(board, tomove, p, masks)) bits |= 1u << kWin;
         }
+    }
+    if (extra) {
+        const int32_t *mv = moves + (size_t)b * 4;
+        if (WHICH == 0 && mv[0] == p) bits |= 1u << 28;
+        if (WHICH == 0 && mv[0] >= 0 && mv[1] == p) bits |= 1u << 29;
+        if (mv[2] == p) bits |= 1u << kKo;
     }
     uint8_t *dst = planes + (size_t)b * nplanes * kPoints + p;
     for (int i = 0; i < nplanes; ++i) dst[(size_t)i * kPoints] = (uint8_t)((bits >> i) & 1u);
 }
 
-int launch_gather(const int8_t *squares, const int8_t *to_move, int B, int which, int nplanes,
-                  uint8_t *planes, cudaStream_t s) {
-    if (B < 0 || nplanes < 1 || nplanes > kGatherPlanes || (which != 0 && which != 1)) {
-        lg_set_error("gather: planes 0..23 of the policy (0) or value (1) set only");
+int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
+                  int nplanes, uint8_t *planes, cudaStream_t s) {
+    if (B < 0 || nplanes < 1 || nplanes > kGatherPlanes || (which != 0 && which != 1) ||
+        (nplanes > 24 && !moves && B > 0)) {
+        lg_set_error("gather: planes 0..31 of the policy (0) or value (1) set; planes 24..31 need moves");
         return LG_ERR_ARG;
     }
     if (B == 0) return LG_OK;
-    if (which == 0)
-        gather_kernel<0><<<B, 384, 0, s>>>(squares, to_move, B, nplanes, planes);
+    const bool extra = nplanes > 24;
+    if (which == 0 && extra)
+        gather_kernel<0, true><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes);
+    else if (which == 0)
+        gather_kernel<0, false><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes);
+    else if (extra)
+        gather_kernel<1, true><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes);
     else
-        gather_kernel<1><<<B, 384, 0, s>>>(squares, to_move, B, nplanes, planes);
+        gather_kernel<1, false><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes);
     return LG_OK;
 }
 
 }  // namespace lg
 
-extern "C" int lg_gather_device(const int8_t *squares, const int8_t *to_move, int B, int which, int nplanes,
-                                uint8_t *planes, void *stream) {
+extern "C" int lg_gather_device(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B,
+                                int which, int nplanes, uint8_t *planes, void *stream) {
     if ((!squares || !to_move || !planes) && B > 0) {
         lg_set_error("lg_gather_device: bad arguments");
         return LG_ERR_ARG;
     }
-    int rc = lg::launch_gather(squares, to_move, B, which, nplanes, planes, (cudaStream_t)stream);
+    int rc = lg::launch_gather(squares, to_move, moves, B, which, nplanes, planes, (cudaStream_t)stream);
     if (rc) return rc;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -122,7 +122,8 @@ struct lg_ctx {
     int *d_err = nullptr;
     // shared
     uint8_t *d_planes = nullptr;
-    int8_t *d_boards = nullptr;  // board-input calls: squares [B][361], then to_move [B]
+    // board-input calls: squares [B][361], to_move [B], then (4-aligned) moves [B][4] int32
+    int8_t *d_boards = nullptr;
     float *d_logits = nullptr, *d_probs = nullptr, *d_value = nullptr;
     float *d_parts = nullptr;  // fused-head partial sums, [4][max_batch * 361]
     float *d_fcpart = nullptr; // value-head FC partial sums
@@ -548,12 +549,13 @@ int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *pr
 // graph of copy-in + forward + copy-out (one graph per chunk size and
 // staging slot).  Two pinned slots alternate, so the host packs chunk k+1
 // while the GPU runs chunk k; chunk k-2's results are handed back first.
-// With `squares` / `to_move` instead of planes, each chunk copies in the
-// boards (362 bytes a position) and the graph gathers the input planes on
+// With `squares` / `to_move` (and `moves` for nets reading planes 24..31)
+// instead of planes, each chunk copies in the boards (362 bytes a position,
+// 16 more with moves) and the graph gathers the input planes on
 // the GPU before the forward.
 int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
              float *logits, float *value, const int8_t *squares = nullptr,
-             const int8_t *to_move = nullptr) {
+             const int8_t *to_move = nullptr, const int32_t *moves = nullptr) {
     Net &n = c->nets[net];
     if (!n.present) {
         lg_set_error("net %d was not created", net);
@@ -567,6 +569,11 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
     if (boards && (n.d.c_in > kGatherPlanes || c->planes_c < 2)) {
         lg_set_error("board input gathers planes 0..%d; the net reads %d planes", kGatherPlanes - 1,
                      n.d.c_in);
+        return LG_ERR_ARG;
+    }
+    const bool with_moves = boards && n.d.c_in > 24;
+    if (with_moves && !moves && B > 0) {
+        lg_set_error("the net reads planes 24..31 (ladders, ko, last moves, komi): moves are needed");
         return LG_ERR_ARG;
     }
     int rc = check_fault(c);
@@ -611,10 +618,14 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
             finish(slot ^ 1);
             return rc;
         }
-        const size_t in_bytes = boards ? (size_t)nb * (kPoints + 1) : (size_t)nb * per_in;
+        // boards: squares, to_move, then the moves at a 4-byte boundary
+        const size_t mv_off = ((size_t)nb * (kPoints + 1) + 3) & ~(size_t)3;
+        const size_t in_bytes = !boards ? (size_t)nb * per_in
+                                        : (with_moves ? mv_off + (size_t)nb * 16 : (size_t)nb * (kPoints + 1));
         if (boards) {
             std::memcpy(hp[slot], squares + (size_t)b0 * kPoints, (size_t)nb * kPoints);
             std::memcpy(hp[slot] + (size_t)nb * kPoints, to_move + b0, (size_t)nb);
+            if (with_moves) std::memcpy(hp[slot] + mv_off, moves + (size_t)b0 * 4, (size_t)nb * 16);
         } else {
             std::memcpy(hp[slot], planes + (size_t)b0 * per_in, in_bytes);
         }
@@ -627,7 +638,8 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
             int nl = 0;
             if (boards) {
                 cudaMemcpyAsync(c->d_boards, hp[slot], in_bytes, cudaMemcpyHostToDevice, c->stream);
-                rc = launch_gather(c->d_boards, c->d_boards + (size_t)nb * kPoints, nb,
+                rc = launch_gather(c->d_boards, c->d_boards + (size_t)nb * kPoints,
+                                   with_moves ? reinterpret_cast<const int32_t *>(c->d_boards + mv_off) : nullptr, nb,
                                    net == LG_NET_POLICY ? 0 : 1, n.d.c_in, c->d_planes, c->stream);
                 nl = 1;
             } else {
@@ -987,7 +999,7 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
     }
     c->planes_c = max_c_in;
     if ((rc = dev_alloc(c, &c->d_planes, mb * max_c_in * kPoints)) ||
-        (rc = dev_alloc(c, &c->d_boards, mb * (kPoints + 1))) ||
+        (rc = dev_alloc(c, &c->d_boards, mb * 384)) ||
         (rc = dev_alloc(c, &c->d_logits, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_probs, mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)) ||
@@ -1042,24 +1054,24 @@ extern "C" int lg_value(lg_ctx *c, const uint8_t *planes, int B, float *value) {
     return run_host(c, LG_NET_VALUE, planes, B, 1.0f, nullptr, nullptr, value);
 }
 
-extern "C" int lg_policy_boards(lg_ctx *c, const int8_t *squares, const int8_t *to_move, int B,
-                                float temperature, float *probs, float *logits) {
+extern "C" int lg_policy_boards(lg_ctx *c, const int8_t *squares, const int8_t *to_move, const int32_t *moves,
+                                int B, float temperature, float *probs, float *logits) {
     if (!c || !probs || !(temperature > 0.0f) || (B > 0 && (!squares || !to_move))) {
         lg_set_error("lg_policy_boards: bad arguments");
         return LG_ERR_ARG;
     }
     std::lock_guard<std::mutex> g(c->mu);
-    return run_host(c, LG_NET_POLICY, nullptr, B, temperature, probs, logits, nullptr, squares, to_move);
+    return run_host(c, LG_NET_POLICY, nullptr, B, temperature, probs, logits, nullptr, squares, to_move, moves);
 }
 
-extern "C" int lg_value_boards(lg_ctx *c, const int8_t *squares, const int8_t *to_move, int B,
-                               float *value) {
+extern "C" int lg_value_boards(lg_ctx *c, const int8_t *squares, const int8_t *to_move, const int32_t *moves,
+                               int B, float *value) {
     if (!c || !value || (B > 0 && (!squares || !to_move))) {
         lg_set_error("lg_value_boards: bad arguments");
         return LG_ERR_ARG;
     }
     std::lock_guard<std::mutex> g(c->mu);
-    return run_host(c, LG_NET_VALUE, nullptr, B, 1.0f, nullptr, nullptr, value, squares, to_move);
+    return run_host(c, LG_NET_VALUE, nullptr, B, 1.0f, nullptr, nullptr, value, squares, to_move, moves);
 }
 
 extern "C" int lg_policy_device(lg_ctx *c, const uint8_t *planes, int B, float temperature,

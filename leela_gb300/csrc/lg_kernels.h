@@ -58,10 +58,12 @@ struct TcLayer {
 
 // Input planes 0..nplanes-1 (nplanes <= kGatherPlanes) of the policy
 // (which = 0) or value (which = 1) set from boards: squares [B][361]
-// (0 black, 1 white, 2 empty), to_move [B]; planes [B][nplanes][361].
-constexpr int kGatherPlanes = 24;
-int launch_gather(const int8_t *squares, const int8_t *to_move, int B, int which, int nplanes,
-                  uint8_t *planes, cudaStream_t s);
+// (0 black, 1 white, 2 empty), to_move [B], moves [B][4] (last move, the
+// move before it, ko point, white-has-komi flag; needed for planes 24..31);
+// planes [B][nplanes][361].
+constexpr int kGatherPlanes = 32;
+int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
+                  int nplanes, uint8_t *planes, cudaStream_t s);
 
 // Expanded 5x5 input: planes [B][C][361] bytes -> L5 BF16 rows with
 // halves*64 channels: channel dx*C + c = plane c at (y, x + dx - 2).

@@ -598,8 +598,227 @@ static int gb_after(const int8_t *sq, int color, int p) {
     return gb_libs(b, p);
 }
 
-void or_gather_planes(const int8_t *squares, int to_move, int which, uint8_t *planes) {
-    memset(planes, 0, 24 * OR_POINTS);
+/* ---- ladder reader (FastBoard.cpp:1273-1292, 1342-1470, 2429-2442,
+ * 2530-2564, 2647-2837), on a plain board: string liberties are exact
+ * counts, as the reference's incrementally kept m_libs are. */
+
+static int gb_count_empty(const int8_t *b, int v) {
+    int nb[4], m = gb_nbrs(v, nb), n = 0;
+    for (int k = 0; k < m; ++k) n += b[nb[k]] == GB_EMPTY;
+    return n;
+}
+
+static int gb_size(const int8_t *b, int q) {
+    uint8_t in[OR_POINTS];
+    int list[OR_POINTS], n;
+    memset(in, 0, sizeof in);
+    gb_string(b, q, in, list, &n);
+    return n;
+}
+
+/* Up to `want` distinct liberties of the string through q, into out[];
+ * returns how many were found. */
+static int gb_liberties(const int8_t *b, int q, int want, int *out) {
+    uint8_t in[OR_POINTS];
+    int list[OR_POINTS], n, cnt = 0;
+    memset(in, 0, sizeof in);
+    gb_string(b, q, in, list, &n);
+    for (int i = 0; i < n && cnt < want; ++i) {
+        int nb[4], m = gb_nbrs(list[i], nb);
+        for (int k = 0; k < m && cnt < want; ++k) {
+            int r = nb[k], dup = 0;
+            if (b[r] != GB_EMPTY) continue;
+            for (int j = 0; j < cnt; ++j) dup |= out[j] == r;
+            if (!dup) out[cnt++] = r;
+        }
+    }
+    return cnt;
+}
+
+static void gb_remove_string(int8_t *b, int q) {
+    uint8_t in[OR_POINTS];
+    int list[OR_POINTS], n;
+    memset(in, 0, sizeof in);
+    gb_string(b, q, in, list, &n);
+    for (int i = 0; i < n; ++i) b[list[i]] = GB_EMPTY;
+}
+
+/* FastBoard::update_board_fast: place, capture opponent strings left without
+ * liberties, remove the new string if it has none. */
+static void gb_play(int8_t *b, int color, int v) {
+    int nb[4], m = gb_nbrs(v, nb);
+    b[v] = (int8_t)color;
+    for (int k = 0; k < m; ++k)
+        if (b[nb[k]] == 1 - color && gb_libs(b, nb[k]) == 0) gb_remove_string(b, nb[k]);
+    if (gb_libs(b, v) == 0) gb_remove_string(b, v);
+}
+
+/* FastBoard::minimum_elib_count: fewest liberties among the opponent strings
+ * next to the point v itself (100 if none). */
+static int gb_min_elib(const int8_t *b, int color, int v) {
+    int nb[4], m = gb_nbrs(v, nb), best = 100;
+    for (int k = 0; k < m; ++k)
+        if (b[nb[k]] == 1 - color) {
+            int l = gb_libs(b, nb[k]);
+            if (l < best) best = l;
+        }
+    return best;
+}
+
+/* FastBoard::is_suicide: no empty neighbour, every own neighbour string in
+ * atari (its liberty is v), no opponent neighbour string in atari. */
+static int gb_is_suicide(const int8_t *b, int v, int color) {
+    if (gb_count_empty(b, v) > 0) return 0;
+    int nb[4], m = gb_nbrs(v, nb);
+    for (int k = 0; k < m; ++k) {
+        int l = gb_libs(b, nb[k]);
+        if (b[nb[k]] == color ? l > 1 : l <= 1) return 0;
+    }
+    return 1;
+}
+
+/* FastBoard::self_atari: fewer than two empty neighbours, no capture and no
+ * connection to a string of 3+ liberties, and v, the empty neighbours and
+ * the liberties of the own neighbour strings (those with 2+ liberties)
+ * number at most two. */
+static int gb_self_atari(const int8_t *b, int color, int v) {
+    if (gb_count_empty(b, v) >= 2) return 0;
+    int nb[4], m = gb_nbrs(v, nb);
+    for (int k = 0; k < m; ++k) {
+        int c = b[nb[k]];
+        if (c == GB_EMPTY) continue;
+        int l = gb_libs(b, nb[k]);
+        if ((c == 1 - color && l <= 1) || (c == color && l >= 3)) return 0;
+    }
+    int set[8], cnt = 0;
+    set[cnt++] = v;
+    for (int k = 0; k < m; ++k) {
+        int r = nb[k];
+        if (b[r] == GB_EMPTY) {
+            int dup = 0;
+            for (int j = 0; j < cnt; ++j) dup |= set[j] == r;
+            if (!dup) set[cnt++] = r;
+        } else if (b[r] == color && gb_libs(b, r) > 1) {
+            int libs[4], nl = gb_liberties(b, r, 4, libs);
+            for (int i = 0; i < nl; ++i) {
+                int dup = 0;
+                for (int j = 0; j < cnt; ++j) dup |= set[j] == libs[i];
+                if (!dup && cnt < 8) set[cnt++] = libs[i];
+            }
+        }
+        if (cnt > 2) return 0;
+    }
+    return 1;
+}
+
+/* FastBoard::saving_size: the size of an own neighbour string in atari whose
+ * saving move (its liberty) is not a self-atari, else 0. */
+static int gb_saving_size(const int8_t *b, int color, int v) {
+    int nb[4], m = gb_nbrs(v, nb);
+    for (int k = 0; k < m; ++k) {
+        if (b[nb[k]] != color || gb_libs(b, nb[k]) > 1) continue;
+        int lib;
+        if (gb_liberties(b, nb[k], 1, &lib) == 1 && !gb_self_atari(b, color, lib)) return gb_size(b, nb[k]);
+    }
+    return 0;
+}
+
+/* FastBoard::check_losing_ladder: `color` (to move) saves the string in
+ * atari next to vtx by playing there; true when the attacker can keep it in
+ * atari until it dies. */
+static int gb_losing_ladder(const int8_t *board, int color, int vtx, int branching) {
+    if (branching > 5) return 0;
+    int elib = gb_min_elib(board, color, vtx);
+    if (elib == 0 || elib == 1) return 0;
+    /* the own strings in atari next to vtx: exactly one, and it cannot
+     * capture an attacker */
+    int nb[4], m = gb_nbrs(vtx, nb), crit = -1, ncrit = 0;
+    uint8_t in_crit[OR_POINTS];
+    memset(in_crit, 0, sizeof in_crit);
+    for (int k = 0; k < m; ++k) {
+        int r = nb[k];
+        if (board[r] != color || gb_libs(board, r) > 1) continue;
+        if (!in_crit[r]) {
+            int list[OR_POINTS], n;
+            gb_string(board, r, in_crit, list, &n);
+            ++ncrit;
+            crit = r;
+        }
+    }
+    if (ncrit != 1) return 0;
+    {
+        uint8_t in[OR_POINTS];
+        int list[OR_POINTS], n;
+        memset(in, 0, sizeof in);
+        gb_string(board, crit, in, list, &n);
+        for (int i = 0; i < n; ++i) {
+            int nb2[4], m2 = gb_nbrs(list[i], nb2);
+            for (int k = 0; k < m2; ++k)
+                if (board[nb2[k]] == 1 - color && gb_libs(board, nb2[k]) <= 1) return 0;
+        }
+    }
+    int8_t b[OR_POINTS];
+    memcpy(b, board, sizeof b);
+    int atari = vtx;
+    gb_play(b, color, vtx);
+    for (;;) {
+        if (b[atari] == GB_EMPTY) return 1;           /* the escape was a suicide */
+        int nl = gb_libs(b, atari);
+        if (nl == 1) return 1;                          /* self-atari */
+        if (nl >= 3) return 0;                          /* escaped */
+        if (gb_min_elib(b, color, atari) == 1) return 0; /* counter-atari */
+        int lib[2];
+        gb_liberties(b, atari, 2, lib);
+        if (gb_count_empty(b, lib[0]) == 3 && gb_count_empty(b, lib[1]) == 3) return 0;
+        int l0 = gb_after(b, color, lib[0]), l1 = gb_after(b, color, lib[1]);
+        int s0 = gb_is_suicide(b, lib[0], 1 - color) || gb_self_atari(b, 1 - color, lib[0]);
+        int s1 = gb_is_suicide(b, lib[1], 1 - color) || gb_self_atari(b, 1 - color, lib[1]);
+        if (s0 && s1) return 0;
+        if (s0) l1 = l0 + 1;
+        if (s1) l0 = l1 + 1;
+        if (l0 == l1) {
+            int8_t b2[OR_POINTS];
+            memcpy(b2, b, sizeof b2);
+            gb_play(b2, 1 - color, lib[0]);
+            int r1 = gb_losing_ladder(b2, color, lib[1], branching + 1);
+            memcpy(b2, b, sizeof b2);
+            gb_play(b2, 1 - color, lib[1]);
+            int r2 = gb_losing_ladder(b2, color, lib[0], branching + 1);
+            return r1 || r2;
+        }
+        gb_play(b, 1 - color, l0 > l1 ? lib[0] : lib[1]);
+        /* the attacker's stone stands (neither suicide nor self-atari was
+         * chosen) and captures no stone next to the saved string, so the
+         * string has exactly one liberty: the next saving move */
+        int next;
+        if (gb_liberties(b, atari, 2, lib) != 1) return 0;
+        next = lib[0];
+        gb_play(b, color, next);
+        atari = next;
+    }
+}
+
+/* FastBoard::check_winning_ladder: playing vtx puts an opponent string of
+ * two liberties in atari and its escape (with two empty neighbours) loses. */
+static int gb_winning_ladder(const int8_t *board, int color, int vtx) {
+    int nb[4], m = gb_nbrs(vtx, nb);
+    for (int k = 0; k < m; ++k) {
+        int r = nb[k];
+        if (board[r] != 1 - color || gb_libs(board, r) != 2) continue;
+        if (gb_self_atari(board, color, vtx)) continue;
+        int8_t b[OR_POINTS];
+        memcpy(b, board, sizeof b);
+        gb_play(b, color, vtx);
+        int esc;
+        if (gb_liberties(b, r, 2, &esc) < 1) continue;
+        if (gb_count_empty(b, esc) == 2 && gb_losing_ladder(b, 1 - color, esc, 0)) return 1;
+    }
+    return 0;
+}
+
+void or_gather_planes(const int8_t *squares, int to_move, const int32_t *moves, int which, int nplanes,
+                      uint8_t *planes) {
+    memset(planes, 0, (size_t)nplanes * OR_POINTS);
     int libs_of[OR_POINTS];
     uint8_t done[OR_POINTS];
     memset(done, 0, sizeof done);
@@ -612,32 +831,50 @@ void or_gather_planes(const int8_t *squares, int to_move, int which, uint8_t *pl
         for (int i = 0; i < n; ++i) { libs_of[list[i]] = l; done[list[i]] = 1; }
     }
     /* policy: own libs 1,2,3,4,5+ at 3..7, opponent's at 8..12, after-move
-     * 1..5,6+ at 13..18, opponent's after-move 1..5 at 19..23 (6+ is plane
-     * 24).  value: libs 1..5,6+ at 3..8 / 9..14, after-move 1..5,6+ at
-     * 15..20, opponent's 1..3 at 21..23 (4.. are planes 24..26). */
+     * 1..5,6+ at 13..18, opponent's after-move 1..5,6+ at 19..24, ladder 25,
+     * ladder win 26, ko 27, last move 28, the move before 29, white stones
+     * when white has komi 30, third line 31.  value: libs 1..5,6+ at 3..8 /
+     * 9..14, after-move 1..5,6+ at 15..20 / 21..26, ladder 27, ladder win 28,
+     * komi 29, third line 30, ko 31. */
     const int lib_cap = which == 0 ? 5 : 6;
     const int opp_lib0 = which == 0 ? 8 : 9;
     const int after0 = which == 0 ? 13 : 15;
     const int oafter0 = which == 0 ? 19 : 21;
-    const int oafter_max = which == 0 ? 5 : 3;
+    const int p_ladder = which == 0 ? 25 : 27, p_win = which == 0 ? 26 : 28;
+    const int p_komi = which == 0 ? 30 : 29, p_line3 = which == 0 ? 31 : 30;
+    const int p_ko = which == 0 ? 27 : 31;
+#define SETP(plane, p) do { if ((plane) < nplanes) planes[(size_t)(plane) * OR_POINTS + (p)] = 1; } while (0)
     for (int p = 0; p < OR_POINTS; ++p) {
-        int c = squares[p];
+        int c = squares[p], x = p % 19, y = p / 19;
+        if (x == 2 || x == 16 || y == 2 || y == 16) SETP(p_line3, p);
         if (c != GB_EMPTY) {
             int mine = c == to_move;
-            planes[(mine ? 1 : 2) * OR_POINTS + p] = 1;
+            if (c == 1 && moves && moves[3]) SETP(p_komi, p);
+            SETP(mine ? 1 : 2, p);
             int l = libs_of[p];
-            if (l >= 1) {
-                int idx = (l >= lib_cap ? lib_cap : l) - 1;
-                planes[((mine ? 3 : opp_lib0) + idx) * OR_POINTS + p] = 1;
-            }
+            if (l >= 1) SETP((mine ? 3 : opp_lib0) + (l >= lib_cap ? lib_cap : l) - 1, p);
         } else {
-            planes[p] = 1;
+            SETP(0, p);
             int al = gb_after(squares, to_move, p);
             int at = gb_after(squares, 1 - to_move, p);
-            if (al >= 1) planes[(after0 + (al >= 6 ? 5 : al - 1)) * OR_POINTS + p] = 1;
-            if (at >= 1 && at <= oafter_max) planes[(oafter0 + at - 1) * OR_POINTS + p] = 1;
+            if (al >= 1) SETP(after0 + (al >= 6 ? 5 : al - 1), p);
+            if (at >= 1) SETP(oafter0 + (at >= 6 ? 5 : at - 1), p);
+            if (nplanes > 24) {
+                if (gb_count_empty(squares, p) == 2 && gb_saving_size(squares, to_move, p) > 0 &&
+                    gb_losing_ladder(squares, to_move, p, 0))
+                    SETP(p_ladder, p);
+                if (gb_winning_ladder(squares, to_move, p)) SETP(p_win, p);
+            }
         }
     }
+    if (moves) {
+        if (moves[0] >= 0 && which == 0) {
+            SETP(28, moves[0]);
+            if (moves[1] >= 0) SETP(29, moves[1]);
+        }
+        if (moves[2] >= 0) SETP(p_ko, moves[2]);
+    }
+#undef SETP
 }
 
 int or_random_board(uint64_t seed, int k, int8_t *squares) {

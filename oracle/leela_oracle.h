@@ -125,14 +125,19 @@ double or_time_pair_f32(const or_net *pol, const float *wp, const or_net *val, c
                         const uint8_t *planes_p, const uint8_t *planes_v, int npos, int iters,
                         int nthreads);
 
-/* Input planes 0..23 of the policy (which = 0) or value (which = 1) set,
- * restating Network::gather_features_policy / gather_features_value
- * (Network.cpp:883-1046, 1048-1201) for the planes that need no ladder
- * reader: colours, string liberties (FastBoard::count_rliberties,
- * FastBoard.cpp:2482-2508) and after-move liberties of both colours
- * (FastBoard::after_liberties, FastBoard.cpp:2511-2528; 0 for a suicide).
- * squares[361]: 0 black, 1 white, 2 empty, point y*19+x; planes[24][361]. */
-void or_gather_planes(const int8_t *squares, int to_move, int which, uint8_t *planes);
+/* Input planes 0..nplanes-1 (nplanes <= 32) of the policy (which = 0) or
+ * value (which = 1) set, restating Network::gather_features_policy /
+ * gather_features_value (Network.cpp:883-1046, 1048-1201): colours, string
+ * liberties (FastBoard::count_rliberties, FastBoard.cpp:2482-2508),
+ * after-move liberties of both colours (FastBoard::after_liberties,
+ * FastBoard.cpp:2511-2528; 0 for a suicide), the ladder reader's planes
+ * (FastBoard::saving_size / check_losing_ladder / check_winning_ladder,
+ * FastBoard.cpp:1273-1292, 2530-2837), ko point, last two moves, komi and
+ * third line.  squares[361]: 0 black, 1 white, 2 empty, point y*19+x;
+ * moves[4] (may be NULL when nplanes <= 24): last move, the move before it,
+ * ko point (point index, -1 none), white-has-komi flag; planes[nplanes][361]. */
+void or_gather_planes(const int8_t *squares, int to_move, const int32_t *moves, int which, int nplanes,
+                      uint8_t *planes);
 
 /* A board reached by k uniformly random legal moves from the empty board
  * (captures applied, suicide excluded, simple ko ignored), for parity cases

@@ -114,8 +114,8 @@ def lib():
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int]
             L.or_time_pair_f32.restype = ctypes.c_double
-            L.or_gather_planes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
-                                           ctypes.c_void_p]
+            L.or_gather_planes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_void_p]
             L.or_random_board.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]
             _lib = L
     return _lib
@@ -230,17 +230,22 @@ def rotate_planes(planes: np.ndarray, sym: int) -> np.ndarray:
     return out
 
 
-def gather_planes(squares: np.ndarray, to_move, which: int) -> np.ndarray:
-    """Planes 0..23 of the policy (which=0) or value (which=1) input set for
-    boards squares [B][361] (0 black, 1 white, 2 empty) -> [B][24][361] u8.
-    Restates Network::gather_features_policy / gather_features_value
-    (Network.cpp:883-1201) for the planes without ladders."""
+def gather_planes(squares: np.ndarray, to_move, which: int, nplanes: int = 24,
+                  moves: np.ndarray | None = None) -> np.ndarray:
+    """Planes 0..nplanes-1 (nplanes <= 32) of the policy (which=0) or value
+    (which=1) input set for boards squares [B][361] (0 black, 1 white,
+    2 empty) -> [B][nplanes][361] u8.  moves [B][4] (last move, the move
+    before it, ko point, white-has-komi flag; point indices, -1 none) is
+    needed for planes 24..31.  Restates Network::gather_features_policy /
+    gather_features_value (Network.cpp:883-1201)."""
     sq = np.ascontiguousarray(squares, dtype=np.int8).reshape(-1, POINTS)
     tm = np.broadcast_to(np.asarray(to_move, dtype=np.int64), (sq.shape[0],))
-    out = np.empty((sq.shape[0], 24, POINTS), dtype=np.uint8)
+    mv = None if moves is None else np.ascontiguousarray(moves, dtype=np.int32).reshape(-1, 4)
+    out = np.empty((sq.shape[0], nplanes, POINTS), dtype=np.uint8)
     L = lib()
     for b in range(sq.shape[0]):
-        L.or_gather_planes(_ptr(sq[b]), int(tm[b]), which, _ptr(out[b]))
+        L.or_gather_planes(_ptr(sq[b]), int(tm[b]), None if mv is None else _ptr(mv[b]), which, nplanes,
+                           _ptr(out[b]))
     return out
 
 

@@ -272,6 +272,13 @@ int cmd_gen(int n, int seed, const std::string &out) {
     PositionStream ps(seed);
     FILE *fp = open_out(out, ".planes_p"), *fv = open_out(out, ".planes_v");
     FILE *fs = open_out(out, ".squares"), *fm = open_out(out, ".meta");
+    FILE *fmv = open_out(out, ".moves");
+    // a board vertex as a point index y*19+x, -1 for none (vertex <= 0)
+    auto point_of = [](GameState &g, int v) -> int32_t {
+        if (v <= 0) return -1;
+        std::pair<int, int> xy = g.board.get_xy(v);
+        return xy.second * 19 + xy.first;
+    };
     for (int i = 0; i < n; ++i) {
         int k;
         GameState g = ps.next(&k);
@@ -289,8 +296,13 @@ int cmd_gen(int n, int seed, const std::string &out) {
         std::fwrite(sq, 1, 361, fs);
         int32_t meta[4] = {g.get_to_move(), (int32_t)g.get_movenum(), k, g.get_komove()};
         std::fwrite(meta, sizeof(int32_t), 4, fm);
+        // what the gather reads besides the board: last move, the move before
+        // it, the ko point, and whether white has komi (|komi| > 0.75)
+        int32_t mv[4] = {point_of(g, g.get_last_move()), point_of(g, g.get_prevlast_move()),
+                         point_of(g, g.get_komove()), std::fabs(g.get_komi()) > 0.75f ? 1 : 0};
+        std::fwrite(mv, sizeof(int32_t), 4, fmv);
     }
-    std::fclose(fp); std::fclose(fv); std::fclose(fs); std::fclose(fm);
+    std::fclose(fp); std::fclose(fv); std::fclose(fs); std::fclose(fm); std::fclose(fmv);
     return 0;
 }
 

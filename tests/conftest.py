@@ -24,7 +24,7 @@ def unpack_planes(packed):
 def positions():
     d = np.load(os.path.join(GOLDEN, "positions_s0.npz"))
     return {"planes_p": unpack_planes(d["planes_p"]), "planes_v": unpack_planes(d["planes_v"]),
-            "squares": d["squares"], "meta": d["meta"]}
+            "squares": d["squares"], "meta": d["meta"], "moves": d["moves"]}
 
 
 @pytest.fixture(scope="session")

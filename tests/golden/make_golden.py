@@ -13,6 +13,8 @@ own code for:
                        uniform legal moves, seed 0): the 32 policy and 32 value
                        planes from the reference gather (Network.cpp:883-1201),
                        bit-packed; board squares; to-move/move number/k/ko point
+                       (meta); last move, previous move, ko point as point
+                       indices (-1 none) and the white-has-komi flag (moves)
   refexact_s0.npz      reference-shaped nets (Network.cpp:783-807, 709-737;
                        ELU, 3x3 heads): get_scored_moves(DIRECT, rot) probs
                        scattered to board order, the raw head output of the
@@ -26,7 +28,10 @@ own code for:
                        confirm another host draws the same weights
   mcowner_s0.npz       Playout::mc_owner(state, 64) for all 1024 positions (the
                        win rate of the side to move; the distilled net's value
-                       labels)
+                       labels).  The reference's playouts draw from per-thread
+                       random streams, so a rerun with another thread schedule
+                       gives other (equally valid) labels; the committed file
+                       is the one the distillation tests were calibrated on.
 
 The fixtures need nothing from the reference at test time.
 """
@@ -92,9 +97,10 @@ def main():
         pv = np.fromfile(pre + ".planes_v", np.uint8).reshape(N_POS, 32, 361)
         sq = np.fromfile(pre + ".squares", np.int8).reshape(N_POS, 361)
         meta = np.fromfile(pre + ".meta", np.int32).reshape(N_POS, 4)
+        moves = np.fromfile(pre + ".moves", np.int32).reshape(N_POS, 4)
         np.savez_compressed(os.path.join(HERE, "positions_s0.npz"),
                             planes_p=np.packbits(pp, axis=-1), planes_v=np.packbits(pv, axis=-1),
-                            squares=sq, meta=meta)
+                            squares=sq, meta=meta, moves=moves)
 
         run([harness, "elucheck", wp], env=env)
 

@@ -13,17 +13,38 @@ pytestmark = pytest.mark.gpu
 POINTS = 361
 
 
-def _gather(lg, squares, to_move, which, nplanes=24):
+def _gather(lg, squares, to_move, which, nplanes=24, moves=None):
     import torch
-    sq = torch.from_numpy(np.ascontiguousarray(squares, dtype=np.int8).reshape(-1, POINTS)).cuda()
+    sq = torch.from_numpy(np.array(squares, dtype=np.int8).reshape(-1, POINTS)).cuda()
     B = sq.shape[0]
-    tm = torch.from_numpy(np.ascontiguousarray(
-        np.broadcast_to(np.asarray(to_move, dtype=np.int8), (B,)))).cuda()
+    tm = torch.from_numpy(np.array(np.broadcast_to(np.asarray(to_move, dtype=np.int8), (B,)))).cuda()
+    mv = None if moves is None else torch.from_numpy(np.array(moves, dtype=np.int32).reshape(B, 4)).cuda()
     out = torch.full((max(B, 1), nplanes, POINTS), 7, dtype=torch.uint8, device="cuda")
     s = torch.cuda.current_stream().cuda_stream
-    lg.gather_device(sq.data_ptr(), tm.data_ptr(), B, which, nplanes, out.data_ptr(), s)
+    lg.gather_device(sq.data_ptr(), tm.data_ptr(), B, which, nplanes, out.data_ptr(), s,
+                     None if mv is None else mv.data_ptr())
     torch.cuda.synchronize()
     return out[:B].cpu().numpy()
+
+
+def _synthetic_moves(squares, to_move, seed):
+    """Last move = a stone of the side that just moved, the move before = a
+    stone of the side to move (or -1), a ko point on some boards, komi on
+    most -- the extra inputs planes 24..31 read."""
+    rng = np.random.default_rng(seed)
+    mv = np.full((len(squares), 4), -1, np.int32)
+    for i, (sq, tm) in enumerate(zip(squares, to_move)):
+        last = np.flatnonzero(sq == 1 - tm)
+        prev = np.flatnonzero(sq == tm)
+        empty = np.flatnonzero(sq == 2)
+        if last.size and rng.random() < 0.9:
+            mv[i, 0] = rng.choice(last)
+            if prev.size and rng.random() < 0.9:
+                mv[i, 1] = rng.choice(prev)
+        if empty.size and rng.random() < 0.2:
+            mv[i, 2] = rng.choice(empty)
+        mv[i, 3] = int(rng.random() < 0.8)
+    return mv
 
 
 @pytest.mark.parametrize("which,key", [(0, "planes_p"), (1, "planes_v")])
@@ -32,6 +53,24 @@ def test_gather_matches_reference_planes(gpu_lib, positions, which, key):
     ref = positions[key][:, :24]
     bad = np.argwhere(got != ref)
     assert bad.size == 0, bad[:5]
+
+
+@pytest.mark.parametrize("which,key", [(0, "planes_p"), (1, "planes_v")])
+def test_gather_all_32_planes_match_reference(gpu_lib, positions, which, key):
+    """Ladders, ko, the last two moves, komi and the third line too."""
+    got = _gather(gpu_lib, positions["squares"], positions["meta"][:, 0], which, 32, positions["moves"])
+    bad = np.argwhere(got != positions[key])
+    assert bad.size == 0, bad[:5]
+
+
+@pytest.mark.parametrize("seed,kmax", [(4, 250), (5, 350)])
+def test_gather_32_planes_match_oracle_on_random_boards(gpu_lib, oracle_mod, seed, kmax):
+    sq, tm = oracle_mod.random_boards(256, seed, kmax=kmax)
+    mv = _synthetic_moves(sq, tm, seed)
+    for which in (0, 1):
+        got = _gather(gpu_lib, sq, tm, which, 32, mv)
+        ref = oracle_mod.gather_planes(sq, tm, which, 32, mv)
+        assert (got == ref).all(), np.argwhere(got != ref)[:5]
 
 
 @pytest.mark.parametrize("seed,kmax", [(1, 250), (2, 400), (3, 600)])
@@ -83,7 +122,7 @@ def test_gather_prefix_and_arguments(gpu_lib, positions):
     dsq = torch.from_numpy(np.ascontiguousarray(sq)).cuda()
     dtm = torch.from_numpy(np.ascontiguousarray(tm.astype(np.int8))).cuda()
     out = torch.zeros((8, 32, POINTS), dtype=torch.uint8, device="cuda")
-    for which, nplanes in ((0, 25), (0, 0), (2, 24)):
+    for which, nplanes in ((0, 33), (0, 0), (2, 24), (0, 25)):  # 25: planes 24.. need moves
         with pytest.raises(lg.LeelaGPUError):
             lg.gather_device(dsq.data_ptr(), dtm.data_ptr(), 8, which, nplanes, out.data_ptr(), None)
     with pytest.raises(lg.LeelaGPUError):
@@ -105,9 +144,19 @@ def test_board_calls_equal_plane_calls(gpu_lib, positions, weights, prec):
     assert np.array_equal(pb, pp) and np.array_equal(lb, lp) and np.array_equal(vb, vp)
 
 
-def test_board_calls_reject_wide_inputs(gpu_lib, weights, positions):
-    """A net reading more than 24 planes cannot take board input."""
+def test_board_calls_feed_32_plane_nets(gpu_lib, weights, positions):
+    """The reference-shaped nets read all 32 planes: from boards + moves they
+    give exactly what they give from the reference gather's planes (FP32);
+    without moves the call is refused."""
     lg = gpu_lib
-    with lg.Context(policy=lg.NetDesc.reference_policy(weights["ref_p"][1]), max_batch=8) as c:
+    n = 40
+    sq, tm, mv = positions["squares"][:n], positions["meta"][:n, 0], positions["moves"][:n]
+    with lg.Context(policy=lg.NetDesc.reference_policy(weights["ref_p"][1]),
+                    value=lg.NetDesc.reference_value(weights["ref_v"][1]), max_batch=16) as c:
         with pytest.raises(lg.LeelaGPUError):
-            c.policy_boards(positions["squares"][:2], positions["meta"][:2, 0])
+            c.policy_boards(sq[:2], tm[:2])
+        pb = c.policy_boards(sq, tm, moves=mv)
+        vb = c.value_boards(sq, tm, moves=mv)
+        pp = c.policy(positions["planes_p"][:n])
+        vp = c.value(positions["planes_v"][:n])
+    assert np.array_equal(pb, pp) and np.array_equal(vb, vp)

@@ -1,7 +1,7 @@
-"""The oracle's restatement of the input-plane gather (planes 0..23 of the
-policy and value sets) against the planes the reference's own gather wrote
-for the 1024 fixture positions (Network.cpp:883-1201), and the oracle's
-random-board generator.  CPU only."""
+"""The oracle's restatement of the input-plane gather (all 32 planes of the
+policy and value sets, the ladder reader included) against the planes the
+reference's own gather wrote for the 1024 fixture positions
+(Network.cpp:883-1201), and the oracle's random-board generator.  CPU only."""
 import numpy as np
 
 
@@ -12,6 +12,20 @@ def test_gather_matches_reference_planes(positions, oracle_mod):
         ref = positions[key][:, :24]
         bad = np.argwhere(got != ref)
         assert bad.size == 0, (key, bad[:5])
+
+
+def test_gather_all_32_planes_match_reference(positions, oracle_mod):
+    """Ladders (FastBoard.cpp:2530-2837), ko, the last two moves, komi and the
+    third line as well: 269 ladder and 1482 ladder-win points in the fixture."""
+    sq, tm, mv = positions["squares"], positions["meta"][:, 0], positions["moves"]
+    for which, key in ((0, "planes_p"), (1, "planes_v")):
+        got = oracle_mod.gather_planes(sq, tm, which, 32, mv)
+        ref = positions[key]
+        bad = np.argwhere(got != ref)
+        assert bad.size == 0, (key, bad[:5])
+    ladder = positions["planes_p"][:, 25].sum()
+    win = positions["planes_p"][:, 26].sum()
+    assert ladder > 200 and win > 1000
 
 
 def test_fixture_covers_every_plane(positions):
