@@ -67,14 +67,25 @@ def load_positions():
     return np.ascontiguousarray(P), np.ascontiguousarray(V)
 
 
-def load_boards():
+def load_boards(with_moves: bool = False):
     """The 1024 fixture boards under the 8 symmetries, in the order of
-    load_positions(): squares [8192][361] int8 and to_move [8192] int8."""
+    load_positions(): squares [8192][361] int8 and to_move [8192] int8 (and
+    moves [8192][4]: last move, the move before, ko point -- rotated with the
+    board -- and the komi flag)."""
     d = np.load(os.path.join(ROOT, "tests", "golden", "positions_s0.npz"))
     import leela_gb300 as lg
     sq = np.concatenate([d["squares"][:, lg.ROTATE[s]] for s in range(8)])
     tm = np.tile(d["meta"][:, 0].astype(np.int8), 8)
-    return np.ascontiguousarray(sq, dtype=np.int8), tm
+    if not with_moves:
+        return np.ascontiguousarray(sq, dtype=np.int8), tm
+    mv = []
+    for s in range(8):
+        inv = np.argsort(lg.ROTATE[s])  # old point -> its index on the rotated board
+        m = d["moves"].copy()
+        for k in range(3):
+            m[:, k] = np.where(m[:, k] >= 0, inv[np.maximum(m[:, k], 0)], -1)
+        mv.append(m)
+    return np.ascontiguousarray(sq, dtype=np.int8), tm, np.ascontiguousarray(np.concatenate(mv), np.int32)
 
 
 def make_weights():
@@ -563,37 +574,46 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
 
 
 def gather_throughput(lg, squares, to_move, dev, sp, reps=20):
-    """lg_gather_device alone: 8192 boards -> 24 policy planes and 24 value
-    planes, boards resident in HBM.  Algorithmic bytes per board and set:
-    362 in + 24 * 361 out."""
+    """lg_gather_device alone, boards resident in HBM: 8192 boards -> 24
+    policy planes and 24 value planes (the benchmark nets' inputs;
+    algorithmic bytes per board and set 362 in + 24 * 361 out), and -> all 32
+    planes of both sets (ladder reader, ko, last moves, komi)."""
     import torch
     B = squares.shape[0]
+    _, _, moves = load_boards(with_moves=True)
     d_sq = torch.from_numpy(squares).to(dev)
     d_tm = torch.from_numpy(to_move).to(dev)
-    out_p = torch.empty((B, 24, 361), dtype=torch.uint8, device=dev)
-    out_v = torch.empty((B, 24, 361), dtype=torch.uint8, device=dev)
-
-    def run():
-        lg.gather_device(d_sq.data_ptr(), d_tm.data_ptr(), B, 0, 24, out_p.data_ptr(), sp)
-        lg.gather_device(d_sq.data_ptr(), d_tm.data_ptr(), B, 1, 24, out_v.data_ptr(), sp)
-
-    for _ in range(3):
-        run()
-    torch.cuda.synchronize()
+    d_mv = torch.from_numpy(moves).to(dev)
+    out_p = torch.empty((B, 32, 361), dtype=torch.uint8, device=dev)
+    out_v = torch.empty((B, 32, 361), dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
-        run()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
+
+    def timed(nplanes):
+        def run():
+            for which, out in ((0, out_p), (1, out_v)):
+                lg.gather_device(d_sq.data_ptr(), d_tm.data_ptr(), B, which, nplanes, out.data_ptr(), sp,
+                                 d_mv.data_ptr())
+        for _ in range(3):
+            run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms = timed(24)
+    ms32 = timed(32)
     per_launch = B * (362 + 24 * 361)
     _, hbm, _ = read_peaks()
     gbs = 2 * per_launch / (ms / 1e3) / 1e9
     return {"boards_per_s_both_sets": B / (ms / 1e3), "us_per_launch": ms * 1e3 / 2,
             "boards_per_launch": B, "algorithmic_bytes_per_launch": per_launch,
-            "achieved_gbs": gbs, "hbm_peak_gbs": hbm, "frac_of_hbm": gbs / hbm if hbm else None}
+            "achieved_gbs": gbs, "hbm_peak_gbs": hbm, "frac_of_hbm": gbs / hbm if hbm else None,
+            "all_32_planes_boards_per_s_both_sets": B / (ms32 / 1e3),
+            "all_32_planes_us_per_launch": ms32 * 1e3 / 2}
 
 
 def distill_config4(wp, wv, planes_p, planes_v, device):
