@@ -64,6 +64,13 @@ __device__ __forceinline__ int tap_shift(int kind, int t) {
     return (t - 2) * kL5Pitch;
 }
 
+// ReLU, round to nearest even and pack: lo in bits 0..15, hi in 16..31.
+__device__ __forceinline__ uint32_t pack_relu_bf16x2(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+
 __device__ __forceinline__ float act_apply(float v, int act) {
     if (act == LG_ACT_ELU) return (v > 0.0f) ? v : (expf(v) - 1.0f);
     return fmaxf(v, 0.0f);
@@ -679,6 +686,31 @@ struct TrunkCfg {
 constexpr uint32_t kFlagPolls = 1u << 22;  // x ~64 ns sleep: bounded at ~0.3 s
 constexpr int kItemRing = 4;               // item descriptors in flight per CTA
 
+// The MMAs of one 64-channel half of an item: NTAPS weight stages (one per
+// tap, 4 K steps of 16 each) against the window in the slot whose descriptor
+// is b_desc; stage g of the ring is slot g & 3.  Descriptor start addresses
+// advance by (bytes >> 4): tap rows of 128 bytes, K steps of 32 bytes.
+// Returns false if a weight stage did not arrive within the wait limit.
+template <int KIND, int NTAPS, int WPRE>
+__device__ __forceinline__ bool issue_taps(uint32_t d_tmem, uint64_t a_desc0, uint64_t b_desc, uint32_t idesc,
+                                           bool first_half, uint32_t &g, uint64_t *w_full, uint64_t *w_empty) {
+    constexpr int kStage16 = TcTCfg<2, 0>::WST_BYTES >> 4;
+#pragma unroll
+    for (int t = 0; t < NTAPS; ++t, ++g) {
+        const int s = g & 3;
+        if (!mbar_wait(&w_full[s], (g >> 2) & 1, kWaitLimit)) return false;
+        tc_fence_after();
+        const uint64_t a = a_desc0 + (uint64_t)(s * kStage16);
+        const uint64_t b = b_desc + (uint64_t)((WPRE + (KIND == 0 ? (t / 3 - 1) * kL3Pitch + (t % 3 - 1)
+                                                                  : (t - 2) * kL5Pitch)) * 8);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+            mma_bf16(d_tmem, a + 2 * kk, b + 2 * kk, idesc, (first_half && t == 0 && kk == 0) ? 0u : 1u);
+        mma_commit(&w_empty[s]);
+    }
+    return true;
+}
+
 __device__ __forceinline__ bool poll_flag(const int *f, int want) {
     uint32_t n = 0;
     while (ld_acquire_gpu(f) < want && ++n < kFlagPolls) __nanosleep(64);
@@ -867,7 +899,14 @@ __global__ void __maxnreg__(96)
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
+        // One thread keeps the tensor pipe fed: every descriptor is a base
+        // computed once plus compile-time offsets (tap rows, K steps), and the
+        // tap and K loops are unrolled per item kind, so issuing an MMA costs
+        // a 64-bit add per operand (an MMA of N = 256 lasts ~128 cycles).
         if (lane == 0) {
+            static_assert(C::S == 4, "stage index is g & 3");
+            const uint64_t a_desc0 = sdesc_sw128(smem_u32(wst));
+            const uint64_t b_desc0 = sdesc_sw128(smem_u32(win));
             uint32_t g = 0, wn = 0;
             for (int q = 0;; ++q) {
                 const int slot = q % kItemRing;
@@ -878,7 +917,6 @@ __global__ void __maxnreg__(96)
                 int l, j;
                 decode(it, l, j);
                 const bool fl = first && l == 0;
-                const int ntaps = fl ? C1::NTAPS : C0::NTAPS;
                 // N: the item's rows, rounded up to the MMA's multiple of 16
                 // (rows past the tensor are zero-filled and not stored)
                 const int nrows = fl ? min(C::TP, (p.rows5 - j * C::TP + 15) / 16 * 16) : min(C::TP, p.rows - j * C::TP);
@@ -888,34 +926,24 @@ __global__ void __maxnreg__(96)
                 if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(76); break; }
                 tc_fence_after();
                 const uint32_t d_tmem = tmem + (uint32_t)(acc * C::TP);
-                bool first_mma = true;
-                for (int h = 0; h < HALVES; ++h, ++wn) {
+                bool ok = true;
+#pragma unroll
+                for (int h = 0; h < HALVES && ok; ++h, ++wn) {
                     const int ws = wn % C::NWIN;
                     const uint32_t wk = wn / C::NWIN;
-                    if (!mbar_wait(&win_full[ws], wk & 1, kWaitLimit)) { fail(77); goto done_mma; }
+                    if (!mbar_wait(&win_full[ws], wk & 1, kWaitLimit)) { fail(77); ok = false; break; }
                     tc_fence_after();
-                    const uint32_t win_addr = smem_u32(win + ws * C::WIN_SLOT);
-                    for (int t = 0; t < ntaps; ++t, ++g) {
-                        const int s = g % C::S;
-                        const uint32_t k = g / C::S;
-                        if (!mbar_wait(&w_full[s], k & 1, kWaitLimit)) { fail(78); goto done_mma; }
-                        tc_fence_after();
-                        const uint32_t a_base = smem_u32(wst + s * C::WST_BYTES);
-                        const int brow = fl ? C1::WPRE + tap_shift(1, t) : C0::WPRE + tap_shift(0, t);
-                        const uint32_t b_base = win_addr + (uint32_t)brow * 128u;
-#pragma unroll
-                        for (int kk = 0; kk < 4; ++kk) {
-                            mma_bf16(d_tmem, sdesc_sw128(a_base + kk * 32), sdesc_sw128(b_base + kk * 32),
-                                     idesc, first_mma ? 0u : 1u);
-                            first_mma = false;
-                        }
-                        mma_commit(&w_empty[s]);
-                    }
+                    const uint64_t b_desc = b_desc0 + (uint64_t)(ws * (C::WIN_SLOT >> 4));
+                    ok = fl ? issue_taps<1, C1::NTAPS, C1::WPRE>(d_tmem, a_desc0, b_desc, idesc, h == 0, g, w_full,
+                                                                 w_empty)
+                            : issue_taps<0, C0::NTAPS, C0::WPRE>(d_tmem, a_desc0, b_desc, idesc, h == 0, g, w_full,
+                                                                 w_empty);
+                    if (!ok) { fail(78); break; }
                     mma_commit(&win_empty[ws]);
                 }
+                if (!ok) break;
                 mma_commit(&acc_full[acc]);
             }
-        done_mma:;
         }
     } else {
         // ------------------------------------------------ epilogue
@@ -965,12 +993,11 @@ __global__ void __maxnreg__(96)
                     if (lane == 0) mbar_arrive(&acc_empty[acc]);
                 }
                 if (c >= nhalf || bad) continue;
-                float f[32];
-#pragma unroll
-                for (int jj = 0; jj < 32; ++jj) f[jj] = act_apply(fmaf(__uint_as_float(v[jj]), scale, bias), p.act);
                 if (head_layer) {
+                    float f[32];
 #pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) f[jj] *= hw;
+                    for (int jj = 0; jj < 32; ++jj)
+                        f[jj] = act_apply(fmaf(__uint_as_float(v[jj]), scale, bias), p.act) * hw;
                     head_store<0>(warp_transpose_sum(f, lane), head_red + rq * 128, rq, quarter, lane,
                                   q_base + c * 32 + lane, p.rows, p.parts);
                 } else {
@@ -995,10 +1022,30 @@ __global__ void __maxnreg__(96)
                         valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
                     }
                     const unsigned vmask = __ballot_sync(0xffffffffu, valid_lane);
-                    __nv_bfloat16 *col = reinterpret_cast<__nv_bfloat16 *>(buf) + o;
+                    // This warp shares its SM sub-partition's issue slots with
+                    // the MMA-issuing thread (a warp reads only the TMEM lane
+                    // quarter of its sub-partition), so the loop is lean:
+                    // per two rows a bias add each, one ReLU + round + pack
+                    // (cvt.rn.relu.bf16x2), two 16-bit stores; pad rows are
+                    // zeroed afterwards.
+                    uint16_t *col = reinterpret_cast<uint16_t *>(buf) + o;
+                    if (p.act == LG_ACT_RELU) {
 #pragma unroll
-                    for (int jj = 0; jj < 32; ++jj)
-                        col[jj * 128] = __float2bfloat16_rn(((vmask >> jj) & 1u) ? f[jj] : 0.0f);
+                        for (int jj = 0; jj < 32; jj += 2) {
+                            const uint32_t w = pack_relu_bf16x2(fmaf(__uint_as_float(v[jj]), scale, bias),
+                                                                fmaf(__uint_as_float(v[jj + 1]), scale, bias));
+                            col[jj * 128] = (uint16_t)w;
+                            col[(jj + 1) * 128] = (uint16_t)(w >> 16);
+                        }
+                    } else {
+#pragma unroll
+                        for (int jj = 0; jj < 32; ++jj) {
+                            const __nv_bfloat16 h =
+                                __float2bfloat16_rn(act_apply(fmaf(__uint_as_float(v[jj]), scale, bias), p.act));
+                            col[jj * 128] = *reinterpret_cast<const uint16_t *>(&h);
+                        }
+                    }
+                    for (unsigned pad = ~vmask; pad; pad &= pad - 1) col[(__ffs(pad) - 1) * 128] = 0;
                     fence_proxy_async();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&stg_full[rq]);
