@@ -4,7 +4,10 @@
 // by 3 rows (mode 1), or cycling through the nine 3x3 tap shifts of the L3
 // layout (mode 2); the B start row (N rows) cycling through the nine tap
 // shifts (mode 3, the conv kernels' case) or through nine multiples of 8
-// rows (mode 4).  Build and run on a GB300:
+// rows (mode 4); mode 5 = mode 3 plus, every 4 MMAs, the per-stage handshake
+// of the conv kernels (tcgen05.commit to an mbarrier, an mbarrier wait that
+// is already satisfied, tcgen05.fence::after_thread_sync).  Build and run on
+// a GB300:
 //   nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 \
 //        -o tc_mma_rate leela_gb300/microbench/tc_mma_rate.cu && ./tc_mma_rate
 #include <cstdio>
@@ -17,7 +20,8 @@ using namespace lg::ptx;
 __device__ __forceinline__ uint32_t idesc_n(int N) { return idesc_bf16(128, N); }
 
 // MODE: 0 = aligned, 1 = A shifted by 3 rows, 2 = A cycling 9 tap shifts,
-// 3 = B cycling 9 tap shifts, 4 = B cycling 9 multiples of 8 rows.  The 36
+// 3 = B cycling 9 tap shifts, 4 = B cycling 9 multiples of 8 rows, 5 = 3 plus
+// the per-stage handshake.  The 36
 // (tap, K step) descriptors of one round are compile-time offsets of two base
 // descriptors (the start-address field is addr >> 4 in the low 14 bits and
 // never carries), so the one issuing thread spends a few instructions per MMA.
@@ -27,12 +31,18 @@ __global__ void __launch_bounds__(128, 1) bench(int rounds, unsigned long long *
     uint8_t *sm = (uint8_t *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
     uint8_t *A = sm;                 // 256 rows x 128 B
     uint8_t *Bm = sm + 256 * 128;    // 256 + 64 rows x 128 B
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bar, bar2[4], bar3;
     __shared__ uint32_t tb;
     int tid = threadIdx.x, warp = tid / 32;
     for (int i = tid; i < 576 * 128 / 16; i += 128) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
     fence_proxy_async();
-    if (tid == 0) { mbar_init(&bar, 1); fence_mbar_init(); }
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        for (int i = 0; i < 4; ++i) mbar_init(&bar2[i], (1 << 20) - 1);  // never completes: commits only count
+        mbar_init(&bar3, 1);
+        fence_mbar_init();
+        mbar_arrive(&bar3);  // phase 0 complete: waits on it return at once
+    }
     if (warp == 0) tmem_alloc(&tb, 256);
     __syncthreads();
     tc_fence_after();
@@ -46,9 +56,14 @@ __global__ void __launch_bounds__(128, 1) bench(int rounds, unsigned long long *
                 const int t9 = u / 4, kk = u % 4;
                 const int tap = 3 + (t9 / 3) * 20 + t9 % 3;  // the 3x3 tap shifts 3,4,5,23,..,45 (L3 pitch 20)
                 const int ra = MODE == 1 ? 3 : (MODE == 2 ? tap : 0);
-                const int rb = MODE == 3 ? tap : (MODE == 4 ? 8 * t9 : 0);
+                const int rb = (MODE == 3 || MODE == 5) ? tap : (MODE == 4 ? 8 * t9 : 0);
                 mma_bf16(tb, a0 + (uint64_t)((ra * 128 + kk * 32) >> 4), b0 + (uint64_t)((rb * 128 + kk * 32) >> 4), id,
                          (r > 0 || u > 0) ? 1u : 0u);
+                if (MODE >= 5 && kk == 3) {
+                    mma_commit(&bar2[t9 & 3]);
+                    if (!mbar_wait(&bar3, 0, 1u << 20)) atomicExch(err, 2);
+                    tc_fence_after();
+                }
             }
         }
         mma_commit(&bar);
@@ -93,6 +108,7 @@ int main() {
     run<256, 3>(sms, smem, rounds, dc, de);
     run<256, 4>(sms, smem, rounds, dc, de);
     run<128, 3>(sms, smem, rounds, dc, de);
+    run<256, 5>(sms, smem, rounds, dc, de);
     int he; cudaMemcpy(&he, de, 4, cudaMemcpyDeviceToHost);
     printf("err=%d\n", he);
     return 0;
