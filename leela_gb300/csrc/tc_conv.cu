@@ -734,7 +734,10 @@ __global__ void __maxnreg__(96)
     uint8_t *wst = stg + C::STG_TOTAL;
 
     __shared__ uint64_t win_full[C::NWIN], win_empty[C::NWIN], w_full[C::S], w_empty[C::S];
-    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], item_done;
+    // item_done: a ring of 4 (an epilogue warp can be up to two items ahead
+    // of the slowest: starting item x needs every warp to have read item
+    // x-2's accumulator, hence to have arrived for item x-3)
+    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], item_done[4];
     __shared__ uint64_t item_full[kItemRing], item_empty[kItemRing];
     __shared__ int item_id[kItemRing];
     __shared__ uint32_t tmem_base;
@@ -779,7 +782,7 @@ __global__ void __maxnreg__(96)
             mbar_init(&item_full[i], 1);
             mbar_init(&item_empty[i], 2 + kEpiWarpsT);  // weight producer, MMA issuer, epilogue warps
         }
-        mbar_init(&item_done, kEpiWarpsT);
+        for (int i = 0; i < 4; ++i) mbar_init(&item_done[i], kEpiWarpsT);
         abort_flag = 0;
         fence_mbar_init();
         prefetch_tensormap(&in_a);
@@ -1092,9 +1095,9 @@ __global__ void __maxnreg__(96)
                 // warps' bulk stores).
                 if (quarter == 0 && lane == 0) bulk_wait0();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&item_done);
+                if (lane == 0) mbar_arrive(&item_done[done_n & 3]);
                 if (warp == 4 && lane == 0) {
-                    if (!mbar_wait(&item_done, done_n & 1, kWaitLimit)) {
+                    if (!mbar_wait(&item_done[done_n & 3], (done_n >> 2) & 1, kWaitLimit)) {
                         fail(83);
                     } else {
                         fence_proxy_async_global();
