@@ -22,8 +22,10 @@
 //
 // Planes 24..31: the ladder reader runs only where it can answer "yes" --
 // an empty point with two empty neighbours next to an own string in atari
-// (ladder), or next to an opponent string of two liberties (ladder win) --
-// one thread per such point on a bitboard copy of the position.
+// (ladder), or next to an opponent string of two liberties (ladder win).
+// The point threads list those candidates in shared memory; then each warp
+// takes candidates from the list and reads the ladder on a row bitboard
+// (ladder.cuh), all 32 lanes together.
 //
 // Input: squares [B][361] (0 black, 1 white, 2 empty; point y*19+x), to_move
 // [B] (0 black, 1 white), and for planes 24..31 moves [B][4] (last move, the
@@ -47,14 +49,18 @@ __device__ __forceinline__ int nbr(int p, int k) {
 }
 
 // WHICH: 0 = policy planes, 1 = value planes; EXTRA: planes 24..31 wanted
-// (the ladder reader's registers and stack stay out of the 24-plane kernel)
+// (the ladder reader's code and shared lists stay out of the 24-plane kernel)
 template <int WHICH, bool EXTRA>
-__global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ squares,
+__global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict__ squares,
                                                      const int8_t *__restrict__ to_move,
                                                      const int32_t *__restrict__ moves, int B,
                                                      int nplanes, uint8_t *__restrict__ planes) {
-    __shared__ lad::Masks masks;
-    __shared__ lad::Board board;
+    constexpr bool extra = EXTRA;
+    constexpr int kCand = extra ? 2 * kPoints : 1;
+    __shared__ uint32_t rowc[2][kBoard];  // row bitboard: bit x of rowc[c][y] = stone of colour c at (y, x)
+    __shared__ short cand[kCand];         // ladder candidates: point | kind << 9 (0 ladder, 1 ladder win)
+    __shared__ uint8_t lad_yes[extra ? kPoints : 1], win_yes[extra ? kPoints : 1];
+    __shared__ int ncand;
     __shared__ int8_t sq[kPoints];
     __shared__ short lab[kPoints];
     __shared__ uint32_t stones[kPoints][kWords];
@@ -75,21 +81,14 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
             stones[p][w] = 0;
             adj[p][w] = 0;
         }
+        if (extra) {
+            lad_yes[p] = 0;
+            win_yes[p] = 0;
+        }
     }
     if (p < kWords) empty[p] = 0;
-    constexpr bool extra = EXTRA;
-    if (extra && p < 3 * kWords) {
-        // board, x != 0, x != 18 masks (bit q = point q)
-        const int kind = p / kWords, w = p % kWords;
-        uint32_t m = 0;
-        for (int j = 0; j < 32; ++j) {
-            const int q = w * 32 + j, x = q % kBoard;
-            const bool in = q < kPoints && (kind == 0 || (kind == 1 ? x != 0 : x != kBoard - 1));
-            m |= (uint32_t)in << j;
-        }
-        (kind == 0 ? masks.board : kind == 1 ? masks.notx0 : masks.notx18)[w] = m;
-    }
-    if (extra && p < 2 * kWords) board.c[p / kWords][p % kWords] = 0;
+    if (extra && p < 2 * kBoard) rowc[p / kBoard][p % kBoard] = 0;
+    if (extra && p == 0) ncand = 0;
     __syncthreads();
     // string labels: minimum point index of the string
     for (int it = 0; it < 2 * kPoints; ++it) {
@@ -112,7 +111,7 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
         if (c == 2) {
             atomicOr(&empty[p >> 5], 1u << (p & 31));
         } else {
-            if (extra && (c == 0 || c == 1)) atomicOr(&board.c[c][p >> 5], 1u << (p & 31));
+            if (extra && (c == 0 || c == 1)) atomicOr(&rowc[c][p / kBoard], 1u << (p % kBoard));
             const int r = lab[p];
             atomicOr(&stones[r][p >> 5], 1u << (p & 31));
             for (int k = 0; k < 4; ++k) {
@@ -128,7 +127,6 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
         libs[p] = (short)n;
     }
     __syncthreads();
-    if (!on) return;
     uint32_t bits = 0;  // bit i = plane i at this point
     // policy: own libs 1,2,3,4,5+ at 3..7, opponent's at 8..12, after-move
     // 1..5,6+ at 13..18, opponent's after-move 1..5,6+ at 19..24, ladder 25,
@@ -140,17 +138,17 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
     constexpr int kAfter0 = WHICH == 0 ? 13 : 15, kOAfter0 = WHICH == 0 ? 19 : 21;
     constexpr int kLadder = WHICH == 0 ? 25 : 27, kWin = WHICH == 0 ? 26 : 28;
     constexpr int kKomi = WHICH == 0 ? 30 : 29, kLine3 = WHICH == 0 ? 31 : 30, kKo = WHICH == 0 ? 27 : 31;
-    {
+    if (on) {
         const int x = p % kBoard, y = p / kBoard;
         if (x == 2 || x == 16 || y == 2 || y == 16) bits |= 1u << kLine3;
     }
-    if (c != 2) {
+    if (on && c != 2) {
         const bool mine = c == tomove;
         bits |= mine ? 2u : 4u;
         if (extra && c == 1 && moves[(size_t)b * 4 + 3]) bits |= 1u << kKomi;
         const int l = libs[lab[p]];
         if (l >= 1) bits |= 1u << ((mine ? 3 : kOppLib0) + (l >= kLibCap ? kLibCap : l) - 1);
-    } else {
+    } else if (on) {
         bits |= 1u;
         int nb[4];
 #pragma unroll
@@ -209,16 +207,39 @@ __global__ void __launch_bounds__(384) gather_kernel(const int8_t *__restrict__ 
             }
             // ladder: two empty neighbours, an own string in atari next to it
             // (its saving move then is no self-atari)
-            if (n_empty == 2 && own_atari && lad::losing_ladder(board, tomove, p, masks)) bits |= 1u << kLadder;
-            if (opp_two && lad::winning_ladder(board, tomove, p, masks)) bits |= 1u << kWin;
+            if (n_empty == 2 && own_atari) cand[atomicAdd(&ncand, 1)] = (short)p;
+            if (opp_two) cand[atomicAdd(&ncand, 1)] = (short)(p | 1 << 9);
         }
     }
     if (extra) {
-        const int32_t *mv = moves + (size_t)b * 4;
-        if (WHICH == 0 && mv[0] == p) bits |= 1u << 28;
-        if (WHICH == 0 && mv[0] >= 0 && mv[1] == p) bits |= 1u << 29;
-        if (mv[2] == p) bits |= 1u << kKo;
+        __syncthreads();
+        // one warp per candidate; the row board in registers (lane y = row y)
+        const int lane = p & 31, warp = p >> 5, nwarps = blockDim.x >> 5;
+        lad::Board wb;
+        wb.c[0] = lane < kBoard ? rowc[0][lane] : 0u;
+        wb.c[1] = lane < kBoard ? rowc[1][lane] : 0u;
+        const int n = ncand;
+        for (int i = warp; i < n; i += nwarps) {
+            const int e = cand[i], q = e & 0x1ff;
+            if (e >> 9) {
+                const bool yes = lad::winning_ladder(wb, tomove, q);
+                if (lane == 0) win_yes[q] = yes;
+            } else {
+                const bool yes = lad::losing_ladder(wb, tomove, q);
+                if (lane == 0) lad_yes[q] = yes;
+            }
+        }
+        __syncthreads();
+        if (on) {
+            if (lad_yes[p]) bits |= 1u << kLadder;
+            if (win_yes[p]) bits |= 1u << kWin;
+            const int32_t *mv = moves + (size_t)b * 4;
+            if (WHICH == 0 && mv[0] == p) bits |= 1u << 28;
+            if (WHICH == 0 && mv[0] >= 0 && mv[1] == p) bits |= 1u << 29;
+            if (mv[2] == p) bits |= 1u << kKo;
+        }
     }
+    if (!on) return;
     uint8_t *dst = planes + (size_t)b * nplanes * kPoints + p;
     for (int i = 0; i < nplanes; ++i) dst[(size_t)i * kPoints] = (uint8_t)((bits >> i) & 1u);
 }
