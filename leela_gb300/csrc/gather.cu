@@ -18,7 +18,9 @@
 //   after-move liberties(p, c)   = |(nbrs(p) | adj of c's strings next to p)
 //                                   & ((empty | stones of captured strings) - {p})|
 // where the captured strings are the opponent strings next to p with one
-// liberty.
+// liberty.  Most empty points (no capture, at most one string joined) need
+// no set: the count is then the empty neighbours, or the joined string's
+// liberties less p plus the empty neighbours outside its adjacency.
 //
 // Planes 24..31: the ladder reader runs only where it can answer "yes" --
 // an empty point with two empty neighbours next to an own string in atari
@@ -63,8 +65,8 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
     __shared__ int ncand;
     __shared__ int8_t sq[kPoints];
     __shared__ short lab[kPoints];
-    __shared__ uint32_t stones[kPoints][kWords];
-    __shared__ uint32_t adj[kPoints][kWords];
+    __shared__ __align__(16) uint32_t stones[kPoints][kWords];
+    __shared__ __align__(16) uint32_t adj[kPoints][kWords];
     __shared__ uint32_t empty[kWords];
     __shared__ short libs[kPoints];
     const int b = blockIdx.x;
@@ -77,9 +79,11 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
         c = squares[(size_t)b * kPoints + p];
         sq[p] = c;
         lab[p] = (c == 2) ? -1 : (short)p;
-        for (int w = 0; w < kWords; ++w) {
-            stones[p][w] = 0;
-            adj[p][w] = 0;
+        uint4 *zs = reinterpret_cast<uint4 *>(stones[p]), *za = reinterpret_cast<uint4 *>(adj[p]);
+#pragma unroll
+        for (int w = 0; w < kWords / 4; ++w) {
+            zs[w] = make_uint4(0u, 0u, 0u, 0u);
+            za[w] = make_uint4(0u, 0u, 0u, 0u);
         }
         if (extra) {
             lad_yes[p] = 0;
@@ -153,6 +157,9 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
         int nb[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) nb[k] = nbr(p, k);
+        int n_empty_nb = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) n_empty_nb += nb[k] >= 0 && sq[nb[k]] == 2;
         // liberties after a stone of colour col is played here
         int after[2];
 #pragma unroll
@@ -161,6 +168,8 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
             // the strings next to p: joined (own colour) or captured
             // (opponent's with one liberty, which is p); -1 = none
             int join[4], capt[4];
+            int join0 = -1;
+            bool one_join = true, no_capt = true;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 join[k] = -1;
@@ -168,8 +177,30 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
                 const int q = nb[k];
                 if (q < 0) continue;
                 const int cq = sq[q];
-                if (cq == col) join[k] = lab[q];
-                else if (cq != 2 && libs[lab[q]] == 1) capt[k] = lab[q];
+                if (cq == col) {
+                    join[k] = lab[q];
+                    if (join0 < 0) join0 = join[k];
+                    else one_join &= join0 == join[k];
+                } else if (cq != 2 && libs[lab[q]] == 1) {
+                    capt[k] = lab[q];
+                    no_capt = false;
+                }
+            }
+            if (no_capt && one_join) {
+                // no capture and at most one string joined: the empty
+                // neighbours, or the string's liberties less p plus the
+                // empty neighbours that are not among them
+                int n = n_empty_nb;
+                if (join0 >= 0) {
+                    n = libs[join0] - 1;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int q = nb[k];
+                        if (q >= 0 && sq[q] == 2 && !((adj[join0][q >> 5] >> (q & 31)) & 1u)) ++n;
+                    }
+                }
+                after[side] = n;
+                continue;
             }
             int n = 0;
             for (int w = 0; w < kWords; ++w) {

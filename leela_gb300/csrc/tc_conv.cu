@@ -71,6 +71,15 @@ __device__ __forceinline__ uint32_t pack_relu_bf16x2(float lo, float hi) {
     return d;
 }
 
+// Two fused multiply-adds in one packed FP32 instruction (fma.rn.f32x2,
+// sm_100 family): d_i = a_i * b + c, each rounded as fmaf.
+__device__ __forceinline__ void ffma2(float &d0, float &d1, float a0, float a1, float b, float c) {
+    asm("{\n.reg .b64 ra, rb, rc, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rb, {%4, %4};\n"
+        "mov.b64 rc, {%5, %5};\nfma.rn.f32x2 rd, ra, rb, rc;\nmov.b64 {%0, %1}, rd;\n}"
+        : "=f"(d0), "=f"(d1)
+        : "f"(a0), "f"(a1), "f"(b), "f"(c));
+}
+
 __device__ __forceinline__ float act_apply(float v, int act) {
     if (act == LG_ACT_ELU) return (v > 0.0f) ? v : (expf(v) - 1.0f);
     return fmaxf(v, 0.0f);
@@ -1028,15 +1037,16 @@ __global__ void __maxnreg__(96)
                     // This warp shares its SM sub-partition's issue slots with
                     // the MMA-issuing thread (a warp reads only the TMEM lane
                     // quarter of its sub-partition), so the loop is lean:
-                    // per two rows a bias add each, one ReLU + round + pack
-                    // (cvt.rn.relu.bf16x2), two 16-bit stores; pad rows are
-                    // zeroed afterwards.
+                    // per two rows one packed scale + bias (fma.rn.f32x2), one
+                    // ReLU + round + pack (cvt.rn.relu.bf16x2), two 16-bit
+                    // stores; pad rows are zeroed afterwards.
                     uint16_t *col = reinterpret_cast<uint16_t *>(buf) + o;
                     if (p.act == LG_ACT_RELU) {
 #pragma unroll
                         for (int jj = 0; jj < 32; jj += 2) {
-                            const uint32_t w = pack_relu_bf16x2(fmaf(__uint_as_float(v[jj]), scale, bias),
-                                                                fmaf(__uint_as_float(v[jj + 1]), scale, bias));
+                            float a0, a1;
+                            ffma2(a0, a1, __uint_as_float(v[jj]), __uint_as_float(v[jj + 1]), scale, bias);
+                            const uint32_t w = pack_relu_bf16x2(a0, a1);
                             col[jj * 128] = (uint16_t)w;
                             col[(jj + 1) * 128] = (uint16_t)(w >> 16);
                         }
