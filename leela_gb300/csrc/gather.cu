@@ -10,8 +10,8 @@
 // ko point, the last two moves, white's komi and the third line.  Planes
 // 0..23 -- the benchmark nets' inputs -- need only the board.
 //
-// One CTA per board, one thread per point.  Strings are labelled by
-// propagating the minimum point index over same-coloured neighbours; every
+// One CTA per board, one thread per point.  Strings are labelled with their
+// minimum point index by a union-find over same-coloured neighbours; every
 // string root owns two 361-bit sets in shared memory (its stones, and the
 // points adjacent to any of its stones), so that
 //   liberties(string)            = |adj & empty|
@@ -50,6 +50,32 @@ __device__ __forceinline__ int nbr(int p, int k) {
     }
 }
 
+// union-find over the points of one board (shared memory); par[x] <= x,
+// and parents only decrease
+__device__ __forceinline__ int find_root(const volatile int *par, int x) {
+    for (int i = 0; i < kPoints && par[x] != x; ++i) x = par[x];
+    return x;
+}
+
+// joins the trees of a and b: the larger root is linked under the smaller
+// (atomicMin); if it stopped being a root meanwhile, the atomicMin has moved
+// its link and the join goes on from the parent it had
+__device__ void unite(int *par, int a, int b) {
+    for (int i = 0; i < 4 * kPoints; ++i) {
+        a = find_root(par, a);
+        b = find_root(par, b);
+        if (a == b) return;
+        if (a < b) {
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        const int old = atomicMin(&par[a], b);
+        if (old == a) return;
+        a = old;
+    }
+}
+
 // WHICH: 0 = policy planes, 1 = value planes; EXTRA: planes 24..31 wanted
 // (the ladder reader's code and shared lists stay out of the 24-plane kernel)
 template <int WHICH, bool EXTRA>
@@ -69,6 +95,8 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
     __shared__ __align__(16) uint32_t adj[kPoints][kWords];
     __shared__ uint32_t empty[kWords];
     __shared__ short libs[kPoints];
+    __shared__ int par[kPoints];                     // union-find parents
+    __shared__ uint8_t adj_lo[kPoints], adj_hi[kPoints];  // words of a root's adjacency set
     const int b = blockIdx.x;
     if (b >= B) return;
     const int p = threadIdx.x;
@@ -94,23 +122,17 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
     if (extra && p < 2 * kBoard) rowc[p / kBoard][p % kBoard] = 0;
     if (extra && p == 0) ncand = 0;
     __syncthreads();
-    // string labels: minimum point index of the string
-    for (int it = 0; it < 2 * kPoints; ++it) {
-        int changed = 0;
-        if (on && c != 2) {
-            int m = lab[p];
-            for (int k = 0; k < 4; ++k) {
-                const int q = nbr(p, k);
-                if (q >= 0 && sq[q] == c) m = min(m, (int)lab[q]);
-            }
-            m = min(m, (int)lab[m]);  // jump towards the root
-            if (m < lab[p]) {
-                lab[p] = (short)m;
-                changed = 1;
-            }
-        }
-        if (!__syncthreads_or(changed)) break;
+    // string labels: the minimum point index of the string, by union-find:
+    // every stone links to its left and upper neighbours of its colour (the
+    // larger root under the smaller), then follows its parents to the root
+    if (on) par[p] = p;
+    __syncthreads();
+    if (on && c != 2) {
+        if (p % kBoard > 0 && sq[p - 1] == c) unite(par, p, p - 1);
+        if (p >= kBoard && sq[p - kBoard] == c) unite(par, p, p - kBoard);
     }
+    __syncthreads();
+    if (on && c != 2) lab[p] = (short)find_root(par, p);
     if (on) {
         if (c == 2) {
             atomicOr(&empty[p >> 5], 1u << (p & 31));
@@ -126,9 +148,18 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
     }
     __syncthreads();
     if (on && c != 2 && lab[p] == p) {
-        int n = 0;
-        for (int w = 0; w < kWords; ++w) n += __popc(adj[p][w] & empty[w]);
+        int n = 0, lo = kWords - 1, hi = 0;
+        for (int w = 0; w < kWords; ++w) {
+            const uint32_t a = adj[p][w];
+            n += __popc(a & empty[w]);
+            if (a) {
+                lo = min(lo, w);
+                hi = w;
+            }
+        }
         libs[p] = (short)n;
+        adj_lo[p] = (uint8_t)lo;
+        adj_hi[p] = (uint8_t)hi;
     }
     __syncthreads();
     uint32_t bits = 0;  // bit i = plane i at this point
@@ -202,8 +233,17 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
                 after[side] = n;
                 continue;
             }
+            // words the union can touch: p's neighbours and the joined
+            // strings' adjacency sets
+            int lo = max(p - kBoard, 0) >> 5, hi = min(p + kBoard, kPoints - 1) >> 5;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (join[k] >= 0) {
+                    lo = min(lo, (int)adj_lo[join[k]]);
+                    hi = max(hi, (int)adj_hi[join[k]]);
+                }
             int n = 0;
-            for (int w = 0; w < kWords; ++w) {
+            for (int w = lo; w <= hi; ++w) {
                 uint32_t u = 0, e = empty[w];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
