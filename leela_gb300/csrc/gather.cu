@@ -77,12 +77,15 @@ __device__ void unite(int *par, int a, int b) {
 }
 
 // WHICH: 0 = policy planes, 1 = value planes; EXTRA: planes 24..31 wanted
-// (the ladder reader's code and shared lists stay out of the 24-plane kernel)
-template <int WHICH, bool EXTRA>
+// (the ladder reader's code and shared lists stay out of the 24-plane
+// kernel); L5: write the first layer's expanded input rows (l5, `halves` x 64
+// BF16 channels a row) instead of the planes
+template <int WHICH, bool EXTRA, bool L5>
 __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict__ squares,
                                                      const int8_t *__restrict__ to_move,
                                                      const int32_t *__restrict__ moves, int B,
-                                                     int nplanes, uint8_t *__restrict__ planes) {
+                                                     int nplanes, uint8_t *__restrict__ planes, int halves,
+                                                     uint4 *__restrict__ l5) {
     constexpr bool extra = EXTRA;
     constexpr int kCand = extra ? 2 * kPoints : 1;
     __shared__ uint32_t rowc[2][kBoard];  // row bitboard: bit x of rowc[c][y] = stone of colour c at (y, x)
@@ -96,6 +99,7 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
     __shared__ uint32_t empty[kWords];
     __shared__ short libs[kPoints];
     __shared__ int par[kPoints];                     // union-find parents
+    __shared__ uint32_t pbits[L5 ? kPoints : 1];     // the planes of each point, for the L5 rows
     __shared__ uint8_t adj_lo[kPoints], adj_hi[kPoints];  // words of a root's adjacency set
     const int b = blockIdx.x;
     if (b >= B) return;
@@ -310,28 +314,88 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
             if (mv[2] == p) bits |= 1u << kKo;
         }
     }
+    if (L5) {
+        // Row r = y * 19 + x of the board's 399 L5 rows (y = 19, 20: zero
+        // pad rows), channel dx * nplanes + c = plane c at (y, x + dx - 2),
+        // zero off the board and from channel 5 * nplanes on; BF16 1.0 is
+        // 0x3F80.  One 16-byte group of 8 channels per thread and step.
+        if (on) pbits[p] = bits;
+        __syncthreads();
+        const int groups = halves * 8;
+        uint4 *dst = l5 + (size_t)b * kL5Board * groups;
+        const bool aligned = (nplanes & 7) == 0;  // a group's 8 channels share one dx
+        for (int i = p; i < kL5Board * groups; i += blockDim.x) {
+            const int r = i / groups, g = i - r * groups;
+            const int y = r / kL5Pitch, x = r - y * kL5Pitch;
+            uint32_t w[4] = {0u, 0u, 0u, 0u};
+            if (y < kBoard) {
+                if (aligned) {
+                    const int ch0 = g * 8, dx = ch0 / nplanes, c0 = ch0 - dx * nplanes, sx = x + dx - 2;
+                    if (dx < 5 && sx >= 0 && sx < kBoard) {
+                        const uint32_t v = pbits[y * kBoard + sx] >> c0;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            w[j] = ((v >> (2 * j)) & 1u) * 0x3F80u | ((v >> (2 * j + 1)) & 1u) * 0x3F800000u;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int ch = g * 8 + j, dx = ch / nplanes, c = ch - dx * nplanes, sx = x + dx - 2;
+                        if (dx < 5 && sx >= 0 && sx < kBoard && ((pbits[y * kBoard + sx] >> c) & 1u))
+                            w[j >> 1] |= (j & 1) ? 0x3F800000u : 0x3F80u;
+                    }
+                }
+            }
+            dst[i] = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        return;
+    }
     if (!on) return;
     uint8_t *dst = planes + (size_t)b * nplanes * kPoints + p;
     for (int i = 0; i < nplanes; ++i) dst[(size_t)i * kPoints] = (uint8_t)((bits >> i) & 1u);
 }
 
-int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
-                  int nplanes, uint8_t *planes, cudaStream_t s) {
+template <bool L5>
+static void launch_gather_kernel(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B,
+                                 int which, int nplanes, uint8_t *planes, int halves, uint4 *l5,
+                                 cudaStream_t s) {
+    const bool extra = nplanes > 24;
+    if (which == 0 && extra)
+        gather_kernel<0, true, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, l5);
+    else if (which == 0)
+        gather_kernel<0, false, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, l5);
+    else if (extra)
+        gather_kernel<1, true, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, l5);
+    else
+        gather_kernel<1, false, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, l5);
+}
+
+static int check_gather(int B, int which, int nplanes, const int32_t *moves) {
     if (B < 0 || nplanes < 1 || nplanes > kGatherPlanes || (which != 0 && which != 1) ||
         (nplanes > 24 && !moves && B > 0)) {
         lg_set_error("gather: planes 0..31 of the policy (0) or value (1) set; planes 24..31 need moves");
         return LG_ERR_ARG;
     }
-    if (B == 0) return LG_OK;
-    const bool extra = nplanes > 24;
-    if (which == 0 && extra)
-        gather_kernel<0, true><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes);
-    else if (which == 0)
-        gather_kernel<0, false><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes);
-    else if (extra)
-        gather_kernel<1, true><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes);
-    else
-        gather_kernel<1, false><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes);
+    return LG_OK;
+}
+
+int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
+                  int nplanes, uint8_t *planes, cudaStream_t s) {
+    if (int rc = check_gather(B, which, nplanes, moves)) return rc;
+    if (B > 0) launch_gather_kernel<false>(squares, to_move, moves, B, which, nplanes, planes, 0, nullptr, s);
+    return LG_OK;
+}
+
+int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
+                     int nplanes, int halves, __nv_bfloat16 *l5, cudaStream_t s) {
+    if (int rc = check_gather(B, which, nplanes, moves)) return rc;
+    if (halves < 1 || 5 * nplanes > halves * 64) {
+        lg_set_error("gather: %d planes need %d L5 channels, the layer has %d", nplanes, 5 * nplanes, halves * 64);
+        return LG_ERR_ARG;
+    }
+    if (B > 0)
+        launch_gather_kernel<true>(squares, to_move, moves, B, which, nplanes, nullptr, halves,
+                                   reinterpret_cast<uint4 *>(l5), s);
     return LG_OK;
 }
 

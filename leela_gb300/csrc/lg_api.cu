@@ -448,16 +448,19 @@ int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float
     return LG_OK;
 }
 
+// l5_ready: the first layer's expanded input rows are already in c->l5 (the
+// board path's gather writes them), so `planes` is not read.
 int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
-               float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof) {
+               float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof,
+               bool l5_ready = false) {
     const lg_net_desc &d = n.d;
     int L = 0;
     const TcConv &first = n.tc[0];
-    {
+    if (!l5_ready) {
         ProfScope ps(c, prof, LG_PROF_PACK, s);
         launch_pack_planes_l5(planes, B, d.c_in, first.halves, c->l5, s);
+        ++L;
     }
-    ++L;
     float *lg = logits_out ? logits_out : c->d_logits;
     const size_t part_stride = (size_t)B * kPoints;
     int bl = 0;
@@ -538,11 +541,12 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
 }
 
 int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
-            float *logits, float *value, cudaStream_t s, int *nlaunch, bool prof = false) {
+            float *logits, float *value, cudaStream_t s, int *nlaunch, bool prof = false,
+            bool l5_ready = false) {
     Net &n = c->nets[net];
     if (n.d.precision == LG_FP32)
         return forward_fp32(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof);
-    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof);
+    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof, l5_ready);
 }
 
 // Host call: chunks of up to max_batch positions go through a cached CUDA
@@ -572,6 +576,7 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
         return LG_ERR_ARG;
     }
     const bool with_moves = boards && n.d.c_in > 24;
+    const bool l5_direct = boards && n.d.precision != LG_FP32;
     if (with_moves && !moves && B > 0) {
         lg_set_error("the net reads planes 24..31 (ladders, ko, last moves, komi): moves are needed");
         return LG_ERR_ARG;
@@ -638,9 +643,13 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
             int nl = 0;
             if (boards) {
                 cudaMemcpyAsync(c->d_boards, hp[slot], in_bytes, cudaMemcpyHostToDevice, c->stream);
-                rc = launch_gather(c->d_boards, c->d_boards + (size_t)nb * kPoints,
-                                   with_moves ? reinterpret_cast<const int32_t *>(c->d_boards + mv_off) : nullptr, nb,
-                                   net == LG_NET_POLICY ? 0 : 1, n.d.c_in, c->d_planes, c->stream);
+                const int8_t *dsq = c->d_boards, *dtm = c->d_boards + (size_t)nb * kPoints;
+                const int32_t *dmv = with_moves ? reinterpret_cast<const int32_t *>(c->d_boards + mv_off) : nullptr;
+                const int which = net == LG_NET_POLICY ? 0 : 1;
+                // tensor-core nets: the gather writes the first layer's
+                // expanded input rows itself (no planes, no packing pass)
+                rc = l5_direct ? launch_gather_l5(dsq, dtm, dmv, nb, which, n.d.c_in, n.tc[0].halves, c->l5, c->stream)
+                               : launch_gather(dsq, dtm, dmv, nb, which, n.d.c_in, c->d_planes, c->stream);
                 nl = 1;
             } else {
                 cudaMemcpyAsync(c->d_planes, hp[slot], in_bytes, cudaMemcpyHostToDevice, c->stream);
@@ -648,7 +657,7 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
             int nf = 0;
             if (!rc)
                 rc = forward(c, net, c->d_planes, nb, T, c->d_probs, want_logits ? c->d_logits : nullptr,
-                             c->d_value, c->stream, &nf);
+                             c->d_value, c->stream, &nf, false, l5_direct);
             nl += nf;
             if (n.d.value_head) {
                 cudaMemcpyAsync(ho[slot], c->d_value, (size_t)nb * sizeof(float), cudaMemcpyDeviceToHost,

@@ -64,6 +64,10 @@ struct TcLayer {
 constexpr int kGatherPlanes = 32;
 int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
                   int nplanes, uint8_t *planes, cudaStream_t s);
+// The same planes written straight as the first layer's expanded input (the
+// rows launch_pack_planes_l5 makes from them, `halves` x 64 channels).
+int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
+                     int nplanes, int halves, __nv_bfloat16 *l5, cudaStream_t s);
 
 // Expanded 5x5 input: planes [B][C][361] bytes -> L5 BF16 rows with
 // halves*64 channels: channel dx*C + c = plane c at (y, x + dx - 2).

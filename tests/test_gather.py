@@ -160,3 +160,29 @@ def test_board_calls_feed_32_plane_nets(gpu_lib, weights, positions):
         pp = c.policy(positions["planes_p"][:n])
         vp = c.value(positions["planes_v"][:n])
     assert np.array_equal(pb, pp) and np.array_equal(vb, vp)
+
+
+@pytest.mark.parametrize("c_in", [32, 18])
+def test_bf16_board_calls_write_the_first_layer_input(gpu_lib, oracle_mod, positions, c_in):
+    """Tensor-core nets fed from boards take the first layer's expanded input
+    rows straight from the gather (no planes, no packing pass): the same
+    outputs, bit for bit, as from the reference gather's planes.  32 planes:
+    160 channels in three 64-channel halves; 18 planes: groups of 8 channels
+    that span two x shifts."""
+    lg, O = gpu_lib, oracle_mod
+    n = 40
+    sq, tm, mv = positions["squares"][:n], positions["meta"][:n, 0], positions["moves"][:n]
+    nets = {}
+    for vh in (0, 1):
+        fc = 256 if vh else 0
+        shape = dict(c_in=c_in, width1=128, width=128, n3x3=2, head_k=1, act=O.RELU, act_head=0,
+                     value_head=vh, fc_hidden=fc, value_map=0)
+        w = O.he_weights(O.make_net(shape), 7 + vh)
+        nets[vh] = lg.NetDesc(w, c_in, 128, 128, 2, 1, O.RELU, 0, vh, fc, 0, precision="bf16")
+    kw = dict(moves=mv) if c_in > 24 else {}
+    with lg.Context(policy=nets[0], value=nets[1], max_batch=16) as c:
+        pb, lb = c.policy_boards(sq, tm, 1.0, return_logits=True, **kw)
+        vb = c.value_boards(sq, tm, **kw)
+        pp, lp = c.policy(positions["planes_p"][:n, :c_in], 1.0, return_logits=True)
+        vp = c.value(positions["planes_v"][:n, :c_in])
+    assert np.array_equal(pb, pp) and np.array_equal(lb, lp) and np.array_equal(vb, vp)
