@@ -153,7 +153,8 @@ LG_API int lg_gather_device(const int8_t *squares, const int8_t *to_move, const 
 
 /* Host-buffer policy / value evaluation from boards (same encoding as
  * lg_gather_device): copies 362 bytes a position to the device (378 with
- * moves), gathers the net's input planes there, then runs the forward;
+ * moves), gathers the net's input planes there (for BF16 / FP8 nets straight
+ * into the first layer's input rows), then runs the forward;
  * results as lg_policy / lg_value.  moves may be NULL when the net reads at
  * most 24 planes.
  * Replaces: Network::get_scored_moves (Network.cpp:624-674) and
