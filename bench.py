@@ -616,8 +616,20 @@ def gather_throughput(lg, squares, to_move, dev, sp, reps=20):
             "all_32_planes_us_per_launch": ms32 * 1e3 / 2}
 
 
+def gather_run(reps):
+    """lg_gather_device alone on 8192 boards (gather_throughput), one JSON line."""
+    import torch
+    import leela_gb300 as lg
+    dev = torch.device("cuda", 0)
+    squares, to_move = load_boards()
+    sp = torch.cuda.current_stream(dev).cuda_stream
+    res = gather_throughput(lg, squares, to_move, dev, sp, reps=reps)
+    print(json.dumps({"gather_run": True, **res}), flush=True)
+
+
 def distill_config4(wp, wv, planes_p, planes_v, device):
-    """BASELINE config 4 on the fixture positions: the student is trained on
+    """The distilled student (64-wide net, entropy-gated fallback to the full
+    net) on the fixture positions: the student is trained on
     positions 0..895 (x8 symmetries), evaluated on 896..1023; labels are the
     full FP32 policy net's softmax and 2*mc_owner(64)-1.  Run at the
     specified teacher temperature 1 and, as an ablation, at 0.05 (the
@@ -642,8 +654,13 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--profile-run", action="store_true",
                     help="only the device-resident warm-up and timed steps (for ncu)")
+    ap.add_argument("--gather-run", action="store_true",
+                    help="only the gather timing: 8192 boards, 24 and 32 planes, both sets (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.gather_run:
+        gather_run(reps=5)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

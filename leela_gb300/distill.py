@@ -225,8 +225,8 @@ def calibrate_threshold(entropy_np, agree_np, target=0.97):
 def run_config4(planes_p, planes_v, position_index, mc_winrate, wp, wv, device=0,
                 train_positions=896, steps=3000, time_budget_s=30.0, teacher_temperature=1.0,
                 threshold=2.5, batch=256, seed=0):
-    """Distillation experiment (BASELINE config 4 at the scale of the fixture
-    positions): labels = the full FP32 policy net's softmax at
+    """Distillation experiment (a distilled 64-wide student with an entropy
+    gate, at the scale of the fixture positions): labels = the full FP32 policy net's softmax at
     teacher_temperature and 2*mc_owner-1 values; train on positions
     < train_positions (all symmetries), evaluate on the rest.  Reports the
     student's top-1 agreement with the full BF16 net, the fallback rate at

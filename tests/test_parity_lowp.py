@@ -126,3 +126,30 @@ def test_bf16_64_wide_net(gpu_lib, oracle_mod, positions, value_head):
             _, logits = c.policy(src, 1.0, return_logits=True)
             assert (logits.argmax(1) == ref.argmax(1)).mean() >= 0.95
             assert rel_logit_err(logits, ref).max() <= 5e-2
+
+
+@pytest.mark.parametrize("c_in", [24, 18])
+def test_bf16_planes_with_other_byte_values(gpu_lib, oracle_mod, positions, c_in):
+    """Plane bytes other than 0/1 reach the first layer exactly: doubling
+    plane 1's bytes gives, bit for bit, what doubling plane 1's first-layer
+    weights gives (x2 is exact in FP32 and in BF16).  The two calls take the
+    packing kernel's two paths (byte conversion; 0/1 bit masks)."""
+    lg, O = gpu_lib, oracle_mod
+    n = 24
+    shape = dict(c_in=c_in, width1=128, width=128, n3x3=2, head_k=1, act=O.RELU, act_head=0,
+                 value_head=0, fc_hidden=0, value_map=0)
+    w = O.he_weights(O.make_net(shape), 11)
+    w2 = w.copy()
+    w2[:128 * c_in * 25].reshape(128, c_in, 25)[:, 1, :] *= 2
+    planes = np.ascontiguousarray(positions["planes_p"][:n, :c_in])
+    doubled = planes.copy()
+    doubled[:, 1] *= 2
+    assert doubled.max() == 2
+
+    def desc(ww):
+        return lg.NetDesc(ww, c_in, 128, 128, 2, 1, O.RELU, 0, 0, precision="bf16")
+
+    with lg.Context(policy=desc(w), max_batch=32) as a, lg.Context(policy=desc(w2), max_batch=32) as b:
+        _, la = a.policy(doubled, 1.0, return_logits=True)
+        _, lb = b.policy(planes, 1.0, return_logits=True)
+    assert np.array_equal(la, lb)
