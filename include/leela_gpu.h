@@ -38,6 +38,7 @@ extern "C" {
 #define LG_FP32 0 /* plain FP32: the drop-in path */
 #define LG_BF16 1 /* BF16 activations and weights, FP32 accumulate (tcgen05) */
 #define LG_FP8W 2 /* E4M3 weights with per-output-channel FP32 scales, BF16 activations */
+#define LG_FP16 3 /* FP16 activations and weights, FP32 accumulate (tcgen05, same rate as BF16) */
 
 #define LG_ACT_ELU 0  /* x > 0 ? x : exp(x) - 1 (Network.cpp:382-383) */
 #define LG_ACT_RELU 1
@@ -57,8 +58,9 @@ extern "C" {
  * Network.cpp:54-137), then for value nets W1[fc_hidden][361], b1, W2, b2.
  * The library copies what it needs; the caller keeps ownership.
  *
- * LG_BF16 / LG_FP8W need c_in <= 32, width1 == width, width in {64, 128}
- * and head_k == 1. */
+ * LG_BF16 / LG_FP16 / LG_FP8W need c_in <= 32, width1 == width, width in
+ * {64, 128} and head_k == 1.  LG_FP16 keeps 10 mantissa bits against
+ * BF16's 7 (its range ends at 65504). */
 typedef struct lg_net_desc {
     int c_in;
     int width1;
@@ -206,9 +208,11 @@ LG_API int lg_stats(lg_ctx *ctx, long long *kernel_launches, long long *batches)
  * the library, held by every GPU that loads it until the process exits.
  *   - B is limited to 4 positions per call; larger B, or a net whose
  *     scratch would not fit, is rejected with LG_ERR_ARG and a message.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream
- *     capture.
+ *   - lg_create looks up the array's device address (cudaGetSymbolAddress)
+ *     for its device when the context has an FP32 policy net, so calls
+ *     only read that cached address.  (Were that lookup not done, the
+ *     first call on a device would make it; such a first call should come
+ *     before any stream capture.)
  *   - Every call, on every context, shares the one array: calls whose work
  *     overlaps on the GPU (different streams, or different host threads
  *     without ordering) race on it.  Nothing in it needs to start at zero.
@@ -217,22 +221,26 @@ LG_API int lg_policy_device_static(lg_ctx *ctx, const uint8_t *planes, int B, fl
                                    float *probs, float *logits, void *stream);
 
 /* Autotuner.  For every power-of-two batch bucket up to max_batch, times the
- * context's tensor-core nets with each kernel choice for the 3x3 layers
- * (0: one launch per layer with 256-row tiles on the transposed kernel,
- * 1: one launch per layer with 128-row tiles, which put twice as many CTAs
- * on a small batch, 2: all 3x3 layers in one persistent cooperative launch,
- * 3: as 2 with the 5x5 first layer in the same launch) and for the first
- * layer (0: 256-row, 1: 128-row tiles; unused by choice 3) and keeps the
- * fastest.  With a cache path, a table saved for the same device, SM count
- * and net shapes is loaded instead (unless force), and a new table is saved
- * there (written to a temporary file and renamed).  Without tuning every
- * bucket uses the 256-row kernel.  No reference counterpart (the OpenCL
- * backend reads a fixed cfg_rowtiles, OpenCL.cpp:634-646).
- * lg_tuning reports the choice for batch B; it returns 1 once tuned, 0 if
- * not, < 0 on error. */
+ * context's nets with each kernel choice for the 3x3 layers of the
+ * tensor-core nets (0: one launch per layer with 256-row tiles on the
+ * transposed kernel, 1: one launch per layer with 128-row tiles, which put
+ * twice as many CTAs on a small batch, 2: all 3x3 layers in one persistent
+ * cooperative launch, 3: as 2 with the 5x5 first layer in the same launch),
+ * for the first layer (0: 256-row, 1: 128-row tiles; unused by choices 3
+ * and 4), and -- for buckets of at most 8 positions -- choice 4: every layer
+ * of the net in one small-batch launch (FP32 nets: 0 = the generic per-layer
+ * FP32 kernels, 4 = the small-batch kernel), and keeps the fastest.  With a
+ * cache path, a table saved for the same device, SM count and net shapes is
+ * loaded instead (unless force), and a new table is saved there (written to
+ * a temporary file and renamed).  Without tuning, buckets of at most 8
+ * positions use choice 4 and larger ones choice 0.  No reference
+ * counterpart (the OpenCL backend reads a fixed cfg_rowtiles,
+ * OpenCL.cpp:634-646).  lg_tuning reports the choice for batch B; it returns
+ * 1 once tuned, 0 if not, < 0 on error. */
 LG_API int lg_autotune(lg_ctx *ctx, const char *cache_path, int force);
 LG_API int lg_tuning(lg_ctx *ctx, int B, int *variant_3x3, int *variant_first);
-/* Sets the kernel choice of B's bucket by hand (3x3: 0-2, first: 0-1). */
+/* Sets the kernel choice of B's bucket by hand (3x3: 0-4, first: 0-1); a
+ * net that choice 4 does not cover runs its per-layer kernels. */
 LG_API int lg_set_tuning(lg_ctx *ctx, int B, int variant_3x3, int variant_first);
 
 /* ---------------------------------------------------------------------
@@ -287,7 +295,8 @@ LG_API int lg_student_forward(lg_student *st, const uint8_t *planes, int B, floa
 #define LG_PROF_TC_TRUNK 5 /* persistent kernel running all 3x3 layers (incl. the fused head) */
 #define LG_PROF_PACK 6     /* tensor-core plane packing (planes -> expanded BF16 rows) */
 #define LG_PROF_TAIL 7     /* softmax, value FC1 + final */
-#define LG_PROF_KINDS 8
+#define LG_PROF_LAT 8      /* small-batch kernel: a whole net in one launch */
+#define LG_PROF_KINDS 9
 LG_API int lg_profile(lg_ctx *ctx, int enable);
 LG_API int lg_profile_read(lg_ctx *ctx, int kind, long long *launches, double *total_ms);
 

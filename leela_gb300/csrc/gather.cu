@@ -51,7 +51,8 @@ __device__ __forceinline__ int nbr(int p, int k) {
 }
 
 // union-find over the points of one board (shared memory); par[x] <= x,
-// and parents only decrease
+// and parents only decrease.  A path to the root strictly decreases, so it
+// has at most x < kPoints steps: the loop bound is never what ends it.
 __device__ __forceinline__ int find_root(const volatile int *par, int x) {
     for (int i = 0; i < kPoints && par[x] != x; ++i) x = par[x];
     return x;
@@ -59,7 +60,10 @@ __device__ __forceinline__ int find_root(const volatile int *par, int x) {
 
 // joins the trees of a and b: the larger root is linked under the smaller
 // (atomicMin); if it stopped being a root meanwhile, the atomicMin has moved
-// its link and the join goes on from the parent it had
+// its link and the join goes on from the parent it had.  Every retry starts
+// from two roots below the previous larger root (both roots are at most the
+// parent found, which is below it), so there are fewer than kPoints
+// rounds: the bound of 4 * kPoints is never what ends the loop.
 __device__ void unite(int *par, int a, int b) {
     for (int i = 0; i < 4 * kPoints; ++i) {
         a = find_root(par, a);
@@ -79,13 +83,14 @@ __device__ void unite(int *par, int a, int b) {
 // WHICH: 0 = policy planes, 1 = value planes; EXTRA: planes 24..31 wanted
 // (the ladder reader's code and shared lists stay out of the 24-plane
 // kernel); L5: write the first layer's expanded input rows (l5, `halves` x 64
-// BF16 channels a row) instead of the planes
+// 16-bit channels a row, 1.0 encoded as `one`: 0x3F80 for BF16, 0x3C00 for
+// FP16) instead of the planes
 template <int WHICH, bool EXTRA, bool L5>
 __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict__ squares,
                                                      const int8_t *__restrict__ to_move,
                                                      const int32_t *__restrict__ moves, int B,
                                                      int nplanes, uint8_t *__restrict__ planes, int halves,
-                                                     uint4 *__restrict__ l5) {
+                                                     uint32_t one, uint4 *__restrict__ l5) {
     constexpr bool extra = EXTRA;
     constexpr int kCand = extra ? 2 * kPoints : 1;
     __shared__ uint32_t rowc[2][kBoard];  // row bitboard: bit x of rowc[c][y] = stone of colour c at (y, x)
@@ -317,8 +322,8 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
     if (L5) {
         // Row r = y * 19 + x of the board's 399 L5 rows (y = 19, 20: zero
         // pad rows), channel dx * nplanes + c = plane c at (y, x + dx - 2),
-        // zero off the board and from channel 5 * nplanes on; BF16 1.0 is
-        // 0x3F80.  One 16-byte group of 8 channels per thread and step.
+        // zero off the board and from channel 5 * nplanes on; 1.0 is `one`.
+        // One 16-byte group of 8 channels per thread and step.
         if (on) pbits[p] = bits;
         __syncthreads();
         const int groups = halves * 8;
@@ -335,14 +340,14 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
                         const uint32_t v = pbits[y * kBoard + sx] >> c0;
 #pragma unroll
                         for (int j = 0; j < 4; ++j)
-                            w[j] = ((v >> (2 * j)) & 1u) * 0x3F80u | ((v >> (2 * j + 1)) & 1u) * 0x3F800000u;
+                            w[j] = ((v >> (2 * j)) & 1u) * one | ((v >> (2 * j + 1)) & 1u) * (one << 16);
                     }
                 } else {
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         const int ch = g * 8 + j, dx = ch / nplanes, c = ch - dx * nplanes, sx = x + dx - 2;
                         if (dx < 5 && sx >= 0 && sx < kBoard && ((pbits[y * kBoard + sx] >> c) & 1u))
-                            w[j >> 1] |= (j & 1) ? 0x3F800000u : 0x3F80u;
+                            w[j >> 1] |= (j & 1) ? (one << 16) : one;
                     }
                 }
             }
@@ -357,17 +362,17 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
 
 template <bool L5>
 static void launch_gather_kernel(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B,
-                                 int which, int nplanes, uint8_t *planes, int halves, uint4 *l5,
+                                 int which, int nplanes, uint8_t *planes, int halves, uint32_t one, uint4 *l5,
                                  cudaStream_t s) {
     const bool extra = nplanes > 24;
     if (which == 0 && extra)
-        gather_kernel<0, true, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, l5);
+        gather_kernel<0, true, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
     else if (which == 0)
-        gather_kernel<0, false, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, l5);
+        gather_kernel<0, false, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
     else if (extra)
-        gather_kernel<1, true, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, l5);
+        gather_kernel<1, true, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
     else
-        gather_kernel<1, false, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, l5);
+        gather_kernel<1, false, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
 }
 
 static int check_gather(int B, int which, int nplanes, const int32_t *moves) {
@@ -382,12 +387,12 @@ static int check_gather(int B, int which, int nplanes, const int32_t *moves) {
 int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
                   int nplanes, uint8_t *planes, cudaStream_t s) {
     if (int rc = check_gather(B, which, nplanes, moves)) return rc;
-    if (B > 0) launch_gather_kernel<false>(squares, to_move, moves, B, which, nplanes, planes, 0, nullptr, s);
+    if (B > 0) launch_gather_kernel<false>(squares, to_move, moves, B, which, nplanes, planes, 0, 0u, nullptr, s);
     return LG_OK;
 }
 
 int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
-                     int nplanes, int halves, __nv_bfloat16 *l5, cudaStream_t s) {
+                     int nplanes, int halves, bool f16, __nv_bfloat16 *l5, cudaStream_t s) {
     if (int rc = check_gather(B, which, nplanes, moves)) return rc;
     if (halves < 1 || 5 * nplanes > halves * 64) {
         lg_set_error("gather: %d planes need %d L5 channels, the layer has %d", nplanes, 5 * nplanes, halves * 64);
@@ -395,7 +400,7 @@ int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t
     }
     if (B > 0)
         launch_gather_kernel<true>(squares, to_move, moves, B, which, nplanes, nullptr, halves,
-                                   reinterpret_cast<uint4 *>(l5), s);
+                                   f16 ? 0x3C00u : 0x3F80u, reinterpret_cast<uint4 *>(l5), s);
     return LG_OK;
 }
 

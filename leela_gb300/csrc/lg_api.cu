@@ -1,6 +1,7 @@
 // lg_api.cu -- the C ABI (include/leela_gpu.h): contexts, weight upload and
 // layout, forward orchestration, CUDA-graph cache, batching server.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <atomic>
@@ -51,7 +52,7 @@ bool valid_desc(const lg_net_desc *d) {
            d->n3x3 < kMaxConv - 2 && (d->head_k == 1 || d->head_k == 3) &&
            (d->act == LG_ACT_ELU || d->act == LG_ACT_RELU) &&
            (!d->value_head || (d->fc_hidden > 0 && d->fc_hidden <= 4096)) &&
-           d->precision >= LG_FP32 && d->precision <= LG_FP8W;
+           d->precision >= LG_FP32 && d->precision <= LG_FP16;
 }
 
 std::vector<Shape> conv_shapes(const lg_net_desc *d) {
@@ -96,6 +97,10 @@ struct Net {
     float head_b = 0.0f;
     float *w1s = nullptr, *b1 = nullptr, *w2 = nullptr;
     float b2 = 0.0f;
+    // small-batch path (latency.cu): per conv layer and the head, weights
+    // [8][cg][k*k][cout] with each split padded to `slice` floats
+    bool lat_ok = false;
+    std::vector<LatConv> lat;
     // tensor-core path
     std::vector<TcConv> tc;
     float *tc_head_w = nullptr;  // [width]
@@ -116,6 +121,11 @@ struct lg_ctx {
     // FP32 buffers
     float *act[2] = {nullptr, nullptr};
     float *partial = nullptr;
+    // small-batch path: partial sums, counters (zero between launches),
+    // value-head partials
+    float *lat_part = nullptr;
+    int *lat_cnt = nullptr;
+    float *lat_fcv = nullptr;
     // tensor-core buffers
     __nv_bfloat16 *l3[2] = {nullptr, nullptr};
     __nv_bfloat16 *l5 = nullptr;
@@ -143,9 +153,12 @@ struct lg_ctx {
     std::vector<cudaEvent_t> event_pool;
     long long prof_launches[LG_PROF_KINDS] = {};
     double prof_ms[LG_PROF_KINDS] = {};
-    // Kernel choice per power-of-two batch bucket (index = log2) for the
-    // 128-wide tensor-core layers: [bucket][0] 3x3 layers (and fused head),
-    // [bucket][1] first layer; 0 = 256-row transposed kernel, 1 = 128-row.
+    // Kernel choice per power-of-two batch bucket (index = log2): [bucket][0]
+    // 3x3 layers (and fused head) of the 128-wide tensor-core nets -- 0 =
+    // 256-row transposed kernel, 1 = 128-row, 2 / 3 = persistent trunk --
+    // or 4 = the whole net in the small-batch kernel (buckets up to
+    // kLatMaxB, nets it supports; the default there); [bucket][1] first
+    // layer, 0 = 256-row, 1 = 128-row.
     int tc_variant[17][2] = {};
     bool tuned = false;
     std::atomic<long long> launches{0};
@@ -202,6 +215,21 @@ bool tc_supported(const lg_net_desc *d) {
            d->head_k == 1 && d->n3x3 >= 1;
 }
 
+// A weight rounded to nearest even in the tensor-core operand type (FP16 for
+// LG_FP16 nets, else BF16), as its 16 bits in a BF16-typed slot.
+__nv_bfloat16 operand16(float v, bool f16) {
+    if (!f16) return __float2bfloat16(v);
+    const __half h = __float2half_rn(v);
+    __nv_bfloat16 b;
+    std::memcpy(&b, &h, sizeof b);
+    return b;
+}
+
+// The value of that rounding, back in FP32 (weights the FP32 heads use).
+float round_operand(float v, bool f16) {
+    return f16 ? __half2float(__float2half_rn(v)) : __bfloat162float(__float2bfloat16(v));
+}
+
 // E4M3 round-to-nearest-even with saturation at 448 (the quantiser of the
 // FP8-weight variant; E4M3 values are exact in BF16).
 float e4m3_round(float x) {
@@ -218,13 +246,60 @@ float e4m3_round(float x) {
     return x < 0 ? -q : q;
 }
 
+// The small-batch kernel's weight layout, for the shapes it covers: every
+// layer's input channels split 8 ways (cin % 8 == 0, and after the first
+// layer 4-channel groups: cin % 32 == 0), at most 128 output channels (even,
+// or the head's one), 1x1 / 3x3 / 5x5 filters, the staged input and the
+// weight slice within the kernel's shared memory, and for value nets an FC
+// layer of at most 256 units in 8 equal slices.  Other nets keep the
+// generic path at every batch size.
+int build_lat(lg_ctx *c, Net &n, const std::vector<std::vector<float>> &Wraw) {
+    const lg_net_desc &d = n.d;
+    const int nl = (int)n.shapes.size();
+    bool ok = nl <= kLatMaxLayers && (!d.value_head || (d.fc_hidden % kLatSplits == 0 && d.fc_hidden <= 256));
+    for (int l = 0; l < nl && ok; ++l) {
+        const Shape sh = n.shapes[l];
+        const int cg = sh.cin / kLatSplits;
+        const int slice = (cg * sh.k * sh.k * sh.cout + 3) & ~3;
+        ok = sh.cin % kLatSplits == 0 && (l == 0 || cg % 4 == 0) && cg <= kLatMaxCg && cg * sh.k <= kLatMaxCg * 5 &&
+             (sh.k == 1 || sh.k == 3 || sh.k == 5) && sh.cout <= 128 && (sh.cout % 2 == 0 || sh.cout == 1) &&
+             slice <= kLatSliceMax;
+    }
+    if (!ok) return LG_OK;
+    for (int l = 0; l < nl; ++l) {
+        const Shape sh = n.shapes[l];
+        const int kk = sh.k * sh.k, cg = sh.cin / kLatSplits;
+        LatConv L{};
+        L.k = sh.k;
+        L.cin = sh.cin;
+        L.cout = sh.cout;
+        L.cg = cg;
+        L.slice = (cg * kk * sh.cout + 3) & ~3;
+        std::vector<float> w((size_t)kLatSplits * L.slice, 0.0f);
+        for (int sp = 0; sp < kLatSplits; ++sp)
+            for (int cl = 0; cl < cg; ++cl)
+                for (int t = 0; t < kk; ++t)
+                    for (int o = 0; o < sh.cout; ++o)
+                        w[(size_t)sp * L.slice + ((size_t)cl * kk + t) * sh.cout + o] =
+                            Wraw[l][((size_t)o * sh.cin + sp * cg + cl) * kk + t];
+        float *dw;
+        int rc = upload(c, &dw, w);
+        if (rc) return rc;
+        L.w = dw;
+        L.bias = l + 1 < nl ? n.bias[l] : nullptr;
+        n.lat.push_back(L);
+    }
+    n.lat_ok = true;
+    return LG_OK;
+}
+
 int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
     if (!valid_desc(d) || !d->weights) {
         lg_set_error("invalid network description");
         return LG_ERR_ARG;
     }
     if (d->precision != LG_FP32 && !tc_supported(d)) {
-        lg_set_error("BF16/FP8 paths need c_in <= 32, width1 == width in {64,128}, head_k == 1");
+        lg_set_error("BF16/FP16/FP8 paths need c_in <= 32, width1 == width in {64,128}, head_k == 1");
         return LG_ERR_ARG;
     }
     n.d = *d;
@@ -266,9 +341,12 @@ int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
             for (int t = 0; t < kk; ++t) wh[(size_t)t * hs.cin + ci] = Wraw.back()[(size_t)ci * kk + t];
         if ((rc = upload(c, &n.head_w, wh))) return rc;
         n.head_b = Braw.back()[0];
+        if ((rc = build_lat(c, n, Wraw))) return rc;
     } else {
-        // ---- tensor-core layouts: [tap][half][N][64] BF16, K-major rows.
+        // ---- tensor-core layouts: [tap][half][N][64] 16-bit operands (BF16,
+        // or FP16 for LG_FP16), K-major rows.
         bool fp8 = d->precision == LG_FP8W;
+        const bool f16 = d->precision == LG_FP16;
         for (int l = 0; l < ntrunk; ++l) {
             auto s = n.shapes[l];
             TcConv t{};
@@ -306,7 +384,7 @@ int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
                         if (fp8) v = e4m3_round(v / scale[o]);
                         int half = kidx / 64;
                         wb[(((size_t)tap * t.halves + half) * s.cout + o) * 64 + kidx % 64] =
-                            __float2bfloat16(v);
+                            operand16(v, f16);
                     }
             if ((rc = upload(c, &t.w, wb)) || (rc = upload(c, &t.bias, Braw[l]))) return rc;
             if (fp8 && (rc = upload(c, &t.scale, scale))) return rc;
@@ -331,9 +409,10 @@ int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
                                            cudaMemcpyDeviceToDevice));
             }
         }
-        // Fused 1x1 head weights, BF16-rounded as the precision states.
+        // Fused 1x1 head weights, rounded to the operand type as the
+        // precision states.
         std::vector<float> hw(Wraw.back());
-        for (auto &v : hw) v = __bfloat162float(__float2bfloat16(v));
+        for (auto &v : hw) v = round_operand(v, f16);
         if ((rc = upload(c, &n.tc_head_w, hw))) return rc;
         n.head_b = Braw.back()[0];
     }
@@ -346,15 +425,15 @@ int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
         std::vector<float> w1s((size_t)slices * kPoints * U, 0.0f), b1(W1 + (size_t)H * kPoints,
                                                                       W1 + (size_t)H * kPoints + H);
         std::vector<float> w2(W1 + (size_t)H * kPoints + H, W1 + (size_t)H * kPoints + 2 * H);
-        bool lowp = d->precision != LG_FP32;
+        const bool lowp = d->precision != LG_FP32, f16 = d->precision == LG_FP16;
         for (int o = 0; o < H; ++o)
             for (int i = 0; i < kPoints; ++i) {
                 float v = W1[(size_t)o * kPoints + i];
-                if (lowp) v = __bfloat162float(__float2bfloat16(v));
+                if (lowp) v = round_operand(v, f16);
                 w1s[((size_t)(o / U) * kPoints + i) * U + o % U] = v;
             }
         if (lowp)
-            for (auto &v : w2) v = __bfloat162float(__float2bfloat16(v));
+            for (auto &v : w2) v = round_operand(v, f16);
         n.b2 = W1[(size_t)H * kPoints + 2 * H];
         if ((rc = upload(c, &n.w1s, w1s)) || (rc = upload(c, &n.b1, b1)) ||
             (rc = upload(c, &n.w2, w2)))
@@ -408,8 +487,56 @@ struct ProfScope {
     }
 };
 
+// Bucket index of batch B (log2 of the next power of two).
+int bucket_of(int B) {
+    int bl = 0;
+    while ((1 << bl) < B && bl < 16) ++bl;
+    return bl;
+}
+
+bool use_lat(lg_ctx *c, const Net &n, int B) {
+    return n.lat_ok && B <= kLatMaxB && c->lat_part && c->tc_variant[bucket_of(B)][0] == 4;
+}
+
+int forward_lat(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs, float *logits_out,
+                float *value, cudaStream_t s, int *nlaunch, bool prof) {
+    const lg_net_desc &d = n.d;
+    LatParams p{};
+    p.nl = (int)n.lat.size();
+    for (int l = 0; l < p.nl; ++l) p.L[l] = n.lat[l];
+    p.B = B;
+    p.c_in = d.c_in;
+    p.act = d.act;
+    p.act_head = d.act_head;
+    p.head_b = n.head_b;
+    p.planes = planes;
+    p.part = c->lat_part;
+    p.cnt = c->lat_cnt;
+    p.err = c->d_err;
+    p.temperature = T;
+    p.probs = probs;
+    p.logits_out = logits_out;
+    p.value_head = d.value_head;
+    p.w1s = n.w1s;
+    p.b1 = n.b1;
+    p.w2 = n.w2;
+    p.b2 = n.b2;
+    p.H = d.fc_hidden;
+    p.value_map = d.value_map;
+    p.value = value;
+    p.fcv = c->lat_fcv;
+    int rc;
+    {
+        ProfScope ps(c, prof, LG_PROF_LAT, s);
+        rc = launch_lat_f32(p, c->sm_count, s);
+    }
+    *nlaunch = 1;
+    return rc;
+}
+
 int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
                  float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof) {
+    if (use_lat(c, n, B)) return forward_lat(c, n, planes, B, T, probs, logits_out, value, s, nlaunch, prof);
     const lg_net_desc &d = n.d;
     int L = 0;
     {
@@ -454,11 +581,12 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
                float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof,
                bool l5_ready = false) {
     const lg_net_desc &d = n.d;
+    const int f16 = d.precision == LG_FP16 ? 1 : 0;
     int L = 0;
     const TcConv &first = n.tc[0];
     if (!l5_ready) {
         ProfScope ps(c, prof, LG_PROF_PACK, s);
-        launch_pack_planes_l5(planes, B, d.c_in, first.halves, c->l5, s);
+        launch_pack_planes_l5(planes, B, d.c_in, first.halves, f16 != 0, c->l5, s);
         ++L;
     }
     float *lg = logits_out ? logits_out : c->d_logits;
@@ -493,6 +621,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
             tt.act = d.act;
             tt.rows = B * kL3Board;
             tt.nl = (int)n.tc.size() - 1;
+            tt.f16 = f16;
             int rc;
             {
                 ProfScope ps(c, prof, LG_PROF_TC_TRUNK, s);
@@ -514,6 +643,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
         tl.in_kind = (l == 0) ? 1 : 0;
         tl.rows = (l == 0) ? B * kL5Board : B * kL3Board;
         tl.variant = (l == 0) ? var1 : var3;
+        tl.f16 = f16;
         __nv_bfloat16 *out = (l == 0) ? c->l3[0] : c->l3[cur ^ 1];
         int rc;
         {
@@ -648,7 +778,8 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
                 const int which = net == LG_NET_POLICY ? 0 : 1;
                 // tensor-core nets: the gather writes the first layer's
                 // expanded input rows itself (no planes, no packing pass)
-                rc = l5_direct ? launch_gather_l5(dsq, dtm, dmv, nb, which, n.d.c_in, n.tc[0].halves, c->l5, c->stream)
+                rc = l5_direct ? launch_gather_l5(dsq, dtm, dmv, nb, which, n.d.c_in, n.tc[0].halves,
+                                                  n.d.precision == LG_FP16, c->l5, c->stream)
                                : launch_gather(dsq, dtm, dmv, nb, which, n.d.c_in, c->d_planes, c->stream);
                 nl = 1;
             } else {
@@ -889,6 +1020,10 @@ void worker_main(lg_ctx *c) {
     }
 }
 
+// Device address of the static scratch array of lg_policy_device_static on
+// `device` (current), resolved once per device and cached (defined below).
+int static_scratch_resolve(int device, void **out);
+
 }  // namespace
 
 // ================================================================ C ABI
@@ -1005,6 +1140,25 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
         if (cudaMemset(c->l3[0], 0, mb * kL3Board * max_tc_l3 * 2) != cudaSuccess ||
             cudaMemset(c->l3[1], 0, mb * kL3Board * max_tc_l3 * 2) != cudaSuccess)
             return fail(LG_ERR_CUDA);
+    }
+    bool any_lat = false;
+    for (int i = 0; i < 2; ++i) any_lat |= c->nets[i].present && c->nets[i].lat_ok;
+    if (any_lat) {
+        if ((rc = lat_init_device()) || (rc = dev_alloc(c, &c->lat_part, lat_part_floats())) ||
+            (rc = dev_alloc(c, &c->lat_cnt, (size_t)kLatCntInts)) ||
+            (rc = dev_alloc(c, &c->lat_fcv, (size_t)kLatMaxB * kLatSplits)))
+            return fail(rc);
+        if (cudaMemset(c->lat_cnt, 0, sizeof(int) * kLatCntInts) != cudaSuccess) return fail(LG_ERR_CUDA);
+    }
+    // small batches default to the small-batch kernel (nets it does not
+    // cover keep their generic path)
+    for (int b = 0; (1 << b) <= kLatMaxB; ++b) c->tc_variant[b][0] = 4;
+    // An FP32 policy net can be evaluated by lg_policy_device_static: look
+    // up its static array's device address now, so that its calls only read
+    // the cached pointer.
+    if (policy && policy->precision == LG_FP32) {
+        void *sp = nullptr;
+        if ((rc = static_scratch_resolve(device, &sp))) return fail(rc);
     }
     c->planes_c = max_c_in;
     if ((rc = dev_alloc(c, &c->d_planes, mb * max_c_in * kPoints)) ||
@@ -1227,6 +1381,30 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
+namespace {
+// Once per device, with that device current: the device address of the
+// array (its name in host code is only a host-side stand-in).  Contexts with
+// an FP32 policy net do this when they are created.
+int static_scratch_resolve(int device, void **out) {
+    if (device < 0 || device >= kStaticMaxDevices) {
+        lg_set_error("static scratch: device %d out of range", device);
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(g_static_mu);
+    if (!g_static_ptr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p) {
+            lg_set_error("cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
+            return LG_ERR_CUDA;
+        }
+        g_static_ptr[device] = p;
+    }
+    *out = g_static_ptr[device];
+    return LG_OK;
+}
+}  // namespace
+
 extern "C" int lg_policy_device_static(lg_ctx *c, const uint8_t *planes, int B, float temperature,
                                        float *probs, float *logits, void *stream) {
     if (!c || !planes || !probs || !(temperature > 0.0f) || B < 0) {
@@ -1244,6 +1422,8 @@ extern "C" int lg_policy_device_static(lg_ctx *c, const uint8_t *planes, int B, 
         return LG_ERR_ARG;
     }
     if (B == 0) return LG_OK;
+    int rc = check_fault(c);
+    if (rc) return rc;
     // Scratch layout: activations x2, split-K partials, logits.
     size_t max_ch = (size_t)n.d.c_in, max_partial = 0;
     for (auto &sh : n.shapes) {
@@ -1260,27 +1440,11 @@ extern "C" int lg_policy_device_static(lg_ctx *c, const uint8_t *planes, int B, 
                      need, B, kStaticScratchBytes);
         return LG_ERR_ARG;
     }
-    if (c->device < 0 || c->device >= kStaticMaxDevices) {
-        lg_set_error("lg_policy_device_static: device %d out of range", c->device);
-        return LG_ERR_ARG;
-    }
     LG_CUDA_TRY(cudaSetDevice(c->device));
-    void *base;
-    {
-        // Once per device, with that device current: the device address of
-        // the array (its name in host code is only a host-side stand-in).
-        std::lock_guard<std::mutex> g(g_static_mu);
-        if (!g_static_ptr[c->device]) {
-            void *p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-            if (e != cudaSuccess || !p) {
-                lg_set_error("cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
-                return LG_ERR_CUDA;
-            }
-            g_static_ptr[c->device] = p;
-        }
-        base = g_static_ptr[c->device];
-    }
+    // The address was resolved when the context was created (lg_create); a
+    // lookup here happens only if that did not run.
+    void *base = nullptr;
+    if ((rc = static_scratch_resolve(c->device, &base))) return rc;
     unsigned char *b = static_cast<unsigned char *>(base);
     float *act[2] = {reinterpret_cast<float *>(b), reinterpret_cast<float *>(b + act_bytes)};
     float *partial = reinterpret_cast<float *>(b + 2 * act_bytes);
@@ -1288,18 +1452,21 @@ extern "C" int lg_policy_device_static(lg_ctx *c, const uint8_t *planes, int B, 
     cudaStream_t s = (cudaStream_t)stream;
     const lg_net_desc &d = n.d;
     launch_pack_planes_f32(planes, B, d.c_in, act[0], s);
+    long long nlaunch = 1;
     int cur = 0;
     const int ntrunk = (int)n.shapes.size() - 1;
     for (int l = 0; l < ntrunk; ++l) {
         auto sh = n.shapes[l];
         launch_conv_f32(act[cur], n.wt[l], n.bias[l], act[cur ^ 1], B, sh.cin, sh.cout, sh.k, d.act,
                         partial, s);
+        nlaunch += conv_f32_partial_floats(B, sh.cin, sh.cout, sh.k) ? 2 : 1;
         cur ^= 1;
     }
     auto hs = n.shapes.back();
     launch_head_conv_f32(act[cur], n.head_w, n.head_b, B, hs.cin, hs.k, d.act_head, d.act, lg, s);
     HeadIn h{lg, 1, 0, 0.0f, 0, d.act, nullptr};
     launch_softmax(h, B, temperature, probs, s);
+    c->launches += nlaunch + 2;  // + head conv, softmax
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         lg_set_error("lg_policy_device_static: launch failed: %s", cudaGetErrorString(e));
@@ -1348,7 +1515,7 @@ bool load_tuning(lg_ctx *c, const char *path) {
         if (pos == std::string::npos) continue;
         int a = 0, d = 0;
         if (sscanf(text.c_str() + pos + strlen(pat), "%d, %d", &a, &d) != 2) return false;
-        if (a < 0 || a > 3 || d < 0 || d > 1) return false;
+        if (a < 0 || a > 4 || d < 0 || d > 1) return false;
         table[b][0] = a;
         table[b][1] = d;
     }
@@ -1356,14 +1523,14 @@ bool load_tuning(lg_ctx *c, const char *path) {
     return true;
 }
 
-int save_tuning(lg_ctx *c, const char *path, const double (*ms)[7]) {
+int save_tuning(lg_ctx *c, const char *path, const double (*ms)[8]) {
     std::string tmp = std::string(path) + ".tmp";
     FILE *f = fopen(tmp.c_str(), "w");
     if (!f) {
         lg_set_error("cannot write %s", tmp.c_str());
         return LG_ERR_ARG;
     }
-    fprintf(f, "{\n \"key\": \"%s\",\n \"order\": \"[3x3 layers: 0 = 256-row transposed per layer, 1 = 128-row per layer, 2 = persistent trunk, 3 = persistent trunk with the first layer in it; first layer: 0 = 256-row, 1 = 128-row]; ms_per_forward for (3x3, first) = (0,0) (1,0) (2,0) (0,1) (1,1) (2,1) (3,0)\",\n \"table\": {",
+    fprintf(f, "{\n \"key\": \"%s\",\n \"order\": \"[3x3 layers: 0 = 256-row transposed per layer, 1 = 128-row per layer, 2 = persistent trunk, 3 = persistent trunk with the first layer in it, 4 = the whole net in one small-batch launch (FP32 nets: 0 = per-layer kernels, 4 = small-batch); first layer: 0 = 256-row, 1 = 128-row]; ms_per_forward for (3x3, first) = (0,0) (1,0) (2,0) (0,1) (1,1) (2,1) (3,0) (4,0), 0 = not timed\",\n \"table\": {",
             tune_key(c).c_str());
     bool first = true;
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16; ++b) {
@@ -1374,8 +1541,8 @@ int save_tuning(lg_ctx *c, const char *path, const double (*ms)[7]) {
     fprintf(f, "\n },\n \"ms_per_forward\": {");
     first = true;
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16; ++b) {
-        fprintf(f, "%s\n  \"%d\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f, %.4f]", first ? "" : ",", 1 << b,
-                ms[b][0], ms[b][1], ms[b][2], ms[b][3], ms[b][4], ms[b][5], ms[b][6]);
+        fprintf(f, "%s\n  \"%d\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f, %.4f, %.4f]", first ? "" : ",", 1 << b,
+                ms[b][0], ms[b][1], ms[b][2], ms[b][3], ms[b][4], ms[b][5], ms[b][6], ms[b][7]);
         first = false;
     }
     fprintf(f, "\n }\n}\n");
@@ -1395,9 +1562,12 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
         return LG_ERR_ARG;
     }
     std::lock_guard<std::mutex> g(c->mu);
-    bool any_tc = false;
-    for (int i = 0; i < 2; ++i) any_tc |= c->nets[i].present && c->nets[i].d.precision != LG_FP32;
-    if (!any_tc) return LG_OK;
+    bool any_tc = false, any_lat = false;
+    for (int i = 0; i < 2; ++i) {
+        any_tc |= c->nets[i].present && c->nets[i].d.precision != LG_FP32;
+        any_lat |= c->nets[i].present && c->nets[i].lat_ok;
+    }
+    if (!any_tc && !any_lat) return LG_OK;
     if (cache_path && !force && load_tuning(c, cache_path)) {
         for (auto &gr : c->graphs) cudaGraphExecDestroy(gr.second.first);
         c->graphs.clear();
@@ -1409,22 +1579,29 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
     LG_CUDA_TRY(cudaEventCreate(&e0));
     LG_CUDA_TRY(cudaEventCreate(&e1));
     LG_CUDA_TRY(cudaMemsetAsync(c->d_planes, 0, (size_t)c->max_batch * c->planes_c * kPoints, c->stream));
-    double ms[17][7] = {};
+    double ms[17][8] = {};
     int rc = LG_OK;
+    // (3x3, first) of timing slot v: the six per-layer / trunk pairs, the
+    // trunk with the first layer in it, the small-batch kernel
+    auto choice = [](int v, int &v3, int &v1) {
+        v3 = v < 6 ? v % 3 : (v == 6 ? 3 : 4);
+        v1 = v < 6 ? v / 3 : 0;
+    };
     for (int b = 0; (1 << b) <= c->max_batch && b <= 16 && rc == LG_OK; ++b) {
         const int B = 1 << b;
         double best = 1e30;
         int best_v = 0;
-        for (int v = 0; v < 7 && rc == LG_OK; ++v) {
-            c->tc_variant[b][0] = v < 6 ? v % 3 : 3;
-            c->tc_variant[b][1] = v < 6 ? v / 3 : 0;
+        for (int v = 0; v < 8 && rc == LG_OK; ++v) {
+            if (v == 7 && (B > kLatMaxB || !any_lat)) continue;
+            if (!any_tc && v != 0 && v != 7) continue;  // FP32 nets: per-layer or small-batch
+            choice(v, c->tc_variant[b][0], c->tc_variant[b][1]);
             const int reps = B >= 64 ? 5 : 20;
             float t = 0.0f;
             for (int it = 0; it < 2 + reps && rc == LG_OK; ++it) {
                 if (it == 2) cudaEventRecord(e0, c->stream);
                 for (int net = 0; net < 2 && rc == LG_OK; ++net) {
                     Net &n = c->nets[net];
-                    if (!n.present || n.d.precision == LG_FP32) continue;
+                    if (!n.present) continue;
                     int nl = 0;
                     rc = forward(c, net, c->d_planes, B, 1.0f, c->d_probs, nullptr, c->d_value, c->stream, &nl);
                 }
@@ -1439,8 +1616,7 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
                 best_v = v;
             }
         }
-        c->tc_variant[b][0] = best_v < 6 ? best_v % 3 : 3;
-        c->tc_variant[b][1] = best_v < 6 ? best_v / 3 : 0;
+        choice(best_v, c->tc_variant[b][0], c->tc_variant[b][1]);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1455,6 +1631,7 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
     c->graphs.clear();
     if (rc != LG_OK) {
         std::memset(c->tc_variant, 0, sizeof c->tc_variant);
+        for (int b = 0; (1 << b) <= kLatMaxB; ++b) c->tc_variant[b][0] = 4;
         return rc;
     }
     c->tuned = true;
@@ -1472,7 +1649,7 @@ extern "C" int lg_tuning(lg_ctx *c, int B, int *variant_3x3, int *variant_first)
 }
 
 extern "C" int lg_set_tuning(lg_ctx *c, int B, int variant_3x3, int variant_first) {
-    if (!c || B < 1 || variant_3x3 < 0 || variant_3x3 > 3 || variant_first < 0 || variant_first > 1) {
+    if (!c || B < 1 || variant_3x3 < 0 || variant_3x3 > 4 || variant_first < 0 || variant_first > 1) {
         lg_set_error("lg_set_tuning: bad arguments");
         return LG_ERR_ARG;
     }

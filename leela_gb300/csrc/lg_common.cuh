@@ -265,5 +265,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
            ((uint32_t)(M >> 4) << 24);
 }
 
+// The same with A/B as FP16 (operand format field 0) when f16 is set.  Both
+// operands of one MMA always have the same type.
+__host__ __device__ constexpr uint32_t idesc_16(int M, int N, bool f16) {
+    return f16 ? ((1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24)) : idesc_bf16(M, N);
+}
+
 }  // namespace ptx
 }  // namespace lg

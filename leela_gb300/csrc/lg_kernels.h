@@ -54,6 +54,7 @@ struct TcLayer {
     int in_kind;          // 0: L3 input (3x3); 1: L5 input (expanded 5x5 first layer)
     int rows;             // input rows processed (B * 400 or B * 399)
     int variant;          // for n == 128: 0 = 256-row transposed kernel, 1 = 128-row kernel
+    int f16 = 0;          // activations and weights are FP16 (else BF16)
 };
 
 // Input planes 0..nplanes-1 (nplanes <= kGatherPlanes) of the policy
@@ -66,12 +67,14 @@ int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *m
                   int nplanes, uint8_t *planes, cudaStream_t s);
 // The same planes written straight as the first layer's expanded input (the
 // rows launch_pack_planes_l5 makes from them, `halves` x 64 channels).
+// (BF16 rows, or FP16 when f16.)
 int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
-                     int nplanes, int halves, __nv_bfloat16 *l5, cudaStream_t s);
+                     int nplanes, int halves, bool f16, __nv_bfloat16 *l5, cudaStream_t s);
 
-// Expanded 5x5 input: planes [B][C][361] bytes -> L5 BF16 rows with
-// halves*64 channels: channel dx*C + c = plane c at (y, x + dx - 2).
-void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv_bfloat16 *out,
+// Expanded 5x5 input: planes [B][C][361] bytes -> L5 rows (BF16, or FP16
+// when f16) with halves*64 channels: channel dx*C + c = plane c at
+// (y, x + dx - 2).
+void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, bool f16, __nv_bfloat16 *out,
                            cudaStream_t s);
 // Writes the layer output (L3 rows) or, for the fused head, the head output
 // before its bias into parts[boards*361] (tc_head_parts() = 1 array).
@@ -101,6 +104,7 @@ struct TcTrunk {
     const void *w0 = nullptr;    // [5][2][128][64] BF16
     const float *bias0 = nullptr, *scale0 = nullptr;
     int rows5 = 0;
+    int f16 = 0;                 // activations and weights are FP16 (else BF16)
 };
 // flags: trunk_flag_ints(rows, rows5) ints of device scratch (reset by the launch).
 int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
@@ -110,6 +114,57 @@ size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves);
 int tc_init_device();
 // Head kernels for the tensor-core path (logits already produced by the
 // fused epilogue): same softmax / value FC as FP32.
+
+// ------------------------------------------- small-batch path (latency.cu)
+//
+// Every conv layer of a net (the head as a layer of one output channel) in
+// one cooperative launch for 1..kLatMaxB positions: units (board row, input
+// channel split) of 8 splits a layer, partial sums per split in FP32, added
+// by the consumer in a fixed order.  Weights per layer: [8][cg][k*k][cout]
+// FP32 (split s holds input channels s*cg .. s*cg + cg - 1), each split's
+// block padded to `slice` floats (a multiple of 4).
+constexpr int kLatMaxB = 8;
+constexpr int kLatSplits = 8;
+constexpr int kLatMaxRows = kLatMaxB * kBoard;
+constexpr int kLatMaxLayers = 16;
+constexpr int kLatMaxCg = 16;
+constexpr int kLatSliceMax = 16 * 9 * 128;  // floats of one split's weights
+// counters: [layer][row], then one per board for the value head, then the
+// exit counter
+constexpr int kLatCntFc = kLatMaxLayers * kLatMaxRows;
+constexpr int kLatCntExit = kLatCntFc + kLatMaxB;
+constexpr int kLatCntInts = kLatCntExit + 1;
+
+struct LatConv {
+    const float *w;     // [8][slice]
+    const float *bias;  // [cout] (the consumer adds it)
+    int k, cin, cout, cg, slice;
+};
+struct LatParams {
+    LatConv L[kLatMaxLayers];  // conv layers, then the head (cout 1)
+    int nl;                    // conv layers + head
+    int B, c_in, act, act_head;
+    float head_b;
+    const uint8_t *planes;     // [B][c_in][361]
+    float *part;               // lat_part_floats()
+    int *cnt;                  // kLatCntInts, zero between launches
+    int *err;
+    // policy: softmax
+    float temperature;
+    float *probs, *logits_out;
+    // value: FC (w1s sliced [H/64][361][64]) + tanh / (1 + tanh) / 2
+    int value_head;
+    const float *w1s, *b1, *w2;
+    float b2;
+    int H, value_map;
+    float *value;
+    float *fcv;                // [kLatMaxB][8]
+};
+size_t lat_part_floats();
+size_t lat_smem_bytes();
+int lat_init_device();
+int lat_grid(int B, int sm_count);
+int launch_lat_f32(const LatParams &p, int sm_count, cudaStream_t s);
 
 // 8-symmetry ensemble helpers (ensemble.cu).
 int ensemble_init_tables();

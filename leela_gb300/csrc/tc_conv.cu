@@ -47,6 +47,7 @@ constexpr int kEpiWarpsT = 16;
 constexpr uint32_t kWaitLimit = 1u << 26;
 
 struct TcParams {
+    int f16;  // operands are FP16 (else BF16)
     const float *bias;
     const float *scale;
     const float *head_w;
@@ -69,6 +70,19 @@ __device__ __forceinline__ uint32_t pack_relu_bf16x2(float lo, float hi) {
     uint32_t d;
     asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
     return d;
+}
+
+// The same with FP16 operands.
+__device__ __forceinline__ uint32_t pack_relu_f16x2(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+
+// One value rounded to nearest even in the operand type (FP16 when f16, else
+// BF16), as its 16 bits.
+__device__ __forceinline__ uint16_t round16(float v, bool f16) {
+    return f16 ? __half_as_ushort(__float2half_rn(v)) : __bfloat16_as_ushort(__float2bfloat16_rn(v));
 }
 
 // Two fused multiply-adds in one packed FP32 instruction (fma.rn.f32x2,
@@ -207,7 +221,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_bf16(128, N);
+            const uint32_t idesc = idesc_16(128, N, p.f16 != 0);
             uint32_t g = 0;
             int local = 0;
             for (int tile = blockIdx.x; tile < p.ntiles && !abort_flag;
@@ -282,11 +296,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         uint4 pk[4];
                         uint32_t *w32 = reinterpret_cast<uint32_t *>(pk);
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) {
-                            __nv_bfloat162 h2 = valid ? __floats2bfloat162_rn(f[2 * i], f[2 * i + 1])
-                                                      : __floats2bfloat162_rn(0.0f, 0.0f);
-                            w32[i] = *reinterpret_cast<uint32_t *>(&h2);
-                        }
+                        for (int i = 0; i < 16; ++i)
+                            w32[i] = valid ? ((uint32_t)round16(f[2 * i], p.f16) |
+                                              ((uint32_t)round16(f[2 * i + 1], p.f16) << 16))
+                                           : 0u;
                         uint4 *dst = reinterpret_cast<uint4 *>(p.out + (size_t)orow * N + cbase + c0);
 #pragma unroll
                         for (int i = 0; i < 4; ++i) dst[i] = pk[i];
@@ -492,7 +505,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
             cta_row_range(p.rows, r0, r1);
             for (int cs = r0; cs < r1 && !abort_flag; cs += C::TP, ++local) {
                 const int nrows = min(C::TP, r1 - cs);
-                const uint32_t idesc = idesc_bf16(128, nrows);
+                const uint32_t idesc = idesc_16(128, nrows, p.f16 != 0);
                 const int acc = local & 1;
                 const uint32_t ak = (uint32_t)(local >> 1);
                 if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(51); break; }
@@ -581,10 +594,9 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                     const int rl = row_lane % kL3Board;
                     const bool valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
                     const unsigned vmask = __ballot_sync(0xffffffffu, valid_lane);
-                    __nv_bfloat16 *col = reinterpret_cast<__nv_bfloat16 *>(buf) + o;
+                    uint16_t *col = reinterpret_cast<uint16_t *>(buf) + o;
 #pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        col[j * 128] = __float2bfloat16_rn(((vmask >> j) & 1u) ? f[j] : 0.0f);
+                    for (int j = 0; j < 32; ++j) col[j * 128] = round16(((vmask >> j) & 1u) ? f[j] : 0.0f, p.f16);
                     fence_proxy_async();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&stg_full[rq]);
@@ -613,7 +625,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                         const int cj = __shfl_sync(0xffffffffu, code, j);
                         if (cj != -1) {
                             const int r = cj >= 0 ? cj : -(cj + 2);
-                            p.out[(size_t)r * NO + o] = __float2bfloat16_rn(cj >= 0 ? f[j] : 0.0f);
+                            reinterpret_cast<uint16_t *>(p.out)[(size_t)r * NO + o] = round16(cj >= 0 ? f[j] : 0.0f, p.f16);
                         }
                     }
                 }
@@ -726,7 +738,7 @@ __device__ __forceinline__ bool poll_flag(const int *f, int want) {
     return n < kFlagPolls;
 }
 
-template <bool HEAD>
+template <bool HEAD, bool F16>
 __global__ void __maxnreg__(96)
     tc_trunk_kernel(const __grid_constant__ CUtensorMap in_a, const __grid_constant__ CUtensorMap in_b,
                     const __grid_constant__ CUtensorMap out_a, const __grid_constant__ CUtensorMap out_b,
@@ -932,7 +944,7 @@ __global__ void __maxnreg__(96)
                 // N: the item's rows, rounded up to the MMA's multiple of 16
                 // (rows past the tensor are zero-filled and not stored)
                 const int nrows = fl ? min(C::TP, (p.rows5 - j * C::TP + 15) / 16 * 16) : min(C::TP, p.rows - j * C::TP);
-                const uint32_t idesc = idesc_bf16(128, nrows);
+                const uint32_t idesc = idesc_16(128, nrows, F16);
                 const int acc = q & 1;
                 const uint32_t ak = (uint32_t)(q >> 1);
                 if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(76); break; }
@@ -1046,17 +1058,14 @@ __global__ void __maxnreg__(96)
                         for (int jj = 0; jj < 32; jj += 2) {
                             float a0, a1;
                             ffma2(a0, a1, __uint_as_float(v[jj]), __uint_as_float(v[jj + 1]), scale, bias);
-                            const uint32_t w = pack_relu_bf16x2(a0, a1);
+                            const uint32_t w = F16 ? pack_relu_f16x2(a0, a1) : pack_relu_bf16x2(a0, a1);
                             col[jj * 128] = (uint16_t)w;
                             col[(jj + 1) * 128] = (uint16_t)(w >> 16);
                         }
                     } else {
 #pragma unroll
-                        for (int jj = 0; jj < 32; ++jj) {
-                            const __nv_bfloat16 h =
-                                __float2bfloat16_rn(act_apply(fmaf(__uint_as_float(v[jj]), scale, bias), p.act));
-                            col[jj * 128] = *reinterpret_cast<const uint16_t *>(&h);
-                        }
+                        for (int jj = 0; jj < 32; ++jj)
+                            col[jj * 128] = round16(act_apply(fmaf(__uint_as_float(v[jj]), scale, bias), p.act), F16);
                     }
                     for (unsigned pad = ~vmask; pad; pad &= pad - 1) col[(__ffs(pad) - 1) * 128] = 0;
                     fence_proxy_async();
@@ -1148,7 +1157,7 @@ __global__ void __maxnreg__(96)
 // shared memory, then every 16-byte group of every row is written once.
 constexpr int kPackMaxC = 64;
 __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__restrict__ planes, int B,
-                                                             int C, int halves,
+                                                             int C, int halves, int f16,
                                                              __nv_bfloat16 *__restrict__ out) {
     __shared__ __align__(16) uint8_t sp[kPackMaxC * kPoints];
     const int b = blockIdx.x;
@@ -1186,7 +1195,7 @@ __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__re
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int r = i / groups, g = i % groups;
         const int y = r / kL5Pitch, x = r % kL5Pitch;
-        __align__(16) __nv_bfloat16 v[8];
+        __align__(16) uint16_t v[8];
         if (aligned) {
             const int ch0 = g * 8;
             const int dx = ch0 / C, c0 = ch0 - dx * C;
@@ -1194,7 +1203,7 @@ __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__re
             const bool in = y < kBoard && ch0 < 5 * C && sx >= 0 && sx < kBoard;
             const uint8_t *col = sp + c0 * kPoints + y * kBoard + sx;
 #pragma unroll
-            for (int j = 0; j < 8; ++j) v[j] = __float2bfloat16(in ? (float)col[j * kPoints] : 0.0f);
+            for (int j = 0; j < 8; ++j) v[j] = round16(in ? (float)col[j * kPoints] : 0.0f, f16);
         } else {
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -1205,17 +1214,17 @@ __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__re
                     const int sx = x + dx - 2;
                     if (sx >= 0 && sx < kBoard) val = (float)sp[c * kPoints + y * kBoard + sx];
                 }
-                v[j] = __float2bfloat16(val);
+                v[j] = round16(val, f16);
             }
         }
         *reinterpret_cast<uint4 *>(dst + (size_t)i * 8) = *reinterpret_cast<const uint4 *>(v);
     }
 }
 
-void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, __nv_bfloat16 *out,
+void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, bool f16, __nv_bfloat16 *out,
                            cudaStream_t s) {
     // four CTAs per board, each writing a quarter of its rows
-    pack_planes_l5_kernel<<<dim3(B, 4), 256, 0, s>>>(planes, B, C, halves, out);
+    pack_planes_l5_kernel<<<dim3(B, 4), 256, 0, s>>>(planes, B, C, halves, f16 ? 1 : 0, out);
 }
 
 // ------------------------------------------------------------------ launch
@@ -1241,8 +1250,10 @@ int tc_init_device() {
     LG_A(64, 1, 0, false) LG_A(64, 1, 0, true) LG_A(64, 2, 1, false) LG_A(64, 3, 1, false)
     LG_A(128, 3, 1, false) LG_A(128, 2, 0, false) LG_A(128, 2, 0, true) LG_A(128, 2, 1, false)
     LG_T(2, 0, false) LG_T(2, 0, true) LG_T(2, 1, false)
-    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<false>), TrunkCfg::SMEM>(tc_trunk_kernel<false>);
-    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<true>), TrunkCfg::SMEM>(tc_trunk_kernel<true>);
+#define LG_TR(HD_, F_) \
+    if (!rc) rc = set_attr<decltype(&tc_trunk_kernel<HD_, F_>), TrunkCfg::SMEM>(tc_trunk_kernel<HD_, F_>);
+    LG_TR(false, false) LG_TR(true, false) LG_TR(false, true) LG_TR(true, true)
+#undef LG_TR
 #undef LG_A
 #undef LG_T
     return rc;
@@ -1338,10 +1349,17 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = T.head_w ? cudaLaunchKernelEx(&cfg, tc_trunk_kernel<true>, in_a, in_b, out_a, out_b, w_map, in5,
-                                                  w0_map, p)
-                             : cudaLaunchKernelEx(&cfg, tc_trunk_kernel<false>, in_a, in_b, out_a, out_b, w_map, in5,
-                                                  w0_map, p);
+    cudaError_t e;
+    if (T.f16)
+        e = T.head_w ? cudaLaunchKernelEx(&cfg, tc_trunk_kernel<true, true>, in_a, in_b, out_a, out_b, w_map, in5,
+                                          w0_map, p)
+                     : cudaLaunchKernelEx(&cfg, tc_trunk_kernel<false, true>, in_a, in_b, out_a, out_b, w_map, in5,
+                                          w0_map, p);
+    else
+        e = T.head_w ? cudaLaunchKernelEx(&cfg, tc_trunk_kernel<true, false>, in_a, in_b, out_a, out_b, w_map, in5,
+                                          w0_map, p)
+                     : cudaLaunchKernelEx(&cfg, tc_trunk_kernel<false, false>, in_a, in_b, out_a, out_b, w_map, in5,
+                                          w0_map, p);
     if (e != cudaSuccess) {
         lg_set_error("trunk launch: %s", cudaGetErrorString(e));
         return LG_ERR_CUDA;
@@ -1358,6 +1376,7 @@ size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves) {
 int launch_tc_conv(const TcLayer &L, __nv_bfloat16 *out_l3, float *parts, size_t part_stride,
                    int *err, cudaStream_t s, int sm_count) {
     TcParams p{};
+    p.f16 = L.f16;
     p.bias = L.bias;
     p.scale = L.scale;
     p.head_w = L.head_w;
@@ -1399,6 +1418,8 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// (FP16 activations and weights move through the same maps: tiled copies do
+// not convert, the element type only fixes the 2-byte element size.)
 int encode_map_2d_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint64_t rows,
                        uint32_t box_inner, uint32_t box_rows, bool swizzle128) {
     static EncodeTiledFn fn = nullptr;

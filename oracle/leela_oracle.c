@@ -910,3 +910,59 @@ int or_random_board(uint64_t seed, int k, int8_t *squares) {
     }
     return color;
 }
+
+/* A config-0/1/2 position: from the empty board, k ~ U[0, kmax] moves, each
+ * uniform over the legal non-pass moves (empty, not the simple-ko point,
+ * not a suicide: FastState::generate_moves, FastState.cpp:57-73), passing
+ * only when nothing else is legal.  Captures as FullBoard::update_board
+ * (FullBoard.cpp:130-201) makes them; the ko point is the captured point
+ * when the stone was played into an opponent eye and captured exactly one
+ * stone (FullBoard.cpp:149-150, 192-197).  Writes squares[361] and
+ * moves[4] = last move, the move before it (-1 none or pass), ko point
+ * (-1 none), white-has-komi flag (1: komi 7.5 goes to white); returns the
+ * side to move.  Uses its own splitmix64 stream, so the positions are the
+ * same on every host. */
+int or_config_board(uint64_t seed, int kmax, int8_t *squares, int32_t *moves) {
+    uint64_t s = seed * 0xD1B54A32D192ED03ull + 0x2545F4914F6CDD1Dull;
+    memset(squares, GB_EMPTY, OR_POINTS);
+    int k = (int)(splitmix64(&s) % (uint64_t)(kmax + 1));
+    int color = 0, ko = -1, last = -1, prev = -1;
+    for (int mv = 0; mv < k; ++mv) {
+        int cand[OR_POINTS], nc = 0, p = -1;
+        for (int q = 0; q < OR_POINTS; ++q)
+            if (squares[q] == GB_EMPTY && q != ko) cand[nc++] = q;
+        while (nc > 0) {
+            int j = (int)(splitmix64(&s) % (uint64_t)nc);
+            int q = cand[j];
+            if (gb_after(squares, color, q) > 0) { p = q; break; }
+            cand[j] = cand[--nc];
+        }
+        prev = last;
+        last = p;
+        ko = -1;
+        if (p >= 0) {
+            int nb[4], m = gb_nbrs(p, nb), eye = 1, captured = 0, csq = -1;
+            for (int j = 0; j < m; ++j) eye &= squares[nb[j]] == 1 - color;
+            squares[p] = (int8_t)color;
+            for (int j = 0; j < m; ++j) {
+                int r = nb[j];
+                if (squares[r] == 1 - color && gb_libs(squares, r) == 0) {
+                    uint8_t in[OR_POINTS];
+                    int list[OR_POINTS], n;
+                    memset(in, 0, sizeof in);
+                    gb_string(squares, r, in, list, &n);
+                    for (int i = 0; i < n; ++i) squares[list[i]] = GB_EMPTY;
+                    captured += n;
+                    csq = r;
+                }
+            }
+            if (captured == 1 && eye) ko = csq;
+        }
+        color = 1 - color;
+    }
+    moves[0] = last;
+    moves[1] = prev;
+    moves[2] = ko;
+    moves[3] = 1;
+    return color;
+}

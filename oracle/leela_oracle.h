@@ -145,6 +145,13 @@ void or_gather_planes(const int8_t *squares, int to_move, const int32_t *moves, 
  * move (0 black, 1 white). */
 int or_random_board(uint64_t seed, int k, int8_t *squares);
 
+/* A position as the benchmark configurations define them: from the empty
+ * board, k ~ U[0, kmax] uniform legal non-pass moves (simple ko, no
+ * suicide), from a splitmix64 stream seeded with `seed`.  Writes
+ * squares[361] and moves[4] (last move, the move before it, ko point,
+ * white-has-komi flag); returns the side to move. */
+int or_config_board(uint64_t seed, int kmax, int8_t *squares, int32_t *moves);
+
 #ifdef __cplusplus
 }
 #endif

@@ -117,6 +117,7 @@ def lib():
             L.or_gather_planes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_void_p]
             L.or_random_board.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]
+            L.or_config_board.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
             _lib = L
     return _lib
 
@@ -262,6 +263,21 @@ def random_boards(n: int, seed: int, kmax: int = 300):
     return sq, tm
 
 
+def config_boards(n: int, seed: int, kmax: int = 250, start: int = 0):
+    """Positions n of the benchmark configurations' kind (empty board,
+    k ~ U[0, kmax] uniform legal moves, simple ko, no suicide), position i
+    drawn from stream seed * 2**32 + start + i: (squares [n][361] int8,
+    to_move [n] int8, moves [n][4] int32 = last move, the move before it,
+    ko point, white-has-komi flag)."""
+    sq = np.empty((n, POINTS), dtype=np.int8)
+    tm = np.empty(n, dtype=np.int8)
+    mv = np.empty((n, 4), dtype=np.int32)
+    L = lib()
+    for i in range(n):
+        tm[i] = L.or_config_board(ctypes.c_uint64((seed << 32) + start + i), kmax, _ptr(sq[i]), _ptr(mv[i]))
+    return sq, tm, mv
+
+
 def e4m3_round(x: float) -> float:
     return float(lib().or_e4m3_round(ctypes.c_float(x)))
 
@@ -274,13 +290,20 @@ def bf16_round_array(x: np.ndarray) -> np.ndarray:
     return r.view(np.float32).reshape(np.shape(x))
 
 
+def fp16_round_array(x: np.ndarray) -> np.ndarray:
+    """IEEE half, round to nearest even (as __float2half_rn), back to float32."""
+    return np.asarray(x, dtype=np.float32).astype(np.float16).astype(np.float32)
+
+
 def quantize_weights(n: OrNet, w: np.ndarray, mode: str) -> np.ndarray:
     """Weights as the low-precision paths see them: 'bf16' rounds every
-    weight to BF16; 'fp8' quantises each conv's W per output channel to E4M3
-    (scale = max|w|/448) and keeps the dequantised values (FC layers stay
-    BF16).  Biases stay FP32 in both."""
+    weight to BF16, 'fp16' to IEEE half (round to nearest even); 'fp8'
+    quantises each conv's W per output channel to E4M3 (scale = max|w|/448)
+    and keeps the dequantised values (FC layers stay BF16).  Biases stay
+    FP32 in all three."""
     w = np.array(w, dtype=np.float32, copy=True)
     L = lib()
+    rnd = fp16_round_array if mode == "fp16" else bf16_round_array
     for k, ci, co, off in conv_shapes(n):
         nw = co * ci * k * k
         W = np.ascontiguousarray(w[off:off + nw])
@@ -290,13 +313,13 @@ def quantize_weights(n: OrNet, w: np.ndarray, mode: str) -> np.ndarray:
             L.or_fp8_dequant_conv(_ptr(W), co, ci * k * k, _ptr(wq), _ptr(sc))
             w[off:off + nw] = wq
         else:
-            w[off:off + nw] = bf16_round_array(W)
+            w[off:off + nw] = rnd(W)
     if n.value_head:
         off = int(L.or_fc_weight_offset(ctypes.byref(n)))
         h = n.fc_hidden
-        w[off:off + h * POINTS] = bf16_round_array(w[off:off + h * POINTS])
+        w[off:off + h * POINTS] = rnd(w[off:off + h * POINTS])
         o2 = off + h * POINTS + h
-        w[o2:o2 + h] = bf16_round_array(w[o2:o2 + h])
+        w[o2:o2 + h] = rnd(w[o2:o2 + h])
     return w
 
 

@@ -1,8 +1,11 @@
 """Regenerates the golden fixtures in tests/golden from the reference engine.
 
-Run in a container that has the reference sources (read-only) and g++:
+Run where the reference sources (read-only) and g++ are present:
 
-    python tests/golden/make_golden.py [--ref /path/to/reference]
+    LEELA_REF=/path/to/reference python tests/golden/make_golden.py [--only NAME ...]
+
+(--ref overrides LEELA_REF; --only regenerates just the named fixtures,
+e.g. --only config0, and leaves the others as they are.)
 
 It builds oracle/_ref/ref_harness from the reference sources (oracle/Makefile
 target `ref`) and the C restatement (oracle/liboracle.so), draws the
@@ -24,6 +27,9 @@ own code for:
                        ReLU, FC 361->256->1 tanh) through the reference's
                        im2col<> + cblas_sgemm + softmax: logits, probs, value;
                        64 positions, rotations 0 and 3
+  config0_s0.npz       the same nets at DIRECT (rotation 0) for all 1024
+                       positions: policy logits and values (the probabilities
+                       follow from the logits by the reference softmax)
   weights.json         FNV-1a checksums of every weight set, so a test can
                        confirm another host draws the same weights
   mcowner_s0.npz       Playout::mc_owner(state, 64) for all 1024 positions (the
@@ -64,9 +70,14 @@ def run(cmd, env=None):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("LEELA_REF"))
     ap.add_argument("--threads", type=int, default=os.cpu_count())
+    ap.add_argument("--only", nargs="*", default=None,
+                    choices=["positions", "refexact", "config1", "config0", "mcowner", "weights"])
     args = ap.parse_args()
+    if not args.ref or not os.path.isdir(args.ref):
+        ap.error("set LEELA_REF (or --ref) to the reference sources")
+    want = (lambda name: True) if not args.only else (lambda name: name in args.only)
 
     odir = os.path.join(ROOT, "oracle")
     run(["make", "-s", "-C", odir, "liboracle.so"])
@@ -91,30 +102,40 @@ def main():
         w_cfg_v.tofile(wv)
         env = dict(os.environ, LEELA_REF_WEIGHTS=wref)
 
-        pre = os.path.join(td, "pos")
-        run([harness, "gen", str(N_POS), str(SEED), pre])
-        pp = np.fromfile(pre + ".planes_p", np.uint8).reshape(N_POS, 32, 361)
-        pv = np.fromfile(pre + ".planes_v", np.uint8).reshape(N_POS, 32, 361)
-        sq = np.fromfile(pre + ".squares", np.int8).reshape(N_POS, 361)
-        meta = np.fromfile(pre + ".meta", np.int32).reshape(N_POS, 4)
-        moves = np.fromfile(pre + ".moves", np.int32).reshape(N_POS, 4)
-        np.savez_compressed(os.path.join(HERE, "positions_s0.npz"),
-                            planes_p=np.packbits(pp, axis=-1), planes_v=np.packbits(pv, axis=-1),
-                            squares=sq, meta=meta, moves=moves)
+        if want("positions"):
+            pre = os.path.join(td, "pos")
+            run([harness, "gen", str(N_POS), str(SEED), pre])
+            pp = np.fromfile(pre + ".planes_p", np.uint8).reshape(N_POS, 32, 361)
+            pv = np.fromfile(pre + ".planes_v", np.uint8).reshape(N_POS, 32, 361)
+            sq = np.fromfile(pre + ".squares", np.int8).reshape(N_POS, 361)
+            meta = np.fromfile(pre + ".meta", np.int32).reshape(N_POS, 4)
+            moves = np.fromfile(pre + ".moves", np.int32).reshape(N_POS, 4)
+            np.savez_compressed(os.path.join(HERE, "positions_s0.npz"),
+                                planes_p=np.packbits(pp, axis=-1), planes_v=np.packbits(pv, axis=-1),
+                                squares=sq, meta=meta, moves=moves)
 
         run([harness, "elucheck", wp], env=env)
 
+        if want("config0"):
+            pre = os.path.join(td, "cfg0all")
+            run([harness, "config", str(N_POS), str(SEED), "0", wp, wv, pre], env=env)
+            v = np.fromfile(pre + ".value", np.float32).reshape(N_POS, 2)
+            np.savez_compressed(os.path.join(HERE, "config0_s0.npz"),
+                                logits_r0=np.fromfile(pre + ".logits", np.float32).reshape(N_POS, 361),
+                                value_pre_r0=v[:, 0], value_r0=v[:, 1])
+
         out = {}
-        for rot in (0, 5):
+        for rot in (0, 5) if want("refexact") else ():
             pre = os.path.join(td, f"refx{rot}")
             run([harness, "refexact", str(N_OUT), str(SEED), str(rot), pre], env=env)
             out[f"probs_r{rot}"] = np.fromfile(pre + ".probs", np.float32).reshape(N_OUT, 361)
             out[f"logits_r{rot}"] = np.fromfile(pre + ".logits", np.float32).reshape(N_OUT, 361)
             out[f"value_r{rot}"] = np.fromfile(pre + ".value", np.float32)
-        np.savez_compressed(os.path.join(HERE, "refexact_s0.npz"), **out)
+        if out:
+            np.savez_compressed(os.path.join(HERE, "refexact_s0.npz"), **out)
 
         out = {}
-        for rot in (0, 3):
+        for rot in (0, 3) if want("config1") else ():
             pre = os.path.join(td, f"cfg{rot}")
             run([harness, "config", str(N_OUT), str(SEED), str(rot), wp, wv, pre], env=env)
             out[f"logits_r{rot}"] = np.fromfile(pre + ".logits", np.float32).reshape(N_OUT, 361)
@@ -122,12 +143,17 @@ def main():
             v = np.fromfile(pre + ".value", np.float32).reshape(N_OUT, 2)
             out[f"value_pre_r{rot}"] = v[:, 0]
             out[f"value_r{rot}"] = v[:, 1]
-        np.savez_compressed(os.path.join(HERE, "config1_s0.npz"), **out)
+        if out:
+            np.savez_compressed(os.path.join(HERE, "config1_s0.npz"), **out)
 
-        pre = os.path.join(td, "mc")
-        run([harness, "mcowner", str(N_POS), str(SEED), "64", str(args.threads), pre])
-        np.savez_compressed(os.path.join(HERE, "mcowner_s0.npz"),
-                            mcowner=np.fromfile(pre + ".mcowner", np.float32))
+        if want("mcowner"):
+            pre = os.path.join(td, "mc")
+            run([harness, "mcowner", str(N_POS), str(SEED), "64", str(args.threads), pre])
+            np.savez_compressed(os.path.join(HERE, "mcowner_s0.npz"),
+                                mcowner=np.fromfile(pre + ".mcowner", np.float32))
+        if not want("weights"):
+            print("done")
+            return
 
     sums = {
         "ref_policy": O.checksum(w_ref_p), "ref_value": O.checksum(w_ref_v),

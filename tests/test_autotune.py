@@ -63,13 +63,14 @@ def test_autotune_writes_and_reloads_its_cache(gpu_lib, weights, positions, tmp_
 
 @pytest.mark.parametrize("B", [1, 3, 64])
 @pytest.mark.parametrize("v3", [2, 3])
-def test_fp8_trunk_matches_per_layer_kernels(gpu_lib, weights, positions, B, v3):
+@pytest.mark.parametrize("prec", ["fp8w", "fp16"])
+def test_trunk_matches_per_layer_kernels(gpu_lib, weights, positions, B, v3, prec):
     """The persistent trunk kernel (3x3 choice 2; choice 3 with the first
     layer in the same launch) computes the same layers as the per-layer
-    launches, FP8 weights (per-channel scales) included."""
+    launches, FP8 weights (per-channel scales) and FP16 operands included."""
     lg = gpu_lib
-    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "fp8w"),
-                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], "fp8w"), max_batch=64) as c:
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], prec),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], prec), max_batch=64) as c:
         c.set_tuning(B, 0, 0)
         p0, l0 = c.policy(positions["planes_p"][:B, :24], 1.0, return_logits=True)
         v0 = c.value(positions["planes_v"][:B, :24])

@@ -1,0 +1,108 @@
+"""Precision variants at the size of the precision configuration: 65,536
+seeded positions (oracle.config_boards, seed 2: empty board, k ~ U[0, 250]
+uniform legal moves, simple ko), planes 0..23 gathered on the GPU, the
+benchmark nets in BF16, FP16 and FP8-weight precision at batch 256, against
+the FP64 oracle's answers in tests/golden/config2_f64.npz (make_config2.py).
+
+Bars, with what limits them on these He-normal nets (nearly flat policies:
+the FP64 top-1/top-2 logit gap has a median of ~0.027):
+  BF16   top-1 >= 0.955   FP64 arithmetic with BF16-rounded weights and exact
+                          activations already agrees only ~0.97: BF16's 7-bit
+                          mantissa caps it, whatever the kernel does
+  FP16   top-1 >= 0.985   FP64 with FP16-rounded weights: ~0.996
+  FP8W   top-1 >= 0.55    E4M3 weights (3-bit mantissa)
+  value  max |v - v64| <= 3e-2 (BF16, FP8W), 5e-3 (FP16)
+Margin check: every top-1 disagreement has an FP64 gap below twice the
+largest logit error the variant shows on a 256-position subset (checked
+live against the FP64 oracle), i.e. the flips are the rounding error, not
+a wrong result.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+N = 65536
+CHUNK = 8192
+BARS = {"bf16": 0.955, "fp16": 0.985, "fp8w": 0.55}
+VALUE_BARS = {"bf16": 3e-2, "fp16": 5e-3, "fp8w": 6e-2}
+
+
+@pytest.fixture(scope="module")
+def config2(oracle_mod):
+    path = os.path.join(GOLDEN, "config2_f64.npz")
+    d = dict(np.load(path))
+    sq, tm, _ = oracle_mod.config_boards(N, int(d["seed"]))
+    assert hashlib.sha256(sq.tobytes()).hexdigest()[:16] == str(d["squares_sha256"]), \
+        "the position generator does not reproduce the fixture's boards"
+    assert hashlib.sha256(tm.tobytes()).hexdigest()[:16] == str(d["to_move_sha256"])
+    return d, sq, tm
+
+
+@pytest.fixture(scope="module")
+def gpu_planes(gpu_lib, config2):
+    """Planes 0..23 of both sets for all positions, gathered on the GPU."""
+    import torch
+    lg = gpu_lib
+    _, sq, tm = config2
+    d_sq = torch.from_numpy(np.ascontiguousarray(sq)).cuda()
+    d_tm = torch.from_numpy(np.ascontiguousarray(tm)).cuda()
+    out = {}
+    s = torch.cuda.current_stream()
+    for which, key in ((0, "p"), (1, "v")):
+        t = torch.empty((N, 24, 361), dtype=torch.uint8, device="cuda")
+        lg.gather_device(d_sq.data_ptr(), d_tm.data_ptr(), N, which, 24, t.data_ptr(), s.cuda_stream)
+        out[key] = t
+    s.synchronize()
+    return out
+
+
+def run_variant(lg, weights, planes, prec):
+    """Logits [N][361] and values [N] of one precision, device-resident."""
+    import torch
+    logits = torch.empty((N, 361), dtype=torch.float32, device="cuda")
+    probs = torch.empty((N, 361), dtype=torch.float32, device="cuda")
+    value = torch.empty(N, dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream()
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], prec),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], prec), max_batch=256) as c:
+        for c0 in range(0, N, CHUNK):
+            c.policy_device(planes["p"][c0].data_ptr(), CHUNK, probs[c0].data_ptr(), 1.0,
+                            logits[c0].data_ptr(), s.cuda_stream)
+            c.value_device(planes["v"][c0].data_ptr(), CHUNK, value[c0].data_ptr(), s.cuda_stream)
+        s.synchronize()
+    return logits, value
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16", "fp8w"])
+def test_top1_agreement_over_65536_positions(gpu_lib, oracle_mod, weights, config2, gpu_planes, prec):
+    lg, O = gpu_lib, oracle_mod
+    d, _, _ = config2
+    logits, value = run_variant(lg, weights, gpu_planes, prec)
+    top1 = logits.argmax(1).cpu().numpy()
+    agree = top1 == d["top1"]
+    verr = np.abs(value.cpu().numpy() - d["value"])
+    # largest logit error on a subset, against the FP64 oracle live
+    sub = np.arange(0, N, N // 256)
+    O.enable_blas()
+    try:
+        l64 = O.forward_f64(weights["cfg_p"][0], weights["cfg_p"][1], gpu_planes["p"][sub].cpu().numpy())
+    finally:
+        O.disable_blas()
+    emax = np.abs(logits[sub].cpu().numpy() - l64).max()
+    gaps = d["gap"][~agree]
+    explained = (gaps < 2 * emax).mean() if gaps.size else 1.0
+    print(f"{prec}: top-1 {agree.mean():.4f} over {N} ({(~agree).sum()} flips), value max err "
+          f"{verr.max():.2e} mean {verr.mean():.2e}, subset logit err max {emax:.2e}, "
+          f"flips with gap < 2*err {explained:.3f}; weight-rounding cap "
+          f"bf16 {(d['top1_w_bf16'] == d['top1'][:d['top1_w_bf16'].size]).mean():.4f} "
+          f"fp16 {(d['top1_w_fp16'] == d['top1'][:d['top1_w_fp16'].size]).mean():.4f}")
+    assert agree.mean() >= BARS[prec]
+    assert verr.max() <= VALUE_BARS[prec]
+    assert explained >= 0.99
+

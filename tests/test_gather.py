@@ -130,7 +130,7 @@ def test_gather_prefix_and_arguments(gpu_lib, positions):
     torch.cuda.synchronize()
 
 
-@pytest.mark.parametrize("prec", ["fp32", "bf16", "fp8w"])
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "fp16", "fp8w"])
 def test_board_calls_equal_plane_calls(gpu_lib, positions, weights, prec):
     lg = gpu_lib
     n = 160  # more than max_batch: two chunks plus a ragged one

@@ -139,3 +139,26 @@ def test_e4m3_rounding(oracle_mod):
 def test_mcowner_labels_in_range():
     d = np.load(os.path.join(GOLDEN, "mcowner_s0.npz"))["mcowner"]
     assert d.shape == (1024,) and np.all((d >= 0) & (d <= 1))
+
+
+def test_config2_fixture_weight_rounding_caps():
+    """The precision fixture's own finding (FP64 arithmetic, exact
+    activations, 16-bit weights, first 8,192 of its positions): weights
+    rounded to BF16 alone keep the FP64 top-1 below 99%, FP16 weights above."""
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_f64.npz"))
+    n = d["top1_w_bf16"].size
+    cap_b = (d["top1_w_bf16"] == d["top1"][:n]).mean()
+    cap_h = (d["top1_w_fp16"] == d["top1"][:n]).mean()
+    assert cap_b < 0.99 < cap_h
+
+
+def test_config2_generator_reproduces_the_fixture(oracle_mod):
+    """oracle.config_boards regenerates the precision fixture's 65,536 boards
+    bit for bit (the GPU test regenerates them on its own host)."""
+    import hashlib
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_f64.npz"))
+    sq, tm, mv = oracle_mod.config_boards(int(d["n"]), int(d["seed"]))
+    assert hashlib.sha256(sq.tobytes()).hexdigest()[:16] == str(d["squares_sha256"])
+    assert hashlib.sha256(tm.tobytes()).hexdigest()[:16] == str(d["to_move_sha256"])
+    # positions of the configurations' kind: stone density near the fixture's
+    assert 0.2 < (sq != 2).mean() < 0.45 and (mv[:, 3] == 1).all()

@@ -154,3 +154,52 @@ def test_avg8_ensemble_matches_oracle(gpu_lib, weights, positions, oracle_mod):
         O.disable_blas()
     assert np.abs(out.cpu().numpy() - ref / 8).max() < 1e-6
     assert np.abs(val.cpu().numpy() - vref / 8).max() < 1e-5
+
+
+@pytest.mark.parametrize("B", [1, 2, 5, 8])
+@pytest.mark.parametrize("shapes", ["config1", "reference"])
+def test_small_batch_kernel_matches_per_layer_path(gpu_lib, weights, positions, B, shapes):
+    """The small-batch kernel (every layer in one launch, 8-way input-channel
+    splits summed in a fixed order) against the per-layer FP32 kernels, for
+    the benchmark nets and the reference's own shapes (ELU, 3x3 heads,
+    32->96->128 and 64-wide value trunk, (1+tanh)/2): same top-1, logits
+    within 1e-5 norm-wise, probabilities within 1e-6, values within 1e-5."""
+    lg = gpu_lib
+    if shapes == "config1":
+        pol = lg.NetDesc.config1_policy(weights["cfg_p"][1])
+        val = lg.NetDesc.config1_value(weights["cfg_v"][1])
+        pp, pv = positions["planes_p"][:B, :24], positions["planes_v"][:B, :24]
+    else:
+        pol = lg.NetDesc.reference_policy(weights["ref_p"][1])
+        val = lg.NetDesc.reference_value(weights["ref_v"][1])
+        pp, pv = positions["planes_p"][:B], positions["planes_v"][:B]
+    with lg.Context(policy=pol, value=val, max_batch=8) as c:
+        assert c.tuning(B)["conv3x3"] == 4  # the default for small batches
+        c.set_tuning(B, 0, 0)
+        p0, l0 = c.policy(pp, 0.75, return_logits=True)
+        v0 = c.value(pv)
+        c.set_tuning(B, 4, 0)
+        n0 = c.stats()["kernel_launches"]
+        p4, l4 = c.policy(pp, 0.75, return_logits=True)
+        v4 = c.value(pv)
+        assert c.stats()["kernel_launches"] - n0 == 2  # one launch per net
+    assert rel_logit_err(l4, l0).max() <= 1e-5
+    assert np.array_equal(l4.argmax(1), l0.argmax(1))
+    assert np.abs(p4 - p0).max() < 1e-6
+    assert np.abs(v4 - v0).max() < 1e-5
+
+
+def test_small_batch_kernel_repeated_calls(gpu_lib, weights, positions):
+    """Counters reset between launches: many calls in a row on one stream
+    (alternating batch sizes, so that rows unused by one call are used by
+    the next) give the same answer every time."""
+    lg = gpu_lib
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1]),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1]), max_batch=8) as c:
+        ref1 = c.policy(positions["planes_p"][:1, :24])
+        ref8 = c.policy(positions["planes_p"][:8, :24])
+        vref = c.value(positions["planes_v"][:8, :24])
+        for i in range(20):
+            assert np.array_equal(c.policy(positions["planes_p"][:1, :24]), ref1)
+            assert np.array_equal(c.policy(positions["planes_p"][:8, :24]), ref8)
+            assert np.array_equal(c.value(positions["planes_v"][:8, :24]), vref)
