@@ -37,6 +37,9 @@
 // with ld.global.cg (L2, never a stale L1 line from an earlier layer).
 #include "lg_kernels.h"
 
+#include <cuda_fp16.h>
+
+#include <algorithm>
 #include <cfloat>
 
 namespace lg {
@@ -74,24 +77,30 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Thread 0 waits until every counter in cnt[lo..hi] reaches `want`, giving
-// up after kLatPolls polls or as soon as another CTA reported an error.
-// Returns false on either.
-__device__ bool wait_rows(const int *cnt, int lo, int hi, int want, int *err) {
-    for (int r = lo; r <= hi; ++r) {
-        uint32_t n = 0;
-        while (ld_acq(cnt + r) < want) {
-            if (++n >= kLatPolls || *(volatile int *)err != 0) return false;
-            __nanosleep(32);
-        }
+// Polls one counter until it reaches `want`: spins, then sleeps between
+// polls; gives up after kLatPolls polls or as soon as another CTA has
+// reported an error.  Returns false on either.
+__device__ __forceinline__ bool poll_one(const int *c, int want, const int *err) {
+    uint32_t n = 0;
+    while (ld_acq(c) < want) {
+        if (++n >= kLatPolls || *(volatile const int *)err != 0) return false;
+        if (n > 64) __nanosleep(32);
     }
     return true;
+}
+
+// The CTA waits until counters cnt[lo..hi] (hi - lo < kLT) reach `want`,
+// one polling thread per counter; true for every thread if all did.
+__device__ __forceinline__ bool wait_rows(const int *cnt, int lo, int hi, int want, const int *err, bool alive) {
+    const int t = threadIdx.x;
+    const bool bad = t <= hi - lo && alive && !poll_one(cnt + lo + t, want, err);
+    return !__syncthreads_or(bad || !alive);
 }
 
 // The weight slice of split s of layer L into shared memory (cp.async, 16 B
 // per copy; slices are padded to 4 floats so every copy is aligned).
 __device__ __forceinline__ void copy_slice(const LatConv &L, int s, float *dst) {
-    const float *src = L.w + (size_t)s * L.slice;
+    const float *src = static_cast<const float *>(L.w) + (size_t)s * L.slice;
     for (int i = threadIdx.x * 4; i < L.slice; i += kLT * 4) cp_async16(dst + i, src + i);
 }
 
@@ -122,24 +131,78 @@ __device__ __forceinline__ void unit_mac(const float *in_s, const float *w_s, in
     }
 }
 
+// 16-bit layers (3x3, 16 input channels a split, 128 output channels) on
+// the warp-level tensor-core MMA m16n8k16 (FP32 accumulate): warp w owns
+// output channels 16 w .. 16 w + 15 (A = weights, w16[tap][o][16]), the
+// three 8-point column tiles of the row (B = staged inputs,
+// in16[dy][xx][16], point x at xx = x + dx), one K step of 16 channels per
+// tap.  acc[j] is the accumulator fragment of column tile j: channel
+// 16 w + g (+ 8 for acc[j][2..3]), points 8 j + 2 t, + 1 (g = lane / 4,
+// t = lane % 4).
+template <bool F16>
+__device__ __forceinline__ void unit_mma(const uint16_t *in16, const uint16_t *w16, int nx, int warp, int lane,
+                                         float (&acc)[3][4]) {
+    const int r8 = lane & 7, mi = lane >> 3;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const int dy = t / 3, dx = t % 3;
+        uint32_t a[4];
+        const uint16_t *ap = w16 + (size_t)((t * 128 + 16 * warp + r8 + 8 * (mi & 1)) * 16 + 8 * (mi >> 1));
+        asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                     : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+                     : "r"(ptx::smem_u32(ap)));
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            uint32_t b[2];
+            const uint16_t *bp = in16 + (size_t)((dy * nx + 8 * j + r8 + dx) * 16 + 8 * (mi & 1));
+            asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];"
+                         : "=r"(b[0]), "=r"(b[1])
+                         : "r"(ptx::smem_u32(bp)));
+            if (F16)
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                    "{%0,%1,%2,%3};"
+                    : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
+                    : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+            else
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                    "{%0,%1,%2,%3};"
+                    : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
+                    : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+        }
+    }
+}
+
+__device__ __forceinline__ uint16_t to16(float v, bool f16) {
+    return f16 ? __half_as_ushort(__float2half_rn(v)) : __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+
 }  // namespace
 
-__global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
+// MODE 0: FP32 throughout.  MODE 1 / 2: the layers marked `mma` take 16-bit
+// inputs (BF16 / FP16, rounded as the consumer stages them) on the warp
+// MMA; the first layer and the head stay FP32 FFMA on the 16-bit-rounded
+// weights (as the tensor-core trunk keeps the head in FP32).
+template <int MODE>
+__global__ void __launch_bounds__(kLT, 1) lat_kernel(const LatParams p) {
+    constexpr bool F16 = MODE == 2;
     extern __shared__ float4 lat_smem4[];
     float *sm = reinterpret_cast<float *>(lat_smem4);
     float *wbuf0 = sm, *wbuf1 = sm + kLatSliceMax;
-    float *in_s = sm + 2 * kLatSliceMax;                      // [cg][K][kPitch]
+    float *in_s = sm + 2 * kLatSliceMax;                      // [cg][K][kPitch] FP32, or in16 [K][nx][16]
+    uint16_t *in16 = reinterpret_cast<uint16_t *>(in_s);
     float *fin = in_s + kLatMaxCg * 5 * kPitch;                // finish stage: 361 head outputs + 8 x 32 sums
-    __shared__ int s_ok, s_last;
+    __shared__ int s_last;
     __shared__ float red[32];
 
-    const int tid = threadIdx.x, G = gridDim.x, cta = blockIdx.x;
+    const int tid = threadIdx.x, G = gridDim.x, cta = blockIdx.x, lane = tid & 31, warp = tid >> 5;
     const int s = cta % kLatSplits, rstep = G / kLatSplits;
     const int rows = p.B * kBoard;
     const int cp = tid % 64, pg = tid / 64;
     bool alive = true;
     auto fail = [&](int code) {
-        if (tid == 0) atomicCAS(p.err, 0, code);
+        if (tid == 0 && alive) atomicCAS(p.err, 0, code);
         alive = false;
     };
 
@@ -147,6 +210,7 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
     cp_async_commit();
     for (int l = 0; l < p.nl; ++l) {
         const LatConv &L = p.L[l];
+        const bool mma = MODE != 0 && L.mma;
         float *w_s = (l & 1) ? wbuf1 : wbuf0;
         __syncthreads();  // the other buffer's last reader (layer l - 1) is done
         if (l + 1 < p.nl) copy_slice(p.L[l + 1], s, (l & 1) ? wbuf0 : wbuf1);
@@ -158,21 +222,17 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
         const int rw = max(r, rp);                             // rows to wait for
         const float *src = p.part + (size_t)((l - 1) & 1) * kPartBuf;
         float *dst = p.part + (size_t)(l & 1) * kPartBuf;
-        const int nx = kRowPts + 2 * r;                        // staged columns
+        // staged columns: x = -r .. 19 + r (FFMA: 20 points), or .. 23 + r
+        // (MMA: three 8-point column tiles)
+        const int nx = (mma ? 24 : kRowPts) + 2 * r;
         for (int row = cta / kLatSplits; row < rows; row += rstep) {
             const int b = row / kBoard, y = row % kBoard;
-            if (tid == 0) {
-                bool ok = alive;
-                if (ok && l > 0)
-                    ok = wait_rows(p.cnt + (l - 1) * kLatMaxRows, b * kBoard + max(0, y - rw),
-                                   b * kBoard + min(kBoard - 1, y + rw), kLatSplits, p.err);
-                s_ok = ok;
-            }
-            __syncthreads();
-            if (!s_ok) {
-                if (alive) fail(91);
+            if (l > 0 && !wait_rows(p.cnt + (l - 1) * kLatMaxRows, b * kBoard + max(0, y - rw),
+                                    b * kBoard + min(kBoard - 1, y + rw), kLatSplits, p.err, alive)) {
+                fail(91);
                 continue;
             }
+            if (!alive) continue;
             // ---- stage the input rows y - r .. y + r of this split's channels
             const int c0 = s * L.cg;
             if (l == 0) {
@@ -186,43 +246,82 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
                     in_s[(c * L.k + dy) * kPitch + xx] = v;
                 }
             } else {
-                // 4 channels per item: sum of the 8 partials, scale, bias, act
+                // 8 channels per item (4 when cg is not a multiple of 8): sum
+                // of the 8 partials, scale, bias, act; every load of an item
+                // is issued before the first add, and at most two items a
+                // thread for a 3x3 layer (one round trip each)
                 const LatConv &P = p.L[l - 1];
-                const int c4n = L.cg / 4, n = c4n * L.k * nx;
+                const int cw = (L.cg % 8 == 0) ? 8 : 4, nc = L.cg / cw, n = nc * L.k * nx;
                 for (int i = tid; i < n; i += kLT) {
-                    const int c4 = i / (L.k * nx), rem = i - c4 * (L.k * nx), dy = rem / nx, xx = rem - dy * nx;
+                    const int ci = i / (L.k * nx), rem = i - ci * (L.k * nx), dy = rem / nx, xx = rem - dy * nx;
                     const int yy = y + dy - r, x = xx - r;
-                    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (yy >= 0 && yy < kBoard && x >= 0 && x < kBoard) {
-                        const int ch = c0 + 4 * c4;
-                        const float *q = src + ((size_t)(b * kBoard + yy) * kRowPts + x) * 128 + ch;
-                        float4 t[kLatSplits];
+                    float v[8];
 #pragma unroll
-                        for (int ss = 0; ss < kLatSplits; ++ss)
-                            t[ss] = __ldcg(reinterpret_cast<const float4 *>(q + (size_t)ss * kLatMaxRows * kRowPts * 128));
+                    for (int e = 0; e < 8; ++e) v[e] = 0.0f;
+                    const int ch = c0 + cw * ci;
+                    if (yy >= 0 && yy < kBoard && x >= 0 && x < kBoard) {
+                        const float *q = src + ((size_t)(b * kBoard + yy) * kRowPts + x) * 128 + ch;
+                        float4 t[kLatSplits][2];
 #pragma unroll
                         for (int ss = 0; ss < kLatSplits; ++ss) {
-                            v.x += t[ss].x;
-                            v.y += t[ss].y;
-                            v.z += t[ss].z;
-                            v.w += t[ss].w;
+                            const float4 *qq = reinterpret_cast<const float4 *>(q + (size_t)ss * kLatMaxRows * kRowPts * 128);
+                            t[ss][0] = __ldcg(qq);
+                            t[ss][1] = cw == 8 ? __ldcg(qq + 1) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                         }
-                        const float4 bb = *reinterpret_cast<const float4 *>(P.bias + ch);
-                        v.x = lat_act(v.x + bb.x, p.act);
-                        v.y = lat_act(v.y + bb.y, p.act);
-                        v.z = lat_act(v.z + bb.z, p.act);
-                        v.w = lat_act(v.w + bb.w, p.act);
+#pragma unroll
+                        for (int ss = 0; ss < kLatSplits; ++ss) {
+                            v[0] += t[ss][0].x;
+                            v[1] += t[ss][0].y;
+                            v[2] += t[ss][0].z;
+                            v[3] += t[ss][0].w;
+                            v[4] += t[ss][1].x;
+                            v[5] += t[ss][1].y;
+                            v[6] += t[ss][1].z;
+                            v[7] += t[ss][1].w;
+                        }
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            if (e >= cw) break;
+                            const float bb = __ldg(P.bias + ch + e);
+                            v[e] = lat_act(P.scale ? fmaf(v[e], __ldg(P.scale + ch + e), bb) : v[e] + bb, p.act);
+                        }
                     }
-                    float *d = in_s + ((4 * c4) * L.k + dy) * kPitch + xx;
-                    d[0] = v.x;
-                    d[L.k * kPitch] = v.y;
-                    d[2 * L.k * kPitch] = v.z;
-                    d[3 * L.k * kPitch] = v.w;
+                    if (mma) {
+                        // cw == 8 (cg = 16): one 16-byte store of 8 channels
+                        uint4 h;
+                        h.x = (uint32_t)to16(v[0], F16) | ((uint32_t)to16(v[1], F16) << 16);
+                        h.y = (uint32_t)to16(v[2], F16) | ((uint32_t)to16(v[3], F16) << 16);
+                        h.z = (uint32_t)to16(v[4], F16) | ((uint32_t)to16(v[5], F16) << 16);
+                        h.w = (uint32_t)to16(v[6], F16) | ((uint32_t)to16(v[7], F16) << 16);
+                        *reinterpret_cast<uint4 *>(in16 + (dy * nx + xx) * 16 + 8 * ci) = h;
+                    } else {
+                        float *d = in_s + ((cw * ci) * L.k + dy) * kPitch + xx;
+#pragma unroll
+                        for (int e = 0; e < 8; ++e)
+                            if (e < cw) d[e * L.k * kPitch] = v[e];
+                    }
                 }
             }
             __syncthreads();
             // ---- partial sums of this unit
-            if (2 * cp < L.cout) {
+            float *o_row = dst + ((size_t)s * kLatMaxRows + row) * kRowPts * 128;
+            if (mma) {
+                float acc[3][4];
+#pragma unroll
+                for (int j = 0; j < 3; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+                unit_mma<F16>(in16, reinterpret_cast<const uint16_t *>(w_s), nx, warp, lane, acc);
+                const int g = lane >> 2, t4 = lane & 3, o = 16 * warp + g;
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int x = 8 * j + 2 * t4 + h;
+                        if (x < kBoard) {
+                            o_row[x * 128 + o] = acc[j][h];
+                            o_row[x * 128 + o + 8] = acc[j][2 + h];
+                        }
+                    }
+            } else if (2 * cp < L.cout) {
                 float acc[5][2];
 #pragma unroll
                 for (int j = 0; j < 5; ++j) acc[j][0] = acc[j][1] = 0.0f;
@@ -232,7 +331,7 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
                     unit_mac<5>(in_s, w_s, L.cg, L.cout, pg, cp, acc);
                 else
                     unit_mac<1>(in_s, w_s, L.cg, L.cout, pg, cp, acc);
-                float *o = dst + ((size_t)s * kLatMaxRows + row) * kRowPts * 128 + 2 * cp;
+                float *o = o_row + 2 * cp;
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
                     const int x = 5 * pg + j;
@@ -242,8 +341,9 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
                     else
                         *reinterpret_cast<float2 *>(o + x * 128) = make_float2(acc[j][0], acc[j][1]);
                 }
-                __threadfence();
             }
+            // publish: the barrier orders every thread's stores before thread
+            // 0's release add
             __syncthreads();
             if (tid == 0) red_release_add(p.cnt + l * kLatMaxRows + row, 1);
         }
@@ -259,14 +359,8 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
     for (int u = cta; u < nfin; u += G) {
         const int b = p.value_head ? u / kLatSplits : u, fs = p.value_head ? u % kLatSplits : 0;
         __syncthreads();
-        if (tid == 0) {
-            bool ok = alive && wait_rows(p.cnt + hl * kLatMaxRows, b * kBoard, b * kBoard + kBoard - 1,
-                                         kLatSplits, p.err);
-            s_ok = ok;
-        }
-        __syncthreads();
-        if (!s_ok) {
-            if (alive) fail(92);
+        if (!wait_rows(p.cnt + hl * kLatMaxRows, b * kBoard, b * kBoard + kBoard - 1, kLatSplits, p.err, alive)) {
+            fail(92);
             continue;
         }
         for (int i = tid; i < kPoints; i += kLT) {
@@ -287,7 +381,7 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
             for (int i = tid; i < kPoints; i += kLT) m = fmaxf(m, fin[i]);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-            if ((tid & 31) == 0) red[tid / 32] = m;
+            if (lane == 0) red[warp] = m;
             __syncthreads();
             if (tid < 32) {
                 float v = tid < kLT / 32 ? red[tid] : -FLT_MAX;
@@ -305,7 +399,7 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
             __syncthreads();
-            if ((tid & 31) == 0) red[tid / 32] = sum;
+            if (lane == 0) red[warp] = sum;
             __syncthreads();
             if (tid < 32) {
                 float v = tid < kLT / 32 ? red[tid] : 0.0f;
@@ -319,7 +413,7 @@ __global__ void __launch_bounds__(kLT, 1) lat_f32_kernel(const LatParams p) {
         } else {
             // FC1 units fs * hs .. + hs (hs = H / 8 <= 32): lane = unit, the 8
             // warps take 8 ranges of the 361 inputs, summed in warp order
-            const int hs = p.H / kLatSplits, lane = tid & 31, warp = tid / 32;
+            const int hs = p.H / kLatSplits;
             const int u0 = fs * hs + lane;
             const int i0 = warp * 46, i1 = min(kPoints, i0 + 46);
             float a = 0.0f;
@@ -374,8 +468,12 @@ size_t lat_smem_bytes() {
 }
 
 int lat_init_device() {
-    cudaError_t e = cudaFuncSetAttribute(lat_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(lat_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)lat_smem_bytes());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(lat_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lat_smem_bytes());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(lat_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lat_smem_bytes());
     if (e != cudaSuccess) {
         lg_set_error("cudaFuncSetAttribute(latency kernel): %s", cudaGetErrorString(e));
         return LG_ERR_CUDA;
@@ -388,9 +486,9 @@ int lat_grid(int B, int sm_count) {
     return g - g % kLatSplits;
 }
 
-int launch_lat_f32(const LatParams &p, int sm_count, cudaStream_t s) {
+int launch_lat(const LatParams &p, int mode, int sm_count, cudaStream_t s) {
     const int G = lat_grid(p.B, sm_count);
-    if (p.B < 1 || p.B > kLatMaxB || p.nl < 2 || p.nl > kLatMaxLayers || G < kLatSplits) {
+    if (p.B < 1 || p.B > kLatMaxB || p.nl < 2 || p.nl > kLatMaxLayers || G < kLatSplits || mode < 0 || mode > 2) {
         lg_set_error("latency kernel: bad arguments (B=%d, layers=%d)", p.B, p.nl);
         return LG_ERR_ARG;
     }
@@ -404,7 +502,9 @@ int launch_lat_f32(const LatParams &p, int sm_count, cudaStream_t s) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, lat_f32_kernel, p);
+    cudaError_t e = mode == 0 ? cudaLaunchKernelEx(&cfg, lat_kernel<0>, p)
+                              : (mode == 1 ? cudaLaunchKernelEx(&cfg, lat_kernel<1>, p)
+                                           : cudaLaunchKernelEx(&cfg, lat_kernel<2>, p));
     if (e != cudaSuccess) {
         lg_set_error("latency kernel launch: %s", cudaGetErrorString(e));
         return LG_ERR_CUDA;

@@ -293,6 +293,73 @@ int build_lat(lg_ctx *c, Net &n, const std::vector<std::vector<float>> &Wraw) {
     return LG_OK;
 }
 
+// The small-batch kernel's layout for tensor-core nets of width 128 (1x1
+// head): the first layer and the head in FP32 on the weights as the
+// precision rounds them (FP8: the E4M3 codes, the per-channel scale being
+// applied by the consumer), the 3x3 layers as 16-bit [8][9][128][16] for the
+// warp MMA.  Biases and scales are the tensor-core path's own arrays.
+int build_lat_tc(lg_ctx *c, Net &n, const std::vector<std::vector<float>> &Wraw) {
+    const lg_net_desc &d = n.d;
+    const int nl = (int)n.shapes.size();
+    const bool fp8 = d.precision == LG_FP8W, f16 = d.precision == LG_FP16;
+    if (d.width != 128 || d.width1 != 128 || d.c_in % kLatSplits != 0 || d.head_k != 1 || nl > kLatMaxLayers ||
+        (d.value_head && (d.fc_hidden % kLatSplits != 0 || d.fc_hidden > 256)) || d.c_in / kLatSplits * 5 > kLatMaxCg * 5)
+        return LG_OK;
+    for (int l = 0; l < nl; ++l) {
+        const Shape sh = n.shapes[l];
+        const int kk = sh.k * sh.k, cg = sh.cin / kLatSplits;
+        const bool head = l + 1 == nl, mid = l > 0 && !head;
+        std::vector<float> scale(sh.cout, 1.0f);
+        if (fp8 && !head)
+            for (int o = 0; o < sh.cout; ++o) {
+                float m = 0.0f;
+                for (size_t i = 0; i < (size_t)sh.cin * kk; ++i) m = std::max(m, std::fabs(Wraw[l][(size_t)o * sh.cin * kk + i]));
+                scale[o] = m > 0.0f ? m / 448.0f : 1.0f;
+            }
+        // the weight as the path computes with it
+        auto wv = [&](int o, int ci, int t) {
+            const float v = Wraw[l][((size_t)o * sh.cin + ci) * kk + t];
+            if (head) return round_operand(v, f16);
+            return fp8 ? e4m3_round(v / scale[o]) : round_operand(v, f16);
+        };
+        LatConv L{};
+        L.k = sh.k;
+        L.cin = sh.cin;
+        L.cout = sh.cout;
+        L.cg = cg;
+        L.mma = mid ? 1 : 0;
+        L.bias = head ? nullptr : n.tc[l].bias;
+        L.scale = head ? nullptr : n.tc[l].scale;
+        int rc;
+        if (mid) {
+            L.slice = 9 * 128 * 16 / 2;
+            std::vector<__nv_bfloat16> w((size_t)kLatSplits * 9 * 128 * 16);
+            for (int sp = 0; sp < kLatSplits; ++sp)
+                for (int t = 0; t < 9; ++t)
+                    for (int o = 0; o < 128; ++o)
+                        for (int cl = 0; cl < 16; ++cl)
+                            w[(((size_t)sp * 9 + t) * 128 + o) * 16 + cl] = operand16(wv(o, sp * 16 + cl, t), f16);
+            __nv_bfloat16 *dw;
+            if ((rc = upload(c, &dw, w))) return rc;
+            L.w = dw;
+        } else {
+            L.slice = (cg * kk * sh.cout + 3) & ~3;
+            std::vector<float> w((size_t)kLatSplits * L.slice, 0.0f);
+            for (int sp = 0; sp < kLatSplits; ++sp)
+                for (int cl = 0; cl < cg; ++cl)
+                    for (int t = 0; t < kk; ++t)
+                        for (int o = 0; o < sh.cout; ++o)
+                            w[(size_t)sp * L.slice + ((size_t)cl * kk + t) * sh.cout + o] = wv(o, sp * cg + cl, t);
+            float *dw;
+            if ((rc = upload(c, &dw, w))) return rc;
+            L.w = dw;
+        }
+        n.lat.push_back(L);
+    }
+    n.lat_ok = true;
+    return LG_OK;
+}
+
 int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
     if (!valid_desc(d) || !d->weights) {
         lg_set_error("invalid network description");
@@ -415,6 +482,7 @@ int build_net(lg_ctx *c, Net &n, const lg_net_desc *d) {
         for (auto &v : hw) v = round_operand(v, f16);
         if ((rc = upload(c, &n.tc_head_w, hw))) return rc;
         n.head_b = Braw.back()[0];
+        if ((rc = build_lat_tc(c, n, Wraw))) return rc;
     }
     if (d->value_head) {
         int H = d->fc_hidden;
@@ -528,7 +596,8 @@ int forward_lat(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float 
     int rc;
     {
         ProfScope ps(c, prof, LG_PROF_LAT, s);
-        rc = launch_lat_f32(p, c->sm_count, s);
+        const int mode = d.precision == LG_FP32 ? 0 : (d.precision == LG_FP16 ? 2 : 1);
+        rc = launch_lat(p, mode, c->sm_count, s);
     }
     *nlaunch = 1;
     return rc;
@@ -580,6 +649,7 @@ int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float
 int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
                float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof,
                bool l5_ready = false) {
+    if (use_lat(c, n, B) && !l5_ready) return forward_lat(c, n, planes, B, T, probs, logits_out, value, s, nlaunch, prof);
     const lg_net_desc &d = n.d;
     const int f16 = d.precision == LG_FP16 ? 1 : 0;
     int L = 0;
@@ -706,7 +776,9 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
         return LG_ERR_ARG;
     }
     const bool with_moves = boards && n.d.c_in > 24;
-    const bool l5_direct = boards && n.d.precision != LG_FP32;
+    // tensor-core nets: the gather writes the first layer's input rows, except
+    // for chunks the small-batch kernel takes (it reads planes)
+    const bool l5_boards = boards && n.d.precision != LG_FP32;
     if (with_moves && !moves && B > 0) {
         lg_set_error("the net reads planes 24..31 (ladders, ko, last moves, komi): moves are needed");
         return LG_ERR_ARG;
@@ -764,6 +836,7 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
         } else {
             std::memcpy(hp[slot], planes + (size_t)b0 * per_in, in_bytes);
         }
+        const bool l5_direct = l5_boards && !use_lat(c, n, nb);
         auto key = std::make_tuple(net, nb, n.d.value_head ? 0u : tbits,
                                    (want_logits ? 1 : 0) + 8 * slot + (boards ? 16 : 0));
         auto it = c->graphs.find(key);

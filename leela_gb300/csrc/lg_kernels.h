@@ -120,9 +120,10 @@ int tc_init_device();
 // Every conv layer of a net (the head as a layer of one output channel) in
 // one cooperative launch for 1..kLatMaxB positions: units (board row, input
 // channel split) of 8 splits a layer, partial sums per split in FP32, added
-// by the consumer in a fixed order.  Weights per layer: [8][cg][k*k][cout]
-// FP32 (split s holds input channels s*cg .. s*cg + cg - 1), each split's
-// block padded to `slice` floats (a multiple of 4).
+// by the consumer in a fixed order.  Weights per layer and split (input
+// channels s*cg .. s*cg + cg - 1): FP32 [cg][k*k][cout], or for the 16-bit
+// layers of tensor-core nets [9][128][16]; each split's block padded to
+// `slice` floats (a multiple of 4).
 constexpr int kLatMaxB = 8;
 constexpr int kLatSplits = 8;
 constexpr int kLatMaxRows = kLatMaxB * kBoard;
@@ -136,9 +137,12 @@ constexpr int kLatCntExit = kLatCntFc + kLatMaxB;
 constexpr int kLatCntInts = kLatCntExit + 1;
 
 struct LatConv {
-    const float *w;     // [8][slice]
-    const float *bias;  // [cout] (the consumer adds it)
+    const void *w;       // [8][slice floats]: FP32 [cg][k*k][cout], or for 16-bit
+                         // layers [9][cout = 128][16] BF16 / FP16
+    const float *bias;   // [cout] (the consumer adds it)
+    const float *scale;  // [cout] per-output-channel weight scale (FP8 weights), or null
     int k, cin, cout, cg, slice;
+    int mma;             // 16-bit layer on the warp MMA (3x3, cg 16, cout 128)
 };
 struct LatParams {
     LatConv L[kLatMaxLayers];  // conv layers, then the head (cout 1)
@@ -164,7 +168,8 @@ size_t lat_part_floats();
 size_t lat_smem_bytes();
 int lat_init_device();
 int lat_grid(int B, int sm_count);
-int launch_lat_f32(const LatParams &p, int sm_count, cudaStream_t s);
+// mode 0: FP32 nets; 1 / 2: BF16 / FP16 activations on the layers marked mma
+int launch_lat(const LatParams &p, int mode, int sm_count, cudaStream_t s);
 
 // 8-symmetry ensemble helpers (ensemble.cu).
 int ensemble_init_tables();

@@ -743,7 +743,8 @@ __global__ void __maxnreg__(96)
     tc_trunk_kernel(const __grid_constant__ CUtensorMap in_a, const __grid_constant__ CUtensorMap in_b,
                     const __grid_constant__ CUtensorMap out_a, const __grid_constant__ CUtensorMap out_b,
                     const __grid_constant__ CUtensorMap w_map, const __grid_constant__ CUtensorMap in5,
-                    const __grid_constant__ CUtensorMap w0_map, const TrunkParams p) {
+                    const __grid_constant__ CUtensorMap w0_map, const __grid_constant__ CUtensorMap out_a_sw,
+                    const __grid_constant__ CUtensorMap out_b_sw, const TrunkParams p) {
     using C = TrunkCfg;
     using C0 = TrunkCfg::C0;
     using C1 = TrunkCfg::C1;
@@ -810,6 +811,8 @@ __global__ void __maxnreg__(96)
         prefetch_tensormap(&in_b);
         prefetch_tensormap(&out_a);
         prefetch_tensormap(&out_b);
+        prefetch_tensormap(&out_a_sw);
+        prefetch_tensormap(&out_b_sw);
         prefetch_tensormap(&w_map);
         if (first) {
             prefetch_tensormap(&in5);
@@ -1003,8 +1006,91 @@ __global__ void __maxnreg__(96)
             const uint32_t t_base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * C::TP + rq * 64);
             const int q_base = cs + rq * 64;
             bool bad = false;
+            // 3x3 ReLU items take the fragment path: TMEM read as the MMA
+            // accumulator fragments (16x256b: thread t holds channels
+            // t/4 + {0, 8, 16, 24} of its quarter for row pairs), packed and
+            // written with stmatrix.trans into a 128-byte-swizzled staging
+            // tile (two 64-channel halves), stored by two TMA boxes.  Head,
+            // first-layer and ELU items keep the 32x32b path below.
+            if (!fl && !head_layer && p.act == LG_ACT_RELU) {
+                const float *bl = p.bias + k * NO, *sl = p.scale ? p.scale + k * NO : nullptr;
+                const int cq = quarter * 32 + (lane >> 2);
+                float fb[4], fs[4];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    fb[m] = __ldg(bl + cq + 8 * m);
+                    fs[m] = sl ? __ldg(sl + cq + 8 * m) : 1.0f;
+                }
+                const CUtensorMap *om_sw = (k & 1) ? &out_a_sw : &out_b_sw;
+                const int hh = quarter >> 1;
+                const uint32_t stg_half = smem_u32(stg + rq * C::STG_BYTES + hh * (C::STG_BYTES / 2));
+                const uint32_t st_addr =
+                    stg_half + (lane & 7) * 128 + (((((quarter & 1) * 4) + (lane >> 3)) ^ (lane & 7)) * 16);
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    uint32_t r0[16], r1[16];
+                    tmem_ld16x256_x4(t_base + 32 * c, r0);
+                    tmem_ld16x256_x4(t_base + (16u << 16) + 32 * c, r1);
+                    tmem_ld_wait();
+                    if (c == 1) {
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&acc_empty[acc]);
+                    }
+                    if (c >= nhalf || bad) continue;
+                    const uint32_t use = uses++;
+                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) {
+                        fail(81);
+                        bad = true;
+                        continue;
+                    }
+                    const int rl = (q_base + c * 32 + lane) % kL3Board;
+                    const unsigned vmask = __ballot_sync(0xffffffffu, (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        uint32_t w[4];
+#pragma unroll
+                        for (int m = 0; m < 4; ++m) {
+                            const uint32_t *rr = (m < 2) ? r0 : r1;
+                            float a0, a1;
+                            ffma2(a0, a1, __uint_as_float(rr[4 * i + 2 * (m & 1)]),
+                                  __uint_as_float(rr[4 * i + 2 * (m & 1) + 1]), fs[m], fb[m]);
+                            w[m] = F16 ? pack_relu_f16x2(a0, a1) : pack_relu_bf16x2(a0, a1);
+                        }
+                        stmatrix_x4_trans(st_addr + i * 1024, w[0], w[1], w[2], w[3]);
+                    }
+                    __syncwarp();
+                    // pad rows (x = 19, y = 19) as zeros: lane L clears row
+                    // 8g + L/4, chunk L%4 of this quarter's 64 bytes
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        const int row = 8 * g + (lane >> 2);
+                        if (!((vmask >> row) & 1u)) {
+                            const uint32_t za = stg_half + row * 128 + ((((quarter & 1) * 4 + (lane & 3)) ^ (row & 7)) * 16);
+                            asm volatile("st.shared.v4.b32 [%0], {%1,%1,%1,%1};" ::"r"(za), "r"(0u) : "memory");
+                        }
+                    }
+                    fence_proxy_async();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&stg_full[rq]);
+                    if (quarter == 0 && lane == 0) {
+                        if (!mbar_wait(&stg_full[rq], use & 1, kWaitLimit)) {
+                            fail(82);
+                        } else {
+                            uint8_t *buf = stg + rq * C::STG_BYTES;
+                            tma_store_2d(om_sw, buf, 0, q_base + c * 32);
+                            tma_store_2d(om_sw, buf + C::STG_BYTES / 2, 64, q_base + c * 32);
+                            bulk_commit();
+                            bulk_wait_read0();
+                        }
+                        mbar_arrive(&stg_empty[rq]);
+                    }
+                    __syncwarp();
+                }
+            }
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
+                if (!fl && !head_layer && p.act == LG_ACT_RELU) break;
                 // One 32-row half at a time (32 registers); the accumulator is
                 // released after the second half's load, which the MMA issuer
                 // needs again only one item later.
@@ -1303,11 +1389,15 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
         lg_set_error("launch_tc_trunk: bad arguments");
         return LG_ERR_ARG;
     }
-    CUtensorMap in_a, in_b, out_a, out_b, w_map, in5, w0_map;
+    CUtensorMap in_a, in_b, out_a, out_b, w_map, in5, w0_map, out_a_sw, out_b_sw;
     int rc = encode_map_2d_bf16(&in_a, T.buf_a, 128, (uint64_t)T.rows, 64, C0::SUBROWS);
     if (!rc) rc = encode_map_2d_bf16(&in_b, T.buf_b, 128, (uint64_t)T.rows, 64, C0::SUBROWS);
     if (!rc) rc = encode_map_2d_bf16(&out_a, T.buf_a, 128, (uint64_t)T.rows, 128, 32, false);
     if (!rc) rc = encode_map_2d_bf16(&out_b, T.buf_b, 128, (uint64_t)T.rows, 128, 32, false);
+    // the fragment-path epilogue's stores: 64-channel boxes from 128-byte
+    // swizzled staging halves
+    if (!rc) rc = encode_map_2d_bf16(&out_a_sw, T.buf_a, 128, (uint64_t)T.rows, 64, 32, true);
+    if (!rc) rc = encode_map_2d_bf16(&out_b_sw, T.buf_b, 128, (uint64_t)T.rows, 64, 32, true);
     if (!rc) rc = encode_map_2d_bf16(&w_map, T.w, 64, (uint64_t)T.nl * C0::NTAPS * 2 * 128, 64, 128);
     if (fused) {
         if (!rc) rc = encode_map_2d_bf16(&in5, T.buf5, 128, (uint64_t)T.rows5, 64, C1::SUBROWS);
@@ -1352,14 +1442,14 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     cudaError_t e;
     if (T.f16)
         e = T.head_w ? cudaLaunchKernelEx(&cfg, tc_trunk_kernel<true, true>, in_a, in_b, out_a, out_b, w_map, in5,
-                                          w0_map, p)
+                                          w0_map, out_a_sw, out_b_sw, p)
                      : cudaLaunchKernelEx(&cfg, tc_trunk_kernel<false, true>, in_a, in_b, out_a, out_b, w_map, in5,
-                                          w0_map, p);
+                                          w0_map, out_a_sw, out_b_sw, p);
     else
         e = T.head_w ? cudaLaunchKernelEx(&cfg, tc_trunk_kernel<true, false>, in_a, in_b, out_a, out_b, w_map, in5,
-                                          w0_map, p)
+                                          w0_map, out_a_sw, out_b_sw, p)
                      : cudaLaunchKernelEx(&cfg, tc_trunk_kernel<false, false>, in_a, in_b, out_a, out_b, w_map, in5,
-                                          w0_map, p);
+                                          w0_map, out_a_sw, out_b_sw, p);
     if (e != cudaSuccess) {
         lg_set_error("trunk launch: %s", cudaGetErrorString(e));
         return LG_ERR_CUDA;

@@ -155,3 +155,32 @@ def test_bf16_planes_with_other_byte_values(gpu_lib, oracle_mod, positions, c_in
         _, la = a.policy(doubled, 1.0, return_logits=True)
         _, lb = b.policy(planes, 1.0, return_logits=True)
     assert np.array_equal(la, lb)
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16", "fp8w"])
+@pytest.mark.parametrize("B", [1, 3, 8])
+def test_small_batch_kernel_lowp(gpu_lib, weights, positions, f64_refs, prec, B):
+    """Choice 4 -- the whole net in one launch, the 3x3 layers on the warp
+    MMA, the first layer and the head in FP32 on the rounded weights -- rounds
+    the activations where the tensor-core trunk does; only the order of the
+    FP32 sums differs.  Same bars against the FP64 oracle (with the variant's
+    own weights) as the batched kernels, one launch per net, and within the
+    same distance of the per-layer kernels' results."""
+    lg = gpu_lib
+    pp, pv = positions["planes_p"][:B, :24], positions["planes_v"][:B, :24]
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], prec),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], prec), max_batch=8) as c:
+        c.set_tuning(B, 0, 0)
+        _, l0 = c.policy(pp, 1.0, return_logits=True)
+        v0 = c.value(pv)
+        c.set_tuning(B, 4, 0)
+        n0 = c.stats()["kernel_launches"]
+        _, l4 = c.policy(pp, 1.0, return_logits=True)
+        v4 = c.value(pv)
+        assert c.stats()["kernel_launches"] - n0 == 2
+    lp64, _, v64 = f64_refs[prec]
+    lbar, vbar = (1e-2, 5e-3) if prec == "fp16" else (5e-2, 3e-2)
+    assert rel_logit_err(l4, lp64[:B]).max() <= lbar
+    assert np.abs(v4 - v64[:B]).max() <= vbar
+    assert rel_logit_err(l4, l0).max() <= lbar
+    assert np.abs(v4 - v0).max() <= vbar
