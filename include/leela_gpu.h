@@ -45,13 +45,17 @@ extern "C" {
 
 #define LG_NET_POLICY 0
 #define LG_NET_VALUE 1
+#define LG_NET_POLICY_LOGITS 2 /* lg_submit only: the policy net's head output
+                                  (logits) instead of probabilities */
 
 /* Network shape and weights.  Conv layers in order: 5x5 c_in -> width1;
  * n3x3 layers 3x3 (width1 ->) width -> width; head head_k x head_k width -> 1.
  * `act` follows every conv but the head, and the head too if act_head.
  * Value nets (value_head = 1) add FC 361 -> fc_hidden (+act) and FC
- * fc_hidden -> 1, then tanh (value_map 0) or (1 + tanh) / 2 (value_map 1,
- * Network.cpp:735-737).
+ * fc_hidden -> 1, then tanh (value_map 0), (1 + tanh) / 2 (value_map 1,
+ * Network.cpp:735-737), or no map (value_map 2: the FC output itself, for
+ * callers that apply their own, as the OpenCL backend's callers do,
+ * Network.cpp:704-705).
  *
  * weights: one flat FP32 array, per conv W[O][C][k][k] then b[O] (the
  * reference's OIHW arrays conv1_w, conv1_b, ... in order,
@@ -178,10 +182,12 @@ LG_API int lg_policy_avg8_device(lg_ctx *ctx, const uint8_t *planes, int B, floa
                                  float *probs, void *stream);
 LG_API int lg_value_avg8_device(lg_ctx *ctx, const uint8_t *planes, int B, float *value, void *stream);
 
-/* Batching server.  lg_submit queues B positions for net LG_NET_POLICY or
- * LG_NET_VALUE and returns at once; `out` (host, [B][361] probabilities at
- * `temperature` or [B] values) is filled before `tag` is reported by
- * lg_poll.  A worker thread gathers queued requests into batches of up to
+/* Batching server.  lg_submit queues B positions for net LG_NET_POLICY,
+ * LG_NET_VALUE or LG_NET_POLICY_LOGITS and returns at once; `out` (host,
+ * [B][361] probabilities at `temperature`, [B] values, or [B][361] head
+ * outputs before the softmax for callers that apply their own, as the
+ * OpenCL backend's forward_cb does, Network.cpp:484-494) is filled before
+ * `tag` is reported by lg_poll.  A worker thread gathers queued requests into batches of up to
  * max_batch, pads each batch to a power-of-two bucket and replays the CUDA
  * graph captured for that bucket.  lg_poll copies up to `max` completed tags
  * and returns how many, waiting at most timeout_us microseconds (0 = do not

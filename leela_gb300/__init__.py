@@ -31,7 +31,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "leela_gpu.h")
 POINTS = 361
 LG_FP32, LG_BF16, LG_FP8W, LG_FP16 = 0, 1, 2, 3
 LG_ACT_ELU, LG_ACT_RELU = 0, 1
-LG_NET_POLICY, LG_NET_VALUE = 0, 1
+LG_NET_POLICY, LG_NET_VALUE, LG_NET_POLICY_LOGITS = 0, 1, 2
 (PROF_TC_3X3, PROF_TC_HEAD, PROF_TC_FIRST, PROF_FP32_CONV, PROF_OTHER, PROF_TC_TRUNK, PROF_PACK,
  PROF_TAIL, PROF_LAT) = range(9)
 PRECISIONS = {"fp32": LG_FP32, "bf16": LG_BF16, "fp8w": LG_FP8W, "fp8": LG_FP8W, "fp16": LG_FP16}

@@ -252,8 +252,9 @@ __global__ void __launch_bounds__(384) softmax_kernel(const HeadIn h, int B, flo
     if (p < kPoints) probs[(size_t)b * kPoints + p] = e / den;
 }
 
-// innerproduct<361,H> (+act) then innerproduct<H,1>, then tanh or (1+tanh)/2
-// (Network.cpp:395-423, 733-737), as a tiled GEMM over boards.
+// innerproduct<361,H> (+act) then innerproduct<H,1>, then tanh, (1+tanh)/2
+// (Network.cpp:395-423, 733-737) or no map (value_map 2), as a tiled GEMM
+// over boards.
 // value_fc1_kernel: one CTA = 32 boards x 64 hidden units x one of
 // kFcSplit fixed K ranges of the 361 inputs.  The 32 boards' head outputs
 // for the range are formed in shared memory from the head partial sums, the
@@ -349,8 +350,8 @@ __global__ void __launch_bounds__(256) value_final_kernel(const float *__restric
     }
     s = block_reduce<256>(s, false, red);
     if (threadIdx.x == 0) {
-        const float t = tanhf(b2 + s);
-        value[b] = value_map ? (1.0f + t) / 2.0f : t;
+        const float x = b2 + s, t = tanhf(x);
+        value[b] = value_map == 2 ? x : (value_map ? (1.0f + t) / 2.0f : t);
     }
 }
 

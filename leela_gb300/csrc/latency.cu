@@ -437,10 +437,10 @@ __global__ void __launch_bounds__(kLT, 1) lat_kernel(const LatParams p) {
                     __threadfence();
                     const int old = atom_acq_rel_add(p.cnt + kLatCntFc + b, 1);
                     if (old == kLatSplits - 1) {
-                        float t = p.b2;
-                        for (int k = 0; k < kLatSplits; ++k) t += *(volatile float *)(p.fcv + b * kLatSplits + k);
-                        t = tanhf(t);
-                        p.value[b] = p.value_map ? (1.0f + t) / 2.0f : t;
+                        float x = p.b2;
+                        for (int k = 0; k < kLatSplits; ++k) x += *(volatile float *)(p.fcv + b * kLatSplits + k);
+                        const float t = tanhf(x);
+                        p.value[b] = p.value_map == 2 ? x : (p.value_map ? (1.0f + t) / 2.0f : t);
                     }
                 }
             }

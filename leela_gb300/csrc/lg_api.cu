@@ -51,7 +51,7 @@ bool valid_desc(const lg_net_desc *d) {
     return d && d->c_in > 0 && d->c_in <= 64 && d->width1 > 0 && d->width > 0 && d->n3x3 >= 0 &&
            d->n3x3 < kMaxConv - 2 && (d->head_k == 1 || d->head_k == 3) &&
            (d->act == LG_ACT_ELU || d->act == LG_ACT_RELU) &&
-           (!d->value_head || (d->fc_hidden > 0 && d->fc_hidden <= 4096)) &&
+           (!d->value_head || (d->fc_hidden > 0 && d->fc_hidden <= 4096)) && d->value_map >= 0 && d->value_map <= 2 &&
            d->precision >= LG_FP32 && d->precision <= LG_FP16;
 }
 
@@ -947,8 +947,10 @@ int next_pow2(int x) {
 // Launches one server batch whose planes are already in pinned slot `slot`:
 // a CUDA graph per (net, bucket, temperature, slot) holding the copy in, the
 // forward and the copy out; completion is recorded on srv_done[slot].
+// `net` may be LG_NET_POLICY_LOGITS: the policy net, head outputs copied out.
 int server_launch(lg_ctx *c, int slot, int net, int nb, float T) {
-    Net &n = c->nets[net];
+    const bool logits = net == LG_NET_POLICY_LOGITS;
+    Net &n = c->nets[logits ? LG_NET_POLICY : net];
     const size_t per_in = (size_t)n.d.c_in * kPoints;
     uint32_t tbits;
     std::memcpy(&tbits, &T, 4);
@@ -960,12 +962,13 @@ int server_launch(lg_ctx *c, int slot, int net, int nb, float T) {
         cudaMemcpyAsync(c->d_planes, c->srv_planes[slot], (size_t)nb * per_in, cudaMemcpyHostToDevice,
                         c->stream);
         int nl = 0;
-        int rc = forward(c, net, c->d_planes, nb, T, c->d_probs, nullptr, c->d_value, c->stream, &nl);
+        int rc = forward(c, logits ? LG_NET_POLICY : net, c->d_planes, nb, T, c->d_probs,
+                         logits ? c->d_logits : nullptr, c->d_value, c->stream, &nl);
         if (n.d.value_head)
             cudaMemcpyAsync(c->srv_out[slot], c->d_value, (size_t)nb * sizeof(float), cudaMemcpyDeviceToHost,
                             c->stream);
         else
-            cudaMemcpyAsync(c->srv_out[slot], c->d_probs, (size_t)nb * kPoints * sizeof(float),
+            cudaMemcpyAsync(c->srv_out[slot], logits ? c->d_logits : c->d_probs, (size_t)nb * kPoints * sizeof(float),
                             cudaMemcpyDeviceToHost, c->stream);
         cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
         if (rc) {
@@ -1042,7 +1045,7 @@ void worker_main(lg_ctx *c) {
             f.reqs = std::move(batch);
             f.net = f.reqs[0].net;
             f.slot = slot;
-            Net &n = c->nets[f.net];
+            Net &n = c->nets[f.net == LG_NET_VALUE ? LG_NET_VALUE : LG_NET_POLICY];
             const size_t per_in = (size_t)n.d.c_in * kPoints;
             int total = 0;
             for (auto &r : f.reqs) total += r.B;
@@ -1073,7 +1076,7 @@ void worker_main(lg_ctx *c) {
                     std::lock_guard<std::mutex> g(c->mu);
                     rc = server_finish(c, f.slot);
                 }
-                const int per_out = c->nets[f.net].d.value_head ? 1 : kPoints;
+                const int per_out = f.net == LG_NET_VALUE ? 1 : kPoints;
                 size_t o = 0;
                 for (auto &r : f.reqs) {
                     if (rc == LG_OK)
@@ -1334,8 +1337,9 @@ extern "C" int lg_value_device(lg_ctx *c, const uint8_t *planes, int B, float *v
 
 extern "C" int lg_submit(lg_ctx *c, int net, const uint8_t *planes, int B, float temperature,
                          float *out, void *tag) {
-    if (!c || (net != LG_NET_POLICY && net != LG_NET_VALUE) || !c->nets[net].present || !planes ||
-        !out || B < 1 || B > c->max_batch || !(temperature > 0.0f)) {
+    if (!c || net < LG_NET_POLICY || net > LG_NET_POLICY_LOGITS ||
+        !c->nets[net == LG_NET_VALUE ? LG_NET_VALUE : LG_NET_POLICY].present || !planes || !out || B < 1 ||
+        B > c->max_batch || !(temperature > 0.0f)) {
         lg_set_error("lg_submit: bad arguments");
         return LG_ERR_ARG;
     }

@@ -274,7 +274,7 @@ int or_forward_f32(const or_net *n, const float *w, const uint8_t *planes, float
         float s = 0.0f;
         for (int i = 0; i < n->fc_hidden; ++i) s = s + W2[i] * b[i];
         float x = b2[0] + s;
-        out[0] = n->value_map ? (1.0f + tanhf(x)) / 2.0f : tanhf(x);
+        out[0] = n->value_map == 2 ? x : (n->value_map ? (1.0f + tanhf(x)) / 2.0f : tanhf(x));
     }
     free(a); free(b); free(col);
     return 0;
@@ -325,7 +325,7 @@ int or_forward_f64(const or_net *n, const float *w, const uint8_t *planes, doubl
         double s = 0.0;
         for (int i = 0; i < n->fc_hidden; ++i) s += (double)W2[i] * b[i];
         double x = (double)b2[0] + s;
-        out[0] = n->value_map ? (1.0 + tanh(x)) / 2.0 : tanh(x);
+        out[0] = n->value_map == 2 ? x : (n->value_map ? (1.0 + tanh(x)) / 2.0 : tanh(x));
     }
     free(a); free(b); free(col); free(Wd);
     return 0;

@@ -59,7 +59,7 @@ typedef struct or_net {
     int act_head;   /* 1 = activation after the head conv too */
     int value_head; /* 0 = policy (361 logits), 1 = value (FC head) */
     int fc_hidden;
-    int value_map;  /* 0 = tanh, 1 = (1 + tanh) / 2 */
+    int value_map;  /* 0 = tanh, 1 = (1 + tanh) / 2, 2 = none (the FC output itself) */
 } or_net;
 
 int or_n_conv(const or_net *n);

@@ -71,10 +71,14 @@ def test_lowp_vs_fp64(gpu_lib, weights, positions, f64_refs, prec):
 
 
 def test_bf16_batch_independent(gpu_lib, weights, positions):
-    """A position's result does not depend on its batch or its slot in it."""
+    """For one kernel choice, a position's result does not depend on its
+    batch or its slot in it (bit for bit).  (Buckets of up to 8 positions
+    default to the small-batch kernel, whose FP32 sums run in another
+    order; here they are set to the per-layer kernels.)"""
     lg = gpu_lib
     with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
                     max_batch=64) as c:
+        c.set_tuning(1, 0, 0)
         planes = positions["planes_p"][:37, :24]
         full = c.policy(planes)
         one = np.concatenate([c.policy(planes[i:i + 1]) for i in (0, 17, 36)])
