@@ -310,6 +310,16 @@ LG_API int lg_profile_read(lg_ctx *ctx, int kind, long long *launches, double *t
  * (n >= 1) fails with LG_ERR_CUDA before it reaches the GPU; 0 disarms. */
 LG_API int lg_inject_fault(lg_ctx *ctx, int nth_call);
 
+/* Test hook (device-side bounded waits): the next launch of kernel `kind`
+ * (0: the persistent trunk -- the first item of the second 3x3 layer; 1:
+ * the small-batch kernel -- row 0 of the second layer) waits for a flag
+ * that nothing publishes, with its wait limits cut to `polls` (0: 4096).
+ * The wait runs out, the kernel records an error word and unwinds (no trap,
+ * no fault), a blocking call returns LG_ERR_DEVICE, and the context keeps
+ * working.  kind -1 disarms.  No reference counterpart (the engine's own
+ * final wait, OpenCL.cpp:575-577, is unbounded). */
+LG_API int lg_inject_stall(lg_ctx *ctx, int kind, int polls);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,7 +49,7 @@ namespace {
 constexpr int kLT = 256;                       // threads per CTA
 constexpr int kRowPts = 20;                    // 19 points + one pad column
 constexpr int kPitch = 24;                     // staged input row: x = -r .. 19 + r
-constexpr uint32_t kLatPolls = 1u << 22;       // x ~32-64 ns: bounded at ~0.3 s
+constexpr uint32_t kLatPolls = 1u << 22;       // default limit, x ~32-64 ns: bounded at ~0.3 s
 constexpr size_t kPartBuf = (size_t)kLatSplits * kLatMaxRows * kRowPts * 128;  // floats per parity
 
 __device__ __forceinline__ float lat_act(float v, int act) {
@@ -78,12 +78,12 @@ __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_g
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Polls one counter until it reaches `want`: spins, then sleeps between
-// polls; gives up after kLatPolls polls or as soon as another CTA has
+// polls; gives up after `limit` polls or as soon as another CTA has
 // reported an error.  Returns false on either.
-__device__ __forceinline__ bool poll_one(const int *c, int want, const int *err) {
+__device__ __forceinline__ bool poll_one(const int *c, int want, const int *err, uint32_t limit) {
     uint32_t n = 0;
     while (ld_acq(c) < want) {
-        if (++n >= kLatPolls || *(volatile const int *)err != 0) return false;
+        if (++n >= limit || *(volatile const int *)err != 0) return false;
         if (n > 64) __nanosleep(32);
     }
     return true;
@@ -91,9 +91,10 @@ __device__ __forceinline__ bool poll_one(const int *c, int want, const int *err)
 
 // The CTA waits until counters cnt[lo..hi] (hi - lo < kLT) reach `want`,
 // one polling thread per counter; true for every thread if all did.
-__device__ __forceinline__ bool wait_rows(const int *cnt, int lo, int hi, int want, const int *err, bool alive) {
+__device__ __forceinline__ bool wait_rows(const int *cnt, int lo, int hi, int want, const int *err, bool alive,
+                                          uint32_t limit) {
     const int t = threadIdx.x;
-    const bool bad = t <= hi - lo && alive && !poll_one(cnt + lo + t, want, err);
+    const bool bad = t <= hi - lo && alive && !poll_one(cnt + lo + t, want, err, limit);
     return !__syncthreads_or(bad || !alive);
 }
 
@@ -227,8 +228,11 @@ __global__ void __launch_bounds__(kLT, 1) lat_kernel(const LatParams p) {
         const int nx = (mma ? 24 : kRowPts) + 2 * r;
         for (int row = cta / kLatSplits; row < rows; row += rstep) {
             const int b = row / kBoard, y = row % kBoard;
+            // (test hook: the stalled row of layer 1 waits for a count no
+            // unit reaches)
+            const int want = (l == 1 && row == p.stall_row) ? kLatSplits + (1 << 20) : kLatSplits;
             if (l > 0 && !wait_rows(p.cnt + (l - 1) * kLatMaxRows, b * kBoard + max(0, y - rw),
-                                    b * kBoard + min(kBoard - 1, y + rw), kLatSplits, p.err, alive)) {
+                                    b * kBoard + min(kBoard - 1, y + rw), want, p.err, alive, p.poll_limit)) {
                 fail(91);
                 continue;
             }
@@ -359,7 +363,8 @@ __global__ void __launch_bounds__(kLT, 1) lat_kernel(const LatParams p) {
     for (int u = cta; u < nfin; u += G) {
         const int b = p.value_head ? u / kLatSplits : u, fs = p.value_head ? u % kLatSplits : 0;
         __syncthreads();
-        if (!wait_rows(p.cnt + hl * kLatMaxRows, b * kBoard, b * kBoard + kBoard - 1, kLatSplits, p.err, alive)) {
+        if (!wait_rows(p.cnt + hl * kLatMaxRows, b * kBoard, b * kBoard + kBoard - 1, kLatSplits, p.err, alive,
+                       p.poll_limit)) {
             fail(92);
             continue;
         }
@@ -486,7 +491,9 @@ int lat_grid(int B, int sm_count) {
     return g - g % kLatSplits;
 }
 
-int launch_lat(const LatParams &p, int mode, int sm_count, cudaStream_t s) {
+int launch_lat(const LatParams &p_in, int mode, int sm_count, cudaStream_t s) {
+    LatParams p = p_in;
+    if (!p.poll_limit) p.poll_limit = kLatPolls;
     const int G = lat_grid(p.B, sm_count);
     if (p.B < 1 || p.B > kLatMaxB || p.nl < 2 || p.nl > kLatMaxLayers || G < kLatSplits || mode < 0 || mode > 2) {
         lg_set_error("latency kernel: bad arguments (B=%d, layers=%d)", p.B, p.nl);

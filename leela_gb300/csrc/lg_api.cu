@@ -164,6 +164,11 @@ struct lg_ctx {
     std::atomic<long long> launches{0};
     std::atomic<long long> batches{0};
     std::atomic<int> fault_in{0};
+    // test hook (lg_inject_stall): the next launch of kernel kind stall_kind
+    // (0 persistent trunk, 1 small-batch kernel) has one wait that nothing
+    // satisfies, with its wait limits cut to stall_polls; -1 = disarmed
+    int stall_kind = -1;
+    uint32_t stall_polls = 0;
     // batching server
     struct Req {
         int net;
@@ -593,6 +598,12 @@ int forward_lat(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float 
     p.value_map = d.value_map;
     p.value = value;
     p.fcv = c->lat_fcv;
+    p.stall_row = -1;
+    if (c->stall_kind == 1) {
+        p.stall_row = 0;
+        p.poll_limit = c->stall_polls;
+        c->stall_kind = -1;
+    }
     int rc;
     {
         ProfScope ps(c, prof, LG_PROF_LAT, s);
@@ -692,6 +703,12 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
             tt.rows = B * kL3Board;
             tt.nl = (int)n.tc.size() - 1;
             tt.f16 = f16;
+            if (c->stall_kind == 0) {
+                // the first item of the second 3x3 layer
+                tt.stall_item = (fuse_first ? (tt.rows5 + 255) / 256 : 0) + (tt.rows + 255) / 256;
+                tt.wait_limit = tt.poll_limit = c->stall_polls;
+                c->stall_kind = -1;
+            }
             int rc;
             {
                 ProfScope ps(c, prof, LG_PROF_TC_TRUNK, s);
@@ -840,9 +857,12 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
         auto key = std::make_tuple(net, nb, n.d.value_head ? 0u : tbits,
                                    (want_logits ? 1 : 0) + 8 * slot + (boards ? 16 : 0));
         auto it = c->graphs.find(key);
-        if (it == c->graphs.end()) {
+        // an armed stall (lg_inject_stall) runs this chunk outside the graph
+        // cache, so that no cached graph keeps the stalled launch
+        const bool direct = c->stall_kind >= 0;
+        if (direct || it == c->graphs.end()) {
             cudaGraph_t g;
-            LG_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            if (!direct) LG_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             int nl = 0;
             if (boards) {
                 cudaMemcpyAsync(c->d_boards, hp[slot], in_bytes, cudaMemcpyHostToDevice, c->stream);
@@ -873,22 +893,32 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
                     cudaMemcpyAsync(hl[slot], c->d_logits, (size_t)nb * kPoints * sizeof(float),
                                     cudaMemcpyDeviceToHost, c->stream);
             }
-            cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
-            if (rc) {
-                if (ce == cudaSuccess) cudaGraphDestroy(g);
-                finish(slot ^ 1);
-                return rc;
+            if (direct) {
+                if (rc) {
+                    finish(slot ^ 1);
+                    return rc;
+                }
+                c->launches += nl;
+            } else {
+                cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+                if (rc) {
+                    if (ce == cudaSuccess) cudaGraphDestroy(g);
+                    finish(slot ^ 1);
+                    return rc;
+                }
+                LG_CUDA_TRY(ce);
+                cudaGraphExec_t ge;
+                cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+                cudaGraphDestroy(g);
+                LG_CUDA_TRY(ie);
+                it = c->graphs.emplace(key, std::make_pair(ge, nl)).first;
             }
-            LG_CUDA_TRY(ce);
-            cudaGraphExec_t ge;
-            cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
-            cudaGraphDestroy(g);
-            LG_CUDA_TRY(ie);
-            it = c->graphs.emplace(key, std::make_pair(ge, nl)).first;
         }
-        LG_CUDA_TRY(cudaGraphLaunch(it->second.first, c->stream));
+        if (!direct) {
+            LG_CUDA_TRY(cudaGraphLaunch(it->second.first, c->stream));
+            c->launches += it->second.second;
+        }
         LG_CUDA_TRY(cudaEventRecord(c->host_done[slot], c->stream));
-        c->launches += it->second.second;
         pend[slot].b0 = b0;
         pend[slot].nb = nb;
         pend[slot].live = true;
@@ -1393,6 +1423,17 @@ extern "C" int lg_stats(lg_ctx *c, long long *kernel_launches, long long *batche
 extern "C" int lg_inject_fault(lg_ctx *c, int nth_call) {
     if (!c || nth_call < 0) return LG_ERR_ARG;
     c->fault_in = nth_call;
+    return LG_OK;
+}
+
+extern "C" int lg_inject_stall(lg_ctx *c, int kind, int polls) {
+    if (!c || kind < -1 || kind > 1 || polls < 0) {
+        lg_set_error("lg_inject_stall: bad arguments");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> g(c->mu);
+    c->stall_kind = kind;
+    c->stall_polls = (uint32_t)(polls ? polls : 1 << 12);
     return LG_OK;
 }
 

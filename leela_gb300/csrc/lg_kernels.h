@@ -105,6 +105,10 @@ struct TcTrunk {
     const float *bias0 = nullptr, *scale0 = nullptr;
     int rows5 = 0;
     int f16 = 0;                 // activations and weights are FP16 (else BF16)
+    // wait limits (0: the defaults) and the test hook that makes one item
+    // wait for a flag that nothing publishes (-1: none)
+    uint32_t wait_limit = 0, poll_limit = 0;
+    int stall_item = -1;
 };
 // flags: trunk_flag_ints(rows, rows5) ints of device scratch (reset by the launch).
 int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
@@ -163,6 +167,8 @@ struct LatParams {
     int H, value_map;
     float *value;
     float *fcv;                // [kLatMaxB][8]
+    uint32_t poll_limit;       // polls of one row counter before it gives up
+    int stall_row;             // test hook: this layer-1 row waits for a count no unit reaches (-1: none)
 };
 size_t lat_part_floats();
 size_t lat_smem_bytes();

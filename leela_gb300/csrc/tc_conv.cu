@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint8_t *wst = smem + 2 * C::WIN_BYTES;    // S x WST_BYTES
 
     __shared__ uint64_t win_full[2], win_empty[2], w_full[C::S], w_empty[C::S];
-    __shared__ uint64_t acc_full[2], acc_empty[2];
+    __shared__ uint64_t acc_full[2], acc_empty[2], mma_done;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
     __shared__ float s_bias[N], s_scale[N], s_head[N];
@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mbar_init(&w_full[i], 1);
             mbar_init(&w_empty[i], 1);
         }
+        mbar_init(&mma_done, 1);
         abort_flag = 0;
         fence_mbar_init();
         prefetch_tensormap(&in_map);
@@ -256,6 +257,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 mma_commit(&acc_full[acc]);
             }
         done_mma:;
+            // every MMA this thread issued has completed before the CTA can
+            // free its tensor memory (also after a wait gave up)
+            mma_commit(&mma_done);
+            mbar_wait(&mma_done, 0, 1u << 20);
         }
     } else {
         // ------------------------------------------------ epilogue
@@ -383,24 +388,19 @@ __device__ __forceinline__ float warp_transpose_sum(float (&a)[32], int lane) {
     return a[0];
 }
 
-// Fused 1x1 head: each of a row group's four epilogue warps (warps
-// 2 + 4 rq .. 5 + 4 rq, one 32-channel quarter each) holds its partial sum for
-// the group's 32 rows (lane = row); they are added in quarter order 0..3 in
-// shared memory (red: 128 floats of this group) and quarter 0 writes the
-// head output of each board point.  All four warps must call it.
+// Fused 1x1 head: each of a row group's four epilogue warps (one 32-channel
+// quarter each) holds its partial sum for the group's 32 rows (lane = row)
+// and writes it to its own part, parts[quarter * part_stride + point]; the
+// finish kernels add the four parts in quarter order 0..3.  No barrier
+// between the warps, so a warp that gave up on a bounded wait can never
+// leave the others waiting.
 template <int KIND>
-__device__ __forceinline__ void head_store(float sum, float *red, int rq, int quarter, int lane, int row, int rows,
-                                           float *parts) {
-    red[quarter * 32 + lane] = sum;
-    named_bar_sync(1 + rq, 128);
-    if (quarter == 0) {
-        const float tot = ((red[lane] + red[32 + lane]) + red[64 + lane]) + red[96 + lane];
-        int orow, point;
-        bool valid;
-        row_target<KIND>(row, rows, orow, valid, point);
-        if (valid) parts[point] = tot;
-    }
-    named_bar_sync(1 + rq, 128);
+__device__ __forceinline__ void head_store(float sum, int quarter, int row, int rows, float *parts,
+                                           size_t part_stride) {
+    int orow, point;
+    bool valid;
+    row_target<KIND>(row, rows, orow, valid, point);
+    if (valid) parts[(size_t)quarter * part_stride + point] = sum;
 }
 
 // Kernel T work split: the rows are cut into 32-row blocks, each CTA takes
@@ -427,13 +427,13 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
     uint8_t *wst = stg + C::STG_TOTAL;            // S x WST_BYTES
 
     __shared__ uint64_t win_full[C::NWIN], win_empty[C::NWIN], w_full[C::S], w_empty[C::S];
-    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4];
+    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], mma_done;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    __shared__ float head_red[HEAD ? 4 * 128 : 1];
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     if (tid == 0) {
+        mbar_init(&mma_done, 1);
         for (int i = 0; i < C::NWIN; ++i) {
             mbar_init(&win_full[i], 1);
             mbar_init(&win_empty[i], 1);
@@ -539,6 +539,8 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                 mma_commit(&acc_full[acc]);
             }
         done_mma:;
+            mma_commit(&mma_done);
+            mbar_wait(&mma_done, 0, 1u << 20);
         }
     } else {
         // ------------------------------------------------ epilogue
@@ -581,8 +583,8 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
                 if (HEAD) {
 #pragma unroll
                     for (int j = 0; j < 32; ++j) f[j] *= hw;
-                    head_store<KIND>(warp_transpose_sum(f, lane), head_red + rq * 128, rq, quarter, lane,
-                                     q_base + c * 32 + lane, p.rows, p.parts);
+                    head_store<KIND>(warp_transpose_sum(f, lane), quarter, q_base + c * 32 + lane, p.rows, p.parts,
+                                     p.part_stride);
                 } else if (C::STAGED) {
                     // Rows q_base + c*32 .. +31 -> staging buffer of this row
                     // group as [32 rows][128 channels] BF16 (pad rows 0), then
@@ -683,6 +685,9 @@ struct TrunkParams {
     size_t part_stride;
     int *flags;           // [n3] chunk flags, the item counter, [n5] first-layer chunk flags
     int *err;
+    uint32_t wait_limit;  // polls of one mbarrier wait before it gives up
+    uint32_t poll_limit;  // polls of one dependency flag before it gives up
+    int stall_item;       // test hook: this item waits for a flag nothing sets (-1: none)
 };
 
 // Shared memory of kernel "trunk": window slots sized for the first layer's
@@ -714,12 +719,13 @@ constexpr int kItemRing = 4;               // item descriptors in flight per CTA
 // Returns false if a weight stage did not arrive within the wait limit.
 template <int KIND, int NTAPS, int WPRE>
 __device__ __forceinline__ bool issue_taps(uint32_t d_tmem, uint64_t a_desc0, uint64_t b_desc, uint32_t idesc,
-                                           bool first_half, uint32_t &g, uint64_t *w_full, uint64_t *w_empty) {
+                                           bool first_half, uint32_t &g, uint64_t *w_full, uint64_t *w_empty,
+                                           uint32_t wl) {
     constexpr int kStage16 = TcTCfg<2, 0>::WST_BYTES >> 4;
 #pragma unroll
     for (int t = 0; t < NTAPS; ++t, ++g) {
         const int s = g & 3;
-        if (!mbar_wait(&w_full[s], (g >> 2) & 1, kWaitLimit)) return false;
+        if (!mbar_wait(&w_full[s], (g >> 2) & 1, wl)) return false;
         tc_fence_after();
         const uint64_t a = a_desc0 + (uint64_t)(s * kStage16);
         const uint64_t b = b_desc + (uint64_t)((WPRE + (KIND == 0 ? (t / 3 - 1) * kL3Pitch + (t % 3 - 1)
@@ -732,10 +738,10 @@ __device__ __forceinline__ bool issue_taps(uint32_t d_tmem, uint64_t a_desc0, ui
     return true;
 }
 
-__device__ __forceinline__ bool poll_flag(const int *f, int want) {
+__device__ __forceinline__ bool poll_flag(const int *f, int want, uint32_t limit) {
     uint32_t n = 0;
-    while (ld_acquire_gpu(f) < want && ++n < kFlagPolls) __nanosleep(64);
-    return n < kFlagPolls;
+    while (ld_acquire_gpu(f) < want && ++n < limit) __nanosleep(64);
+    return n < limit;
 }
 
 template <bool HEAD, bool F16>
@@ -759,14 +765,14 @@ __global__ void __maxnreg__(96)
     // item_done: a ring of 4 (an epilogue warp can be up to two items ahead
     // of the slowest: starting item x needs every warp to have read item
     // x-2's accumulator, hence to have arrived for item x-3)
-    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], item_done[4];
+    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], item_done[4], mma_done;
     __shared__ uint64_t item_full[kItemRing], item_empty[kItemRing];
     __shared__ int item_id[kItemRing];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    __shared__ float head_red[HEAD ? 4 * 128 : 1];
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+#define WAIT_LIM (p.wait_limit)  // mbarrier waits (try_wait polls): read from the parameter bank at each use
     const int n3 = (p.rows + C::TP - 1) / C::TP;
     const int n5 = p.rows5 > 0 ? (p.rows5 + C::TP - 1) / C::TP : 0;
     const int first = n5 > 0 ? 1 : 0;
@@ -805,6 +811,7 @@ __global__ void __maxnreg__(96)
             mbar_init(&item_empty[i], 2 + kEpiWarpsT);  // weight producer, MMA issuer, epilogue warps
         }
         for (int i = 0; i < 4; ++i) mbar_init(&item_done[i], kEpiWarpsT);
+        mbar_init(&mma_done, 1);
         abort_flag = 0;
         fence_mbar_init();
         prefetch_tensormap(&in_a);
@@ -838,9 +845,9 @@ __global__ void __maxnreg__(96)
                 const uint32_t qk = (uint32_t)(q / kItemRing);
                 // Claim only once the item ring and the next window slot are
                 // free, so that a claimed item is worked on at once.
-                bool ok = mbar_wait(&item_empty[slot], (qk & 1) ^ 1, kWaitLimit);
+                bool ok = mbar_wait(&item_empty[slot], (qk & 1) ^ 1, WAIT_LIM);
                 const int ws0 = wn % C::NWIN;
-                ok = ok && mbar_wait(&win_empty[ws0], ((wn / C::NWIN) & 1) ^ 1, kWaitLimit);
+                ok = ok && mbar_wait(&win_empty[ws0], ((wn / C::NWIN) & 1) ^ 1, WAIT_LIM);
                 int it = -1;
                 if (ok && !abort_flag) {
                     it = atomicAdd(p.flags + n3, 1);
@@ -864,7 +871,7 @@ __global__ void __maxnreg__(96)
                     const int lo5 = max(0, lo3 - (hi3 - 1) / kL3Board - kBoard);
                     const int hi5 = min(p.rows5 - 1, hi3 - 1);
                     for (int jj = lo5 / C::TP; jj <= hi5 / C::TP; ++jj)
-                        if (!poll_flag(flags0 + jj, 1)) {
+                        if (!poll_flag(flags0 + jj, 1, p.poll_limit)) {
                             fail(71);
                             goto done_windows;
                         }
@@ -872,8 +879,11 @@ __global__ void __maxnreg__(96)
                 } else if (!fl && k > 0) {
                     // layer k-1 of chunks j-1 .. j+1 is stored
                     const int lo = max(0, j - 1), hi = min(n3 - 1, j + 1);
+                    // (test hook: the stalled item waits for a layer count
+                    // no item ever publishes)
+                    const int want = it == p.stall_item ? (1 << 30) : k;
                     for (int jj = lo; jj <= hi; ++jj)
-                        if (!poll_flag(p.flags + jj, k)) {
+                        if (!poll_flag(p.flags + jj, want, p.poll_limit)) {
                             fail(71);
                             goto done_windows;
                         }
@@ -887,7 +897,7 @@ __global__ void __maxnreg__(96)
                     const int ws = wn % C::NWIN;
                     const uint32_t wk = wn / C::NWIN;
                     // (the first half's slot was waited for before the claim)
-                    if (h > 0 && !mbar_wait(&win_empty[ws], (wk & 1) ^ 1, kWaitLimit)) { fail(73); goto done_windows; }
+                    if (h > 0 && !mbar_wait(&win_empty[ws], (wk & 1) ^ 1, WAIT_LIM)) { fail(73); goto done_windows; }
                     mbar_arrive_expect_tx(&win_full[ws], bytes);
                     for (int sb = 0; sb < 2; ++sb)
                         tma_load_2d(win + ws * C::WIN_SLOT + sb * sub * 128, im, &win_full[ws], h * 64,
@@ -902,7 +912,7 @@ __global__ void __maxnreg__(96)
             uint32_t g = 0;
             for (int q = 0;; ++q) {
                 const int slot = q % kItemRing;
-                if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, kWaitLimit)) { fail(70); break; }
+                if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, WAIT_LIM)) { fail(70); break; }
                 const int it = item_id[slot];
                 mbar_arrive(&item_empty[slot]);
                 if (it < 0) break;
@@ -916,7 +926,7 @@ __global__ void __maxnreg__(96)
                     for (int t = 0; t < ntaps; ++t, ++g) {
                         const int s = g % C::S;
                         const uint32_t k = g / C::S;
-                        if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, kWaitLimit)) { fail(74); goto done_weights; }
+                        if (!mbar_wait(&w_empty[s], (k & 1) ^ 1, WAIT_LIM)) { fail(74); goto done_weights; }
                         mbar_arrive_expect_tx(&w_full[s], C::WST_BYTES);
                         tma_load_2d(wst + s * C::WST_BYTES, wm, &w_full[s], 0, ((wl * ntaps + t) * HALVES + h) * NO);
                     }
@@ -937,7 +947,7 @@ __global__ void __maxnreg__(96)
             uint32_t g = 0, wn = 0;
             for (int q = 0;; ++q) {
                 const int slot = q % kItemRing;
-                if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, kWaitLimit)) { fail(75); break; }
+                if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, WAIT_LIM)) { fail(75); break; }
                 const int it = item_id[slot];
                 mbar_arrive(&item_empty[slot]);
                 if (it < 0) break;
@@ -950,7 +960,7 @@ __global__ void __maxnreg__(96)
                 const uint32_t idesc = idesc_16(128, nrows, F16);
                 const int acc = q & 1;
                 const uint32_t ak = (uint32_t)(q >> 1);
-                if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, kWaitLimit)) { fail(76); break; }
+                if (!mbar_wait(&acc_empty[acc], (ak & 1) ^ 1, WAIT_LIM)) { fail(76); break; }
                 tc_fence_after();
                 const uint32_t d_tmem = tmem + (uint32_t)(acc * C::TP);
                 bool ok = true;
@@ -958,19 +968,23 @@ __global__ void __maxnreg__(96)
                 for (int h = 0; h < HALVES && ok; ++h, ++wn) {
                     const int ws = wn % C::NWIN;
                     const uint32_t wk = wn / C::NWIN;
-                    if (!mbar_wait(&win_full[ws], wk & 1, kWaitLimit)) { fail(77); ok = false; break; }
+                    if (!mbar_wait(&win_full[ws], wk & 1, WAIT_LIM)) { fail(77); ok = false; break; }
                     tc_fence_after();
                     const uint64_t b_desc = b_desc0 + (uint64_t)(ws * (C::WIN_SLOT >> 4));
                     ok = fl ? issue_taps<1, C1::NTAPS, C1::WPRE>(d_tmem, a_desc0, b_desc, idesc, h == 0, g, w_full,
-                                                                 w_empty)
+                                                                 w_empty, WAIT_LIM)
                             : issue_taps<0, C0::NTAPS, C0::WPRE>(d_tmem, a_desc0, b_desc, idesc, h == 0, g, w_full,
-                                                                 w_empty);
+                                                                 w_empty, WAIT_LIM);
                     if (!ok) { fail(78); break; }
                     mma_commit(&win_empty[ws]);
                 }
                 if (!ok) break;
                 mma_commit(&acc_full[acc]);
             }
+            // every MMA this thread issued has completed before the CTA can
+            // free its tensor memory (also after a wait gave up)
+            mma_commit(&mma_done);
+            mbar_wait(&mma_done, 0, 1u << 20);
         }
     } else {
         // ------------------------------------------------ epilogue
@@ -981,7 +995,7 @@ __global__ void __maxnreg__(96)
         uint32_t uses = 0, done_n = 0;
         for (int q = 0;; ++q) {
             const int slot = q % kItemRing;
-            if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, kWaitLimit)) { fail(79); break; }
+            if (!mbar_wait(&item_full[slot], (uint32_t)(q / kItemRing) & 1, WAIT_LIM)) { fail(79); break; }
             const int it = item_id[slot];
             __syncwarp();
             if (lane == 0) mbar_arrive(&item_empty[slot]);
@@ -1001,7 +1015,7 @@ __global__ void __maxnreg__(96)
             const int nhalf = max(0, min(2, (nrows - rq * 64 + 31) / 32));
             const int acc = q & 1;
             const uint32_t ak = (uint32_t)(q >> 1);
-            if (!mbar_wait(&acc_full[acc], ak & 1, kWaitLimit)) { fail(80); break; }
+            if (!mbar_wait(&acc_full[acc], ak & 1, WAIT_LIM)) { fail(80); break; }
             tc_fence_after();
             const uint32_t t_base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * C::TP + rq * 64);
             const int q_base = cs + rq * 64;
@@ -1039,7 +1053,7 @@ __global__ void __maxnreg__(96)
                     }
                     if (c >= nhalf || bad) continue;
                     const uint32_t use = uses++;
-                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) {
+                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, WAIT_LIM)) {
                         fail(81);
                         bad = true;
                         continue;
@@ -1074,7 +1088,7 @@ __global__ void __maxnreg__(96)
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&stg_full[rq]);
                     if (quarter == 0 && lane == 0) {
-                        if (!mbar_wait(&stg_full[rq], use & 1, kWaitLimit)) {
+                        if (!mbar_wait(&stg_full[rq], use & 1, WAIT_LIM)) {
                             fail(82);
                         } else {
                             uint8_t *buf = stg + rq * C::STG_BYTES;
@@ -1108,12 +1122,12 @@ __global__ void __maxnreg__(96)
 #pragma unroll
                     for (int jj = 0; jj < 32; ++jj)
                         f[jj] = act_apply(fmaf(__uint_as_float(v[jj]), scale, bias), p.act) * hw;
-                    head_store<0>(warp_transpose_sum(f, lane), head_red + rq * 128, rq, quarter, lane,
-                                  q_base + c * 32 + lane, p.rows, p.parts);
+                    head_store<0>(warp_transpose_sum(f, lane), quarter, q_base + c * 32 + lane, p.rows, p.parts,
+                                  p.part_stride);
                 } else {
                     const uint32_t use = uses++;
                     uint8_t *buf = stg + rq * C::STG_BYTES;
-                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, kWaitLimit)) {
+                    if (!mbar_wait(&stg_empty[rq], (use & 1) ^ 1, WAIT_LIM)) {
                         fail(81);
                         bad = true;
                         continue;
@@ -1159,7 +1173,7 @@ __global__ void __maxnreg__(96)
                     if (lane == 0) mbar_arrive(&stg_full[rq]);
                     if (quarter == 0) {
                         // every lane of the warp holds its row's target; lane 0 stores
-                        const bool ok = lane != 0 || mbar_wait(&stg_full[rq], use & 1, kWaitLimit);
+                        const bool ok = lane != 0 || mbar_wait(&stg_full[rq], use & 1, WAIT_LIM);
                         if (!ok) fail(82);
                         if (!fl) {
                             if (lane == 0 && ok) tma_store_2d(om, buf, 0, q_base + c * 32);
@@ -1202,7 +1216,7 @@ __global__ void __maxnreg__(96)
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&item_done[done_n & 3]);
                 if (warp == 4 && lane == 0) {
-                    if (!mbar_wait(&item_done[done_n & 3], (done_n >> 2) & 1, kWaitLimit)) {
+                    if (!mbar_wait(&item_done[done_n & 3], (done_n >> 2) & 1, WAIT_LIM)) {
                         fail(83);
                     } else {
                         fence_proxy_async_global();
@@ -1234,6 +1248,7 @@ __global__ void __maxnreg__(96)
     if (warp == 1) tmem_dealloc(tmem, 512);
     if (warp == 1) tmem_relinquish();
 }
+#undef WAIT_LIM
 
 // ------------------------------------------------------------------ packing
 
@@ -1345,7 +1360,10 @@ int tc_init_device() {
     return rc;
 }
 
-int tc_head_parts(int n, int variant) { return 1; }
+// Parts the fused head writes: four (one per TMEM lane quarter) for the
+// transposed 128-wide kernels and the trunk, one for the 128-row kernel
+// (variant 1) and the 64-wide nets (kernel A sums all channels per row).
+int tc_head_parts(int n, int variant) { return (n == 128 && variant != 1) ? 4 : 1; }
 
 size_t trunk_flag_ints(int rows, int rows5) {
     return (size_t)(rows + TrunkCfg::TP - 1) / TrunkCfg::TP + 1 + (size_t)(rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP;
@@ -1422,6 +1440,9 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     p.part_stride = part_stride;
     p.flags = flags;
     p.err = err;
+    p.wait_limit = T.wait_limit ? T.wait_limit : kWaitLimit;
+    p.poll_limit = T.poll_limit ? T.poll_limit : kFlagPolls;
+    p.stall_item = T.stall_item;
     const int n3 = (T.rows + TrunkCfg::TP - 1) / TrunkCfg::TP;
     const int n5 = fused ? (T.rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP : 0;
     const int grid = std::min(n5 + T.nl * n3, sm_count);
