@@ -95,12 +95,14 @@ def make_weights():
 
 
 def read_peaks():
+    """(BF16 burst TFLOP/s, BF16 sustained TFLOP/s, HBM GB/s, source)."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             p = json.load(f)
-        return p.get("bf16_tflops_sustained", 1700.0), p.get("hbm_gbs", 6800.0), "measured"
+        return (p.get("bf16_tflops", 1900.0), p.get("bf16_tflops_sustained", 1700.0), p.get("hbm_gbs", 6800.0),
+                "measured")
     except (OSError, ValueError):
-        return 1700.0, 6800.0, "fallback"
+        return 1900.0, 1700.0, 6800.0, "fallback"
 
 
 class ClockSampler:
@@ -340,14 +342,15 @@ def run_ours(args, world, rank, local):
 
     extras = {}
     if rank == 0:
-        extras = secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp)
+        extras = secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp,
+                                        quick=args.quick)
         extras["e2e_planes"] = e2e_planes
         extras["gather"] = gather_throughput(lg, squares, to_move, dev, sp)
 
     if rank != 0:
         ctx.close()
         return
-    peak, hbm, peak_kind = read_peaks()
+    peak_burst, peak_sust, hbm, peak_kind = read_peaks()
     if ntr and tuning.get("conv3x3") == 3:
         # persistent kernel: the 5x5 first layer and all 11 3x3 layers of one net
         kernel_name = "tc_trunk_kernel (5x5 24->128 + 11 x 3x3 128->128 in one launch, batch 256)"
@@ -369,6 +372,7 @@ def run_ours(args, world, rank, local):
     if os.path.exists(tpath):
         with open(tpath) as f:
             traffic = json.load(f).get("tc_trunk_kernel" if ntr else "tc_convT_kernel<2,0,0>")
+    total_ms = sum(x for x in (ms3, msh, msf, mso, mstr, mspk, mstl))
     line = {
         "metric": METRIC, "value": value, "unit": "positions/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
@@ -381,40 +385,83 @@ def run_ours(args, world, rank, local):
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs 142 MB per step > L2 129 MB; no flush"},
         "e2e": e2e,
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_burst, "unit": "TFLOP/s",
+                     "frac": (achieved / peak_burst) if achieved else None, "traffic": traffic,
                      "kernel": kernel_name,
-                     "peak_source": f"bf16_tflops_sustained ({peak_kind})",
-                     "launches": n_dom, "avg_launch_us": avg3 * 1e6,
-                     "flop_per_launch": flop_launch},
-        "kernel_time_share": {
-            "tc_3x3": ms3, "tc_3x3_fused_head": msh, "tc_trunk": mstr, "tc_5x5_first": msf,
-            "pack_planes": mspk, "softmax_value_fc": mstl, "other": mso,
-            "launches": {"tc_3x3": n3, "tc_head": nh, "tc_trunk": ntr, "tc_first": nf,
-                         "pack_planes": npk, "softmax_value_fc": ntl, "other": no}},
+                     "peak_source": f"bf16_tflops, burst ({peak_kind}): the kernel runs in a sub-second "
+                                    f"region at max clocks",
+                     "frac_of_sustained": (achieved / peak_sust) if achieved else None,
+                     "launches": n_dom, "avg_launch_us": avg3 * 1e6, "flop_per_launch": flop_launch},
+        "kernel_time_share": {k: round(v / total_ms, 4) for k, v in (
+            ("tc_trunk", mstr), ("tc_3x3", ms3 + msh), ("tc_5x5_first", msf), ("pack_planes", mspk),
+            ("softmax_value_fc", mstl), ("other", mso)) if v},
         "kernel_choice_batch256": tuning,
         "clocks": clk,
         "gpu_launches": gpu_launches,
         "pair_flop_rate_tflops": FLOP_PAIR_PER_POS * value / world / 1e12,
     }
-    line.update(extras)
+    # the key secondary numbers in the line (short, so that it survives
+    # whole); everything in --detail
+    line["summary"] = summarize(extras, value)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(planes_p, planes_v, seconds=args.cpu_seconds)
+    if args.detail:
+        with open(args.detail, "w") as f:
+            json.dump({"line": line, "extras": extras}, f, indent=1)
     ctx.close()
     print(json.dumps(line), flush=True)
 
 
-def serving_config3(lg, wp, wv, planes_p, planes_v, device, n_req=100_000, rate=200_000.0,
-                    mean_batch=48, max_batch=512):
+def summarize(x, value):
+    """A few figures of the secondary measurements for the JSON line."""
+    r = lambda v, n=4: None if v is None else round(v, n)  # noqa: E731
+    out = {}
+    b1 = x.get("fp32_batch1", {})
+    if b1:
+        out["fp32_batch1_pairs_per_s"] = r(b1.get("small_batch_device_pairs_per_s"), 1)
+        out["fp32_batch1_host_api_pairs_per_s"] = r(b1.get("small_batch_host_api_pairs_per_s"), 1)
+        out["ratio_bf16_b256_vs_fp32_b1"] = r(value / b1["small_batch_device_pairs_per_s"], 1)
+    if "bf16_by_batch_positions_per_s" in x:
+        out["bf16_pairs_per_s_by_batch"] = {k: round(v) for k, v in x["bf16_by_batch_positions_per_s"].items()}
+    if "fp16_b256_pairs_per_s" in x:
+        out["fp16_b256_pairs_per_s"] = round(x["fp16_b256_pairs_per_s"])
+    c2 = x.get("config2_vs_fp64", {})
+    for prec, d in c2.items():
+        if isinstance(d, dict) and "top1" in d:
+            out[f"top1_vs_fp64_{prec}"] = r(d["top1"])
+    if "positions" in c2:
+        out["top1_positions"] = c2["positions"]
+    sv = x.get("serving_config3", {})
+    if "by_rate" in sv:
+        out["serving"] = {k: [round(v["throughput_positions_per_s"]), r(v["latency_p50_ms"], 2),
+                              r(v["latency_p99_ms"], 2)] for k, v in sv["by_rate"].items() if "latency_p50_ms" in v}
+    d4 = x.get("distill_config4", {}).get("teacher_T1", {})
+    if "student_only_leaf_evals_per_s" in d4:
+        out["distill"] = {"student_only_evals_per_s": round(d4["student_only_leaf_evals_per_s"]),
+                          "full_net_evals_per_s": round(d4["full_net_leaf_evals_per_s"]),
+                          "student_top1": r(d4["student_top1_agreement_with_full_net"]),
+                          "gate_2.5_fallback": r(d4["gate_spec"]["fallback_rate"]),
+                          "gate_2.5_speedup": r(d4["gate_spec"]["speedup_vs_full_net"])}
+    return out
+
+
+def serving_config3(lg, wp, wv, planes_p, planes_v, device, rates=(100_000.0, 200_000.0, 400_000.0, 800_000.0),
+                    n_req=100_000, mean_batch=48, max_batch=512):
     """Uneven batching as the search produces it: n_req single-position
-    requests with Poisson arrivals (rate per second, seed 2), grouped into
-    batches of Geometric(mean 48) sizes clipped to [1, 512] (seed 3).  Each
-    batch is submitted to both nets (lg_submit) at its last arrival; the
-    server merges what is queued, pads to a power-of-two bucket and replays
-    that bucket's CUDA graph.  Latency = completion of both nets - arrival."""
+    requests with Poisson arrivals (at each of `rates` per second, seed 2),
+    grouped into batches of Geometric(mean 48) sizes clipped to [1, 512]
+    (seed 3).  Each batch is submitted to both nets (lg_submit) at its last
+    arrival; the server merges what is queued, pads to a power-of-two bucket
+    and replays that bucket's CUDA graph.  Latency = completion of both nets
+    - arrival; throughput = requests / (last completion - first arrival).
+    The client sleeps until each due time (the interpreter's thread switch
+    interval is set to 20 us), so that the thread timing completions is not
+    held off by a busy-waiting submitter."""
+    import sys as _sys
     import tempfile
     import threading as th
-    arrivals = np.cumsum(np.random.default_rng(2).exponential(1.0 / rate, n_req))
+    old_switch = _sys.getswitchinterval()
+    _sys.setswitchinterval(2e-5)
     rng = np.random.default_rng(3)
     sizes, total = [], 0
     while total < n_req:
@@ -422,6 +469,7 @@ def serving_config3(lg, wp, wv, planes_p, planes_v, device, n_req=100_000, rate=
         sizes.append(b)
         total += b
     n_pos = planes_p.shape[0]
+    res = {}
     with lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"),
                     value=lg.NetDesc.config1_value(wv, "bf16"), device=device,
                     max_batch=max_batch) as ctx:
@@ -445,131 +493,176 @@ def serving_config3(lg, wp, wv, planes_p, planes_v, device, n_req=100_000, rate=
             batches.append((np.ascontiguousarray(planes_p[idx]), np.ascontiguousarray(planes_v[idx]),
                             np.empty((sz, 361), np.float32), np.empty(sz, np.float32), start, sz))
             start += sz
-        done = {}
-        stop = th.Event()
+        for rate in rates:
+            arrivals = np.cumsum(np.random.default_rng(2).exponential(1.0 / rate, n_req))
+            done = {}
+            stop = th.Event()
+            served0 = ctx.stats()["batches"]
 
-        def poller():
-            while not stop.is_set() or len(done) < 2 * len(batches):
-                for t in ctx.poll(512, timeout_us=2000):
-                    done[t] = time.perf_counter()
-                if stop.is_set() and len(done) >= 2 * len(batches):
-                    break
+            def poller():
+                while not stop.is_set() or len(done) < 2 * len(batches):
+                    for t in ctx.poll(512, timeout_us=2000):
+                        done[t] = time.perf_counter()
+                    if stop.is_set() and len(done) >= 2 * len(batches):
+                        break
 
-        pt = th.Thread(target=poller, daemon=True)
-        pt.start()
-        t0 = time.perf_counter() + 0.01
-        for k, (bp, bv, op, ov, st, sz) in enumerate(batches):
-            due = t0 + arrivals[st + sz - 1]
-            while time.perf_counter() < due:
-                pass
-            ctx.submit(lg.LG_NET_POLICY, bp, op, tag=2 * k + 1)
-            ctx.submit(lg.LG_NET_VALUE, bv, ov, tag=2 * k + 2)
-        stop.set()
-        pt.join(timeout=60)
-        served = ctx.stats()["batches"]
-    if len(done) < 2 * len(batches):
-        return {"error": f"only {len(done)} of {2 * len(batches)} submissions completed"}
-    lat = np.empty(n_req)
-    last = 0.0
-    for k, (_, _, _, _, st, sz) in enumerate(batches):
-        comp = max(done[2 * k + 1], done[2 * k + 2])
-        last = max(last, comp)
-        lat[st:st + sz] = comp - (t0 + arrivals[st:st + sz])
-    return {"requests": n_req, "arrival_rate_per_s": rate, "client_batches": len(sizes),
-            "server_batches": int(served), "mean_client_batch": float(np.mean(sizes)),
-            "throughput_positions_per_s": n_req / (last - (t0 + arrivals[0])),
-            "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
-            "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "note": "policy + value per request; BF16; CUDA graph per power-of-two bucket "
-                    "(host copies inside the graph); autotuned kernel choice per bucket"}
+            pt = th.Thread(target=poller, daemon=True)
+            pt.start()
+            t0 = time.perf_counter() + 0.01
+            for k, (bp, bv, op, ov, st, sz) in enumerate(batches):
+                due = t0 + arrivals[st + sz - 1]
+                wait = due - time.perf_counter()
+                if wait > 2e-4:
+                    time.sleep(wait - 1e-4)
+                while time.perf_counter() < due:
+                    pass
+                ctx.submit(lg.LG_NET_POLICY, bp, op, tag=2 * k + 1)
+                ctx.submit(lg.LG_NET_VALUE, bv, ov, tag=2 * k + 2)
+            stop.set()
+            pt.join(timeout=60)
+            served = ctx.stats()["batches"] - served0
+            if len(done) < 2 * len(batches):
+                res[f"{int(rate)}"] = {"error": f"only {len(done)} of {2 * len(batches)} submissions completed"}
+                continue
+            lat = np.empty(n_req)
+            last = 0.0
+            for k, (_, _, _, _, st, sz) in enumerate(batches):
+                comp = max(done[2 * k + 1], done[2 * k + 2])
+                last = max(last, comp)
+                lat[st:st + sz] = comp - (t0 + arrivals[st:st + sz])
+            res[f"{int(rate)}"] = {
+                "throughput_positions_per_s": n_req / (last - (t0 + arrivals[0])),
+                "latency_p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "latency_p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "server_batches": int(served), "client_batches": len(sizes)}
+    _sys.setswitchinterval(old_switch)
+    return {"requests_per_rate": n_req, "mean_client_batch": float(np.mean(sizes)), "by_rate": res,
+            "note": "policy + value per request; BF16; CUDA graph per power-of-two bucket (host copies inside "
+                    "the graph); autotuned kernel choice per bucket"}
 
 
-def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp):
-    """FP32 batch-1 throughput, BF16 at the other batch sizes, and top-1
-    agreement with the FP64 oracle."""
+def config2_vs_fp64(lg, wp, wv, device, sp, subset=512):
+    """Precision variants against the FP64 oracle over the 65,536 positions of
+    the precision configuration: top-1 agreement against the oracle's FP64
+    answers (tests/golden/config2_f64.npz, make_config2.py), value errors
+    against its FP64 values, probability errors on `subset` positions
+    computed live by the oracle, and the share of top-1 flips whose FP64
+    top-1/top-2 gap is below twice the largest logit error seen on the
+    subset."""
+    import hashlib
+
     import torch
+    from oracle import oracle as O
+    d = np.load(os.path.join(ROOT, "tests", "golden", "config2_f64.npz"))
+    n = int(d["n"])
+    sq, tm, _ = O.config_boards(n, int(d["seed"]))
+    if hashlib.sha256(sq.tobytes()).hexdigest()[:16] != str(d["squares_sha256"]):
+        return {"error": "position generator does not reproduce the fixture"}
+    dev = torch.device("cuda", device)
+    d_sq, d_tm = torch.from_numpy(sq).to(dev), torch.from_numpy(tm).to(dev)
+    planes = {}
+    for which, key in ((0, "p"), (1, "v")):
+        t = torch.empty((n, 24, 361), dtype=torch.uint8, device=dev)
+        lg.gather_device(d_sq.data_ptr(), d_tm.data_ptr(), n, which, 24, t.data_ptr(), sp)
+        planes[key] = t
+    torch.cuda.synchronize()
+    sub = np.arange(0, n, n // subset)
+    P, V = O.make_net(O.CFG_POLICY), O.make_net(O.CFG_VALUE)
+    O.enable_blas()
+    l64 = O.forward_f64(P, wp, planes["p"][sub].cpu().numpy())
+    O.disable_blas()
+    p64 = O.softmax_f64(l64, 1.0)
+    out = {"positions": n, "prob_error_subset": int(sub.size)}
+    for prec in ("bf16", "fp16", "fp8w"):
+        logits = torch.empty((n, 361), device=dev)
+        probs = torch.empty((n, 361), device=dev)
+        val = torch.empty(n, device=dev)
+        with lg.Context(policy=lg.NetDesc.config1_policy(wp, prec), value=lg.NetDesc.config1_value(wv, prec),
+                        device=device, max_batch=256) as c:
+            c.policy_device(planes["p"].data_ptr(), n, probs.data_ptr(), 1.0, logits.data_ptr(), sp)
+            c.value_device(planes["v"].data_ptr(), n, val.data_ptr(), sp)
+            torch.cuda.synchronize()
+        agree = logits.argmax(1).cpu().numpy() == d["top1"]
+        verr = np.abs(val.cpu().numpy() - d["value"])
+        emax = float(np.abs(logits[sub].cpu().numpy() - l64).max())
+        perr = np.abs(probs[sub].cpu().numpy() - p64)
+        gaps = d["gap"][~agree]
+        out[prec] = {"top1": float(agree.mean()), "flips": int((~agree).sum()),
+                     "flips_within_2x_logit_error": float((gaps < 2 * emax).mean()) if gaps.size else 1.0,
+                     "logit_max_abs_err_subset": emax,
+                     "prob_max_abs_err": float(perr.max()), "prob_mean_abs_err": float(perr.mean()),
+                     "value_max_abs_err": float(verr.max()), "value_mean_abs_err": float(verr.mean())}
+    ncap = d["top1_w_bf16"].size
+    out["weight_rounding_only_top1"] = {"bf16": float((d["top1_w_bf16"] == d["top1"][:ncap]).mean()),
+                                        "fp16": float((d["top1_w_fp16"] == d["top1"][:ncap]).mean()),
+                                        "positions": int(ncap)}
+    return out
+
+
+def pair_rate_device(lg, wp, wv, prec, B, d_p, d_v, dev, sp, choice=None, reps=None, autotune=True):
+    """Policy + value pairs per second, device-resident inputs, batch B."""
+    import tempfile
+
+    import torch
+    with lg.Context(policy=lg.NetDesc.config1_policy(wp, prec),
+                    value=lg.NetDesc.config1_value(wv, prec), device=dev.index, max_batch=B) as cb:
+        if choice is not None:
+            cb.set_tuning(B, *choice)
+        elif autotune:
+            cb.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{prec}_{B}.json"))
+        probs = torch.empty((B, 361), device=dev)
+        val = torch.empty(B, device=dev)
+        reps = reps or max(4, min(200, 4096 // B))
+        for i in range(3):
+            cb.policy_device(d_p.data_ptr(), B, probs.data_ptr(), 1.0, None, sp)
+            cb.value_device(d_v.data_ptr(), B, val.data_ptr(), sp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(reps):
+            off = (i * B) % (8192 - B + 1)
+            cb.policy_device(d_p[off].data_ptr(), B, probs.data_ptr(), 1.0, None, sp)
+            cb.value_device(d_v[off].data_ptr(), B, val.data_ptr(), sp)
+        e1.record()
+        torch.cuda.synchronize()
+        return B * reps / (e0.elapsed_time(e1) / 1e3), cb.tuning(B)
+
+
+def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp, quick=False):
+    """FP32 batch 1 (the ratio's denominator), BF16 at the other batch sizes,
+    FP16 at batch 256, the precision variants against FP64 over 65,536
+    positions, serving and distillation."""
     out = {}
-    # FP32 plain path at batch 1 (policy + value per position).
+    # FP32 plain path at batch 1 (policy + value per position): the
+    # small-batch kernel (the default at batch 1) and the per-layer kernels
+    r_lat, _ = pair_rate_device(lg, wp, wv, "fp32", 1, d_p, d_v, dev, sp, choice=(4, 0), reps=400)
+    r_gen, _ = pair_rate_device(lg, wp, wv, "fp32", 1, d_p, d_v, dev, sp, choice=(0, 0), reps=200)
     with lg.Context(policy=lg.NetDesc.config1_policy(wp, "fp32"),
-                    value=lg.NetDesc.config1_value(wv, "fp32"), device=dev.index,
-                    max_batch=1) as c32:
-        n = 200
+                    value=lg.NetDesc.config1_value(wv, "fp32"), device=dev.index, max_batch=1) as c32:
         for i in range(5):
             c32.policy(planes_p[i:i + 1])
             c32.value(planes_v[i:i + 1])
+        n = 300
         t0 = time.perf_counter()
         for i in range(n):
             c32.policy(planes_p[i:i + 1])
             c32.value(planes_v[i:i + 1])
         host_rate = n / (time.perf_counter() - t0)
-        probs = torch.empty((1, 361), device=dev)
-        val = torch.empty(1, device=dev)
-        for i in range(5):
-            c32.policy_device(d_p[i].data_ptr(), 1, probs.data_ptr(), 1.0, None, sp)
-            c32.value_device(d_v[i].data_ptr(), 1, val.data_ptr(), sp)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for i in range(n):
-            c32.policy_device(d_p[i].data_ptr(), 1, probs.data_ptr(), 1.0, None, sp)
-            c32.value_device(d_v[i].data_ptr(), 1, val.data_ptr(), sp)
-        e1.record()
-        torch.cuda.synchronize()
-        dev_rate = n / (e0.elapsed_time(e1) / 1e3)
-    out["fp32_plain_batch1"] = {"host_api_positions_per_s": host_rate,
-                                "device_positions_per_s": dev_rate}
-    # BF16 at the other configured batch sizes (device-resident inputs),
-    # autotuned as a user's context would be.
-    import tempfile
-    by_batch = {}
+    out["fp32_batch1"] = {"small_batch_device_pairs_per_s": r_lat, "per_layer_device_pairs_per_s": r_gen,
+                          "small_batch_host_api_pairs_per_s": host_rate,
+                          "note": "policy + value per position, batch 1; device = inputs resident, CUDA "
+                                  "events; host API = lg_policy + lg_value blocking calls"}
+    by_batch, choices = {}, {}
     for b in (1, 8, 64, 256):
-        with lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"),
-                        value=lg.NetDesc.config1_value(wv, "bf16"), device=dev.index,
-                        max_batch=b) as cb:
-            cb.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{b}.json"))
-            probs = torch.empty((b, 361), device=dev)
-            val = torch.empty(b, device=dev)
-            reps = max(4, min(200, 4096 // b))
-            for i in range(3):
-                cb.policy_device(d_p.data_ptr(), b, probs.data_ptr(), 1.0, None, sp)
-                cb.value_device(d_v.data_ptr(), b, val.data_ptr(), sp)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for i in range(reps):
-                off = (i * b) % (8192 - b + 1)
-                cb.policy_device(d_p[off].data_ptr(), b, probs.data_ptr(), 1.0, None, sp)
-                cb.value_device(d_v[off].data_ptr(), b, val.data_ptr(), sp)
-            e1.record()
-            torch.cuda.synchronize()
-            by_batch[str(b)] = b * reps / (e0.elapsed_time(e1) / 1e3)
+        by_batch[str(b)], choices[str(b)] = pair_rate_device(lg, wp, wv, "bf16", b, d_p, d_v, dev, sp)
     out["bf16_by_batch_positions_per_s"] = by_batch
-    out["ratio_bf16_batched_vs_fp32_batch1"] = by_batch["256"] / dev_rate
-    # Top-1 agreement with the FP64 oracle (BF16 and FP8 weights), 256 positions.
-    from oracle import oracle as O
-    P, V = O.make_net(O.CFG_POLICY), O.make_net(O.CFG_VALUE)
-    idx = np.arange(0, 8192, 32)
-    O.enable_blas()
-    l64 = O.forward_f64(P, wp, planes_p[idx])
-    v64 = O.forward_f64(V, wv, planes_v[idx])
-    O.disable_blas()
-    p64 = O.softmax_f64(l64, 1.0)
-    agree = {}
-    for prec in ("bf16", "fp8w"):
-        with lg.Context(policy=lg.NetDesc.config1_policy(wp, prec),
-                        value=lg.NetDesc.config1_value(wv, prec), device=dev.index,
-                        max_batch=256) as cq:
-            pr, lo = cq.policy(planes_p[idx], 1.0, return_logits=True)
-            vq = cq.value(planes_v[idx])
-        agree[prec] = {"top1": float((lo.argmax(1) == l64.argmax(1)).mean()),
-                       "prob_max_abs_err": float(np.abs(pr - p64).max()),
-                       "prob_mean_abs_err": float(np.abs(pr - p64).mean()),
-                       "value_max_abs_err": float(np.abs(vq - v64).max()),
-                       "value_mean_abs_err": float(np.abs(vq - v64).mean()),
-                       "positions": int(idx.size)}
-    out["vs_fp64_oracle"] = agree
-    out["serving_config3"] = serving_config3(lg, wp, wv, planes_p, planes_v, dev.index)
-    out["distill_config4"] = distill_config4(wp, wv, planes_p, planes_v, dev.index)
+    out["bf16_kernel_choice_by_batch"] = choices
+    out["fp16_b256_pairs_per_s"], _ = pair_rate_device(lg, wp, wv, "fp16", 256, d_p, d_v, dev, sp)
+    out["ratio_bf16_batched_vs_fp32_batch1"] = by_batch["256"] / r_lat
+    out["config2_vs_fp64"] = config2_vs_fp64(lg, wp, wv, dev.index, sp)
+    if not quick:
+        out["serving_config3"] = serving_config3(lg, wp, wv, planes_p, planes_v, dev.index)
+        out["distill_config4"] = distill_config4(wp, wv, planes_p, planes_v, dev.index)
     return out
 
 
@@ -607,7 +700,7 @@ def gather_throughput(lg, squares, to_move, dev, sp, reps=20):
     ms = timed(24)
     ms32 = timed(32)
     per_launch = B * (362 + 24 * 361)
-    _, hbm, _ = read_peaks()
+    _, _, hbm, _ = read_peaks()
     gbs = 2 * per_launch / (ms / 1e3) / 1e9
     return {"boards_per_s_both_sets": B / (ms / 1e3), "us_per_launch": ms * 1e3 / 2,
             "boards_per_launch": B, "algorithmic_bytes_per_launch": per_launch,
@@ -654,6 +747,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--profile-run", action="store_true",
                     help="only the device-resident warm-up and timed steps (for ncu)")
+    ap.add_argument("--quick", action="store_true",
+                    help="skip the serving replay and the distillation experiment")
+    ap.add_argument("--detail", default=None, help="write every secondary measurement to this JSON file")
     ap.add_argument("--gather-run", action="store_true",
                     help="only the gather timing: 8192 boards, 24 and 32 planes, both sets (for ncu)")
     args = ap.parse_args()
