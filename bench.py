@@ -435,13 +435,14 @@ def summarize(x, value):
     if "by_rate" in sv:
         out["serving"] = {k: [round(v["throughput_positions_per_s"]), r(v["latency_p50_ms"], 2),
                               r(v["latency_p99_ms"], 2)] for k, v in sv["by_rate"].items() if "latency_p50_ms" in v}
-    d4 = x.get("distill_config4", {}).get("teacher_T1", {})
-    if "student_only_leaf_evals_per_s" in d4:
-        out["distill"] = {"student_only_evals_per_s": round(d4["student_only_leaf_evals_per_s"]),
-                          "full_net_evals_per_s": round(d4["full_net_leaf_evals_per_s"]),
-                          "student_top1": r(d4["student_top1_agreement_with_full_net"]),
-                          "gate_2.5_fallback": r(d4["gate_spec"]["fallback_rate"]),
-                          "gate_2.5_speedup": r(d4["gate_spec"]["speedup_vs_full_net"])}
+    d4 = x.get("distill", {})
+    if "student_only_evals_per_s" in d4:
+        out["distill"] = {"student_only_evals_per_s": round(d4["student_only_evals_per_s"]),
+                          "full_pair_evals_per_s": round(d4["full_pair_evals_per_s"]),
+                          "student_only_speedup": r(d4["student_only_speedup"], 2),
+                          "gated_speedup_at_fallback": {k[9:]: r(d4[k]["speedup"], 2)
+                                                        for k in ("fallback_0", "fallback_10pct", "fallback_100")
+                                                        if k in d4}}
     return out
 
 
@@ -662,7 +663,7 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
     out["config2_vs_fp64"] = config2_vs_fp64(lg, wp, wv, dev.index, sp)
     if not quick:
         out["serving_config3"] = serving_config3(lg, wp, wv, planes_p, planes_v, dev.index)
-        out["distill_config4"] = distill_config4(wp, wv, planes_p, planes_v, dev.index)
+        out["distill"] = distill_rates(wp, wv, planes_p, planes_v, dev.index)
     return out
 
 
@@ -720,21 +721,174 @@ def gather_run(reps):
     print(json.dumps({"gather_run": True, **res}), flush=True)
 
 
-def distill_config4(wp, wv, planes_p, planes_v, device):
-    """The distilled student (64-wide net, entropy-gated fallback to the full
-    net) on the fixture positions: the student is trained on
-    positions 0..895 (x8 symmetries), evaluated on 896..1023; labels are the
-    full FP32 policy net's softmax and 2*mc_owner(64)-1.  Run at the
-    specified teacher temperature 1 and, as an ablation, at 0.05 (the
-    He-normal teacher's policies are nearly flat at temperature 1)."""
+def latency_run(B, reps):
+    """The small-batch kernel alone at batch B: `reps` policy + value calls
+    of the FP32 and the BF16 benchmark nets, inputs resident, one JSON line
+    of device microseconds per net call."""
+    import torch
+
+    import leela_gb300 as lg
+    from leela_gb300 import build as Bld
+    Bld.build()
+    dev = torch.device("cuda", 0)
+    planes_p, planes_v = load_positions()
+    _, _, wp, wv = make_weights()
+    d_p = torch.from_numpy(planes_p[:64]).to(dev)
+    d_v = torch.from_numpy(planes_v[:64]).to(dev)
+    sp = torch.cuda.current_stream(dev).cuda_stream
+    out = {"latency_run": True, "batch": B}
+    for prec in ("fp32", "bf16"):
+        with lg.Context(policy=lg.NetDesc.config1_policy(wp, prec), value=lg.NetDesc.config1_value(wv, prec),
+                        max_batch=max(B, 1)) as c:
+            c.set_tuning(B, 4, 0)
+            probs = torch.empty((B, 361), device=dev)
+            val = torch.empty(B, device=dev)
+            for _ in range(3):
+                c.policy_device(d_p.data_ptr(), B, probs.data_ptr(), 1.0, None, sp)
+                c.value_device(d_v.data_ptr(), B, val.data_ptr(), sp)
+            torch.cuda.synchronize()
+            c.profile(True)
+            for i in range(reps):
+                c.policy_device(d_p[i % 32].data_ptr(), B, probs.data_ptr(), 1.0, None, sp)
+                c.value_device(d_v[i % 32].data_ptr(), B, val.data_ptr(), sp)
+            torch.cuda.synchronize()
+            n, ms = c.profile_read(lg.PROF_LAT)
+            c.profile(False)
+            out[prec] = {"launches": n, "us_per_launch": ms * 1e3 / max(n, 1)}
+    print(json.dumps(out), flush=True)
+
+
+def student_run(reps):
+    """The fused student kernel (and its finish kernels) alone on the 8192
+    benchmark inputs: `reps` calls, one JSON line of evaluations per second."""
+    import torch
+
+    from leela_gb300 import build as Bld
     from leela_gb300 import distill
-    mc = np.load(os.path.join(ROOT, "tests", "golden", "mcowner_s0.npz"))["mcowner"]
-    pos_index = np.arange(planes_p.shape[0]) % 1024
-    res = {}
-    for name, temp in (("teacher_T1", 1.0), ("teacher_T0.05", 0.05)):
-        res[name] = distill.run_config4(planes_p, planes_v, pos_index, mc, wp, wv, device,
-                                        teacher_temperature=temp, time_budget_s=25.0)
-    return res
+    Bld.build()
+    dev = torch.device("cuda", 0)
+    planes_p, _ = load_positions()
+    N = planes_p.shape[0]
+    d_p = torch.from_numpy(planes_p).to(dev)
+    st = distill.Student(max_batch=8)
+    st.init_he(0)
+    params = st.get_params()
+    st.close()
+    s = torch.cuda.current_stream(dev).cuda_stream
+    with distill.FastNet(params, max_batch=N) as fast:
+        probs = torch.empty((N, 361), device=dev)
+        val = torch.empty(N, device=dev)
+        for _ in range(3):
+            fast.device(d_p.data_ptr(), N, probs.data_ptr(), val.data_ptr(), 1.0, None, None, s)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fast.device(d_p.data_ptr(), N, probs.data_ptr(), val.data_ptr(), 1.0, None, None, s)
+        e1.record()
+        fast.status(s)
+        ms = e0.elapsed_time(e1) / max(reps, 1)
+    print(json.dumps({"student_run": True, "positions": N, "ms_per_call": ms, "evals_per_s": N / (ms / 1e3)}),
+          flush=True)
+
+
+def distill_rates(wp, wv, planes_p, planes_v, device, N=8192):
+    """Leaf evaluations per second of the learned fast path's pieces on the
+    8192 benchmark inputs (resident on the GPU): the full BF16 pair as the
+    headline serves it (autotuned, batches of 256), the student alone (fused
+    kernel, one call of 8192), and the gated path at fallback rates of 0%,
+    ~10% and 100% (thresholds at entropy percentiles of this student).  The
+    speed does not depend on what the student learned -- the fallback rate
+    does (the trained students: bench.py --distill-run)."""
+    import tempfile
+
+    import torch
+
+    import leela_gb300 as lg
+    from leela_gb300 import distill
+    dev = torch.device("cuda", device)
+    s = torch.cuda.current_stream(dev).cuda_stream
+    d_p = torch.from_numpy(planes_p[:N]).to(dev)
+    d_v = torch.from_numpy(planes_v[:N]).to(dev)
+    st = distill.Student(max_batch=8, device=device)
+    st.init_he(0)
+    params = st.get_params()
+    st.close()
+
+    def timed(fn, reps=5):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return N / (e0.elapsed_time(e1) / reps / 1e3)
+
+    out = {}
+    with lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"), value=lg.NetDesc.config1_value(wv, "bf16"),
+                    device=device, max_batch=BATCH) as cf, distill.FastNet(params, max_batch=N, device=device) as fast:
+        cf.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{BATCH}.json"))
+        fp = torch.empty((N, 361), device=dev)
+        fv = torch.empty(N, device=dev)
+        se = torch.empty(N, device=dev)
+
+        def full():
+            cf.policy_device(d_p.data_ptr(), N, fp.data_ptr(), 1.0, None, s)
+            cf.value_device(d_v.data_ptr(), N, fv.data_ptr(), s)
+
+        def student():
+            fast.device(d_p.data_ptr(), N, fp.data_ptr(), fv.data_ptr(), 1.0, None, se.data_ptr(), s)
+
+        out["full_pair_evals_per_s"] = timed(full)
+        out["student_only_evals_per_s"] = timed(student)
+        fast.status(s)
+        ent = se.cpu().numpy()
+        out["student_only_speedup"] = out["student_only_evals_per_s"] / out["full_pair_evals_per_s"]
+        for name, thr in (("fallback_0", 1e9), ("fallback_10pct", float(np.percentile(ent, 90))),
+                          ("fallback_100", -1.0)):
+            g = distill.GatedEvaluator(fast, cf, thr)
+            buf = [None]
+
+            def gated():
+                buf[0] = g.evaluate(d_p, d_v, s, buf[0])
+
+            rate = timed(gated)
+            out[name] = {"fallback_rate": int(buf[0][3].item()) / N, "evals_per_s": rate,
+                         "speedup": rate / out["full_pair_evals_per_s"]}
+        fast.status(s)
+    return out
+
+
+def distill_run():
+    """The learned fast path at its configuration's scale (one JSON line):
+    1,048,576 positions from the seeded generator, value labels from the
+    reference's own Playout::mc_owner(64) (tests/golden/config4_mcowner.npz,
+    made by tests/golden/make_config4.py), policy labels from the full FP32
+    net, the student trained by this library's kernels, judged on 65,536
+    held-out positions by the full BF16 nets (leela_gb300.distill.run_config4)."""
+    import hashlib
+
+    import torch
+
+    from leela_gb300 import build as B
+    from leela_gb300 import distill
+    from oracle import oracle as O
+    B.build()
+    d = np.load(os.path.join(ROOT, "tests", "golden", "config4_mcowner.npz"))
+    n, seed = int(d["n"]), int(d["seed"])
+    t0 = time.perf_counter()
+    sq, tm, _ = O.config_boards(n, seed)
+    gen_s = time.perf_counter() - t0
+    if hashlib.sha256(sq.tobytes()).hexdigest()[:16] != str(d["squares_sha256"]):
+        print(json.dumps({"distill_run": True, "error": "the position generator does not reproduce the labels' boards"}))
+        return
+    _, _, wp, wv = make_weights()
+    res = distill.run_config4(sq, tm, d["winrate_x128"].astype(np.float32) / 128.0, wp, wv, 0)
+    res["board_generation_seconds"] = gen_s
+    print(json.dumps({"distill_run": True, **res}), flush=True)
 
 
 def main():
@@ -752,10 +906,25 @@ def main():
     ap.add_argument("--detail", default=None, help="write every secondary measurement to this JSON file")
     ap.add_argument("--gather-run", action="store_true",
                     help="only the gather timing: 8192 boards, 24 and 32 planes, both sets (for ncu)")
+    ap.add_argument("--latency-run", type=int, default=0, metavar="B",
+                    help="only the small-batch kernel at batch B, --steps calls per net and precision (for ncu)")
+    ap.add_argument("--student-run", action="store_true",
+                    help="only the fused student kernel on the 8192 benchmark inputs, --steps calls (for ncu)")
+    ap.add_argument("--distill-run", action="store_true",
+                    help="the learned fast path at its configuration's scale (1M positions; minutes)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.gather_run:
         gather_run(reps=5)
+        return
+    if args.latency_run:
+        latency_run(args.latency_run, reps=args.steps)
+        return
+    if args.student_run:
+        student_run(reps=args.steps)
+        return
+    if args.distill_run:
+        distill_run()
         return
     world, rank, local = dist_setup()
     if args.impl == "reference":

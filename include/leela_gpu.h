@@ -287,6 +287,42 @@ LG_API int lg_student_grads(lg_student *st, const uint8_t *planes, int B, const 
 LG_API int lg_student_forward(lg_student *st, const uint8_t *planes, int B, float *probs, float *value,
                               void *stream);
 
+/* The distilled student served for evaluation: BF16, one fused kernel for
+ * the whole trunk (5x5 c_in -> 64, n3x3 x 3x3 64 -> 64, ReLU) and both 1x1
+ * heads of two boards at a time, activations kept in shared memory; then the
+ * softmax (with the policy's entropy) and the value FC.  Weights in the
+ * lg_student flat layout with width 64 (lg_fast_param_count floats); c_in a
+ * multiple of 4 up to 24.  No reference counterpart: the engine evaluates
+ * every leaf with the full nets (UCTNode.cpp:74-121, Network.cpp:590-674).
+ *
+ * lg_fast_device is asynchronous on `stream` (device pointers; logits and
+ * entropy may be NULL); lg_fast_status waits for the stream and reports a
+ * kernel's error word (LG_ERR_DEVICE) if one gave up a bounded wait. */
+typedef struct lg_fast lg_fast;
+LG_API size_t lg_fast_param_count(int c_in, int n3x3, int fc_hidden);
+LG_API int lg_fast_create(int device, int c_in, int n3x3, int fc_hidden, int max_batch, const float *weights,
+                          lg_fast **out);
+LG_API int lg_fast_set_weights(lg_fast *f, const float *weights);
+LG_API void lg_fast_destroy(lg_fast *f);
+LG_API int lg_fast_device(lg_fast *f, const uint8_t *planes, int B, float temperature, float *probs,
+                          float *logits, float *value, float *entropy, void *stream);
+LG_API int lg_fast_status(lg_fast *f, void *stream);
+
+/* The learned fast path for a batch of leaves: the student answers all B
+ * positions; those whose policy entropy exceeds `threshold` nats are
+ * compacted on the device, run through the full context's policy and value
+ * nets (tensor-core nets on the persistent trunk kernel, batch size read on
+ * the device) and written over the student's answers -- no host
+ * synchronisation anywhere.  planes_p / planes_v: the positions' planes for
+ * the full policy / value net ([B][c_in][361] each; the student reads
+ * planes_p).  fallback (optional, [B] bytes): 1 where the full nets
+ * answered; count (optional, one int): how many.  B <= the student's
+ * max_batch.  Asynchronous on `stream`.  No reference counterpart (see
+ * lg_fast). */
+LG_API int lg_gated_device(lg_fast *student, lg_ctx *full, const uint8_t *planes_p, const uint8_t *planes_v,
+                           int B, float temperature, float threshold, float *probs, float *value,
+                           uint8_t *fallback, int32_t *count, void *stream);
+
 /* Per-kernel timing for the roofline report.  lg_profile(ctx, 1) clears the
  * counters and brackets every kernel launched by later device-pointer calls
  * (lg_policy_device / lg_value_device) with CUDA events on the launching

@@ -237,11 +237,17 @@ __device__ __forceinline__ float head_value(const HeadIn &h, int b, int p) {
 }
 
 // Network.cpp:450-469 per board: alpha = max/T; p = exp(x/T - alpha)/sum.
+// Boards a launch processes: B, or with a device-side count the first
+// *count - count_base of them.
+__device__ __forceinline__ int head_boards(const HeadIn &h, int B) {
+    return h.count ? min(B, max(0, *h.count - h.count_base)) : B;
+}
+
 __global__ void __launch_bounds__(384) softmax_kernel(const HeadIn h, int B, float temperature,
-                                                      float *__restrict__ probs) {
+                                                      float *__restrict__ probs, float *__restrict__ entropy) {
     __shared__ float red[32];
     int b = blockIdx.x;
-    if (b >= B) return;
+    if (b >= head_boards(h, B)) return;
     int p = threadIdx.x;
     float x = (p < kPoints) ? head_value(h, b, p) : -FLT_MAX;
     if (h.logits_out && p < kPoints) h.logits_out[(size_t)b * kPoints + p] = x;
@@ -250,6 +256,12 @@ __global__ void __launch_bounds__(384) softmax_kernel(const HeadIn h, int B, flo
     float e = (p < kPoints) ? expf((x / temperature) - alpha) : 0.0f;
     float den = block_reduce<384>(e, false, red);
     if (p < kPoints) probs[(size_t)b * kPoints + p] = e / den;
+    if (entropy) {
+        // -sum p ln p = ln(den) - sum e z / den, z = x/T - alpha = ln e
+        const float ez = (p < kPoints) ? e * ((x / temperature) - alpha) : 0.0f;
+        const float s = block_reduce<384>(ez, false, red);
+        if (p == 0) entropy[b] = logf(den) - s / den;
+    }
 }
 
 // innerproduct<361,H> (+act) then innerproduct<H,1>, then tanh, (1+tanh)/2
@@ -276,6 +288,8 @@ __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
     __shared__ __align__(16) float Ws[kFcK][kFcUnits];
     const int tid = threadIdx.x;
     const int b0 = blockIdx.x * kFcBoards, slice = blockIdx.y, ks = blockIdx.z;
+    const int Bc = head_boards(h, B);
+    if (b0 >= Bc) return;
     const int k0 = ks * kFcK, nk = min(kPoints, k0 + kFcK) - k0;
     // W1 slice rows k0 .. k0+nk-1: contiguous, float4 loads
     const float4 *wsrc = reinterpret_cast<const float4 *>(w1s + ((size_t)slice * kPoints + k0) * kFcUnits);
@@ -299,7 +313,7 @@ __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
     for (int j = 0; j < kPer; ++j) {
         const int i = tid + 256 * j;
         const int bi = i / nk, kk = i - bi * nk, b = b0 + bi;
-        xv[j] = (i < kFcBoards * nk && b < B) ? head_value(h, b, k0 + kk) : 0.0f;
+        xv[j] = (i < kFcBoards * nk && b < Bc) ? head_value(h, b, k0 + kk) : 0.0f;
     }
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
@@ -307,7 +321,7 @@ __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
         if (i < kFcBoards * nk) {
             const int bi = i / nk, kk = i - bi * nk, b = b0 + bi;
             Xs[kk][bi] = xv[j];
-            if (h.logits_out && slice == 0 && b < B) h.logits_out[(size_t)b * kPoints + k0 + kk] = xv[j];
+            if (h.logits_out && slice == 0 && b < Bc) h.logits_out[(size_t)b * kPoints + k0 + kk] = xv[j];
         }
     }
     __syncthreads();
@@ -329,7 +343,7 @@ __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int b = b0 + 4 * bq + j;
-        if (b < B)
+        if (b < Bc)
             *reinterpret_cast<float2 *>(pre + ((size_t)ks * B + b) * Hp + u) = make_float2(acc[j][0], acc[j][1]);
     }
 }
@@ -337,10 +351,11 @@ __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
 __global__ void __launch_bounds__(256) value_final_kernel(const float *__restrict__ pre, int B, int H, int Hp,
                                                           const float *__restrict__ b1,
                                                           const float *__restrict__ w2, float b2, int act,
-                                                          int value_map, float *__restrict__ value) {
+                                                          int value_map, float *__restrict__ value,
+                                                          const int *__restrict__ count, int count_base) {
     __shared__ float red[32];
     const int b = blockIdx.x;
-    if (b >= B) return;
+    if (b >= B || (count && b >= *count - count_base)) return;
     float s = 0.0f;
     for (int u = threadIdx.x; u < H; u += 256) {
         float z = b1[u];
@@ -411,8 +426,8 @@ void launch_head_conv_f32(const float *in, const float *wh, float bias, int B, i
     head_conv_f32<<<blocks, 256, 0, s>>>(in, wh, bias, B, C, k, do_act, act, logits);
 }
 
-void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s) {
-    softmax_kernel<<<B, 384, 0, s>>>(h, B, temperature, probs);
+void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s, float *entropy) {
+    softmax_kernel<<<B, 384, 0, s>>>(h, B, temperature, probs, entropy);
 }
 
 void launch_value_fc(const HeadIn &h, int B, const float *w1s, const float *b1, const float *w2,
@@ -421,7 +436,8 @@ void launch_value_fc(const HeadIn &h, int B, const float *w1s, const float *b1, 
     const int slices = (H + kFcUnits - 1) / kFcUnits;
     dim3 grid((B + kFcBoards - 1) / kFcBoards, slices, kFcSplit);
     value_fc1_kernel<<<grid, 256, 0, s>>>(h, B, w1s, slices * kFcUnits, part);
-    value_final_kernel<<<B, 256, 0, s>>>(part, B, H, slices * kFcUnits, b1, w2, b2, act, value_map, value);
+    value_final_kernel<<<B, 256, 0, s>>>(part, B, H, slices * kFcUnits, b1, w2, b2, act, value_map, value,
+                                         h.count, h.count_base);
 }
 
 size_t value_fc_part_floats(int B, int H) {

@@ -657,27 +657,41 @@ int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float
 
 // l5_ready: the first layer's expanded input rows are already in c->l5 (the
 // board path's gather writes them), so `planes` is not read.
+// count (device, optional): only the first *count - count_base of the B
+// positions are computed -- a batch whose size is known only on the device
+// (the gated path); it runs on the persistent trunk with the first layer
+// inside it, which a net must support (trunk_fusable).
+bool trunk_fusable(const Net &n) {
+    return n.trunk_w != nullptr && n.tc.size() >= 2 && n.tc[0].k == 5 && n.tc[0].halves == 2 &&
+           n.tc[0].cout == 128;
+}
+
 int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
                float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof,
-               bool l5_ready = false) {
-    if (use_lat(c, n, B) && !l5_ready) return forward_lat(c, n, planes, B, T, probs, logits_out, value, s, nlaunch, prof);
+               bool l5_ready = false, const int *count = nullptr, int count_base = 0) {
+    if (!count && use_lat(c, n, B) && !l5_ready)
+        return forward_lat(c, n, planes, B, T, probs, logits_out, value, s, nlaunch, prof);
+    if (count && !trunk_fusable(n)) {
+        lg_set_error("a device-side batch size needs a 128-wide tensor-core net with a 5x5 first layer");
+        return LG_ERR_ARG;
+    }
     const lg_net_desc &d = n.d;
     const int f16 = d.precision == LG_FP16 ? 1 : 0;
     int L = 0;
     const TcConv &first = n.tc[0];
     if (!l5_ready) {
         ProfScope ps(c, prof, LG_PROF_PACK, s);
-        launch_pack_planes_l5(planes, B, d.c_in, first.halves, f16 != 0, c->l5, s);
+        launch_pack_planes_l5(planes, B, d.c_in, first.halves, f16 != 0, c->l5, s, count, count_base);
         ++L;
     }
     float *lg = logits_out ? logits_out : c->d_logits;
     const size_t part_stride = (size_t)B * kPoints;
     int bl = 0;
     while ((1 << bl) < B && bl < 16) ++bl;
-    const int var3 = c->tc_variant[bl][0], var1 = c->tc_variant[bl][1];
+    const int var3 = count ? 3 : c->tc_variant[bl][0], var1 = c->tc_variant[bl][1];
     const bool use_trunk = (var3 == 2 || var3 == 3) && n.trunk_w != nullptr;
     // choice 3: the 5x5 first layer runs inside the trunk launch too
-    const bool fuse_first = use_trunk && var3 == 3 && first.k == 5 && first.halves == 2 && first.cout == 128;
+    const bool fuse_first = use_trunk && var3 == 3 && trunk_fusable(n);
     int cur = 0;
     for (size_t l = fuse_first ? 1 : 0; l < n.tc.size(); ++l) {
         const TcConv &t = n.tc[l];
@@ -703,6 +717,8 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
             tt.rows = B * kL3Board;
             tt.nl = (int)n.tc.size() - 1;
             tt.f16 = f16;
+            tt.count = count;
+            tt.count_base = count_base;
             if (c->stall_kind == 0) {
                 // the first item of the second 3x3 layer
                 tt.stall_item = (fuse_first ? (tt.rows5 + 255) / 256 : 0) + (tt.rows + 255) / 256;
@@ -745,7 +761,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
     {
         ProfScope ps(c, prof, LG_PROF_TAIL, s);
         HeadIn h{c->d_parts, tc_head_parts(d.width, use_trunk ? 0 : var3), part_stride, n.head_b, d.act_head,
-                 d.act, lg};
+                 d.act, lg, count, count_base};
         if (!d.value_head)
             launch_softmax(h, B, T, probs, s);
         else
@@ -1363,6 +1379,73 @@ extern "C" int lg_value_device(lg_ctx *c, const uint8_t *planes, int B, float *v
     std::lock_guard<std::mutex> g(c->mu);
     return run_device(c, LG_NET_VALUE, planes, B, 1.0f, nullptr, nullptr, value,
                       (cudaStream_t)stream);
+}
+
+// The learned fast path over B positions, all on `stream`: the student
+// (fused kernel, softmax with entropy, value FC) answers every position; the
+// gate compacts the indices of those above the entropy threshold; their
+// planes are gathered and run through the full nets in chunks of max_batch
+// whose sizes the kernels read from the device-side count; the full nets'
+// answers are scattered over the student's.
+extern "C" int lg_gated_device(lg_fast *f, lg_ctx *c, const uint8_t *planes_p, const uint8_t *planes_v, int B,
+                               float temperature, float threshold, float *probs, float *value, uint8_t *fallback,
+                               int32_t *count, void *stream) {
+    if (!f || !c || !planes_p || !planes_v || (((uintptr_t)planes_p | (uintptr_t)planes_v) & 3) || B < 1 || !probs ||
+        !value || !(temperature > 0.0f)) {
+        lg_set_error("lg_gated_device: bad arguments (planes 4-byte aligned)");
+        return LG_ERR_ARG;
+    }
+    Net &np = c->nets[LG_NET_POLICY], &nv = c->nets[LG_NET_VALUE];
+    if (!np.present || !nv.present || np.d.precision == LG_FP32 || nv.d.precision == LG_FP32 ||
+        !trunk_fusable(np) || !trunk_fusable(nv)) {
+        lg_set_error("lg_gated_device: the full context needs tensor-core policy and value nets "
+                     "(128 wide, 5x5 first layer)");
+        return LG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lf(fast_mutex(f));
+    std::lock_guard<std::mutex> lc(c->mu);
+    cudaSetDevice(c->device);
+    const size_t bytes_p = (size_t)np.d.c_in * kPoints, bytes_v = (size_t)nv.d.c_in * kPoints;
+    GateScratch g{};
+    int rc = fast_gate_scratch(f, bytes_p, bytes_v, &g);
+    if (rc) return rc;
+    if (B > g.max_batch || g.device != c->device || g.c_in != np.d.c_in || bytes_p % 4 || bytes_v % 4) {
+        lg_set_error("lg_gated_device: B above the student's max_batch, another device, or the student's "
+                     "input planes differ from the policy net's");
+        return LG_ERR_ARG;
+    }
+    rc = check_fault(c);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    int nl = 0;
+    long long total = 0;
+    rc = fast_forward(f, planes_p, B, temperature, probs, nullptr, value, g.entropy, s, &nl);
+    if (rc) return rc;
+    total += nl;
+    launch_gate(g.entropy, B, threshold, fallback ? fallback : g.fallback, g.idx, g.count, count, s);
+    launch_gate_gather(planes_p, (int)bytes_p, g.idx, g.count, B, g.planes_p, s);
+    launch_gate_gather(planes_v, (int)bytes_v, g.idx, g.count, B, g.planes_v, s);
+    total += 3;
+    for (int b0 = 0; b0 < B; b0 += c->max_batch) {
+        const int nb = std::min(c->max_batch, B - b0);
+        rc = forward_tc(c, np, g.planes_p + (size_t)b0 * bytes_p, nb, temperature, g.probs + (size_t)b0 * kPoints,
+                        nullptr, nullptr, s, &nl, c->profiling, false, g.count, b0);
+        if (rc) return rc;
+        total += nl;
+        rc = forward_tc(c, nv, g.planes_v + (size_t)b0 * bytes_v, nb, 1.0f, nullptr, nullptr, g.value + b0, s, &nl,
+                        c->profiling, false, g.count, b0);
+        if (rc) return rc;
+        total += nl;
+    }
+    launch_gate_scatter(g.probs, g.value, g.idx, g.count, B, probs, value, s);
+    total += 1;
+    c->launches += total;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        lg_set_error("lg_gated_device: launch failed: %s", cudaGetErrorString(e));
+        return LG_ERR_CUDA;
+    }
+    return LG_OK;
 }
 
 extern "C" int lg_submit(lg_ctx *c, int net, const uint8_t *planes, int B, float temperature,

@@ -3,6 +3,8 @@
 #include "../../include/leela_gpu.h"
 #include "lg_common.cuh"
 
+#include <mutex>
+
 namespace lg {
 
 // ------------------------------------------------------------ FP32 path
@@ -16,6 +18,9 @@ void launch_head_conv_f32(const float *in, const float *wh, float bias, int B, i
 // Input of the finish kernels: the head output of point (b, p) is
 //   act_head?(sum_k parts[k * part_stride + b * 361 + p] + head_b).
 // When logits_out is set the finish kernel also writes that value there.
+// With `count` set, only boards b < *count - count_base (read on the device)
+// are processed: the batch size of a launch whose positions were selected
+// on the device.
 struct HeadIn {
     const float *parts;
     int nparts;
@@ -24,8 +29,12 @@ struct HeadIn {
     int head_act;
     int act;
     float *logits_out;
+    const int *count = nullptr;
+    int count_base = 0;
 };
-void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s);
+// entropy (optional): -sum p ln p of each board's probabilities, in nats.
+void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s,
+                    float *entropy = nullptr);
 // Value head: two launches (tiled split-K FC1 pre-activations, then a
 // fixed-order sum, b1, activation, FC2 and the value map); `part` holds
 // value_fc_part_floats(B, H) floats.  w1s is W1 sliced by
@@ -74,8 +83,9 @@ int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t
 // Expanded 5x5 input: planes [B][C][361] bytes -> L5 rows (BF16, or FP16
 // when f16) with halves*64 channels: channel dx*C + c = plane c at
 // (y, x + dx - 2).
+// With count set, boards b >= *count - count_base are skipped.
 void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, bool f16, __nv_bfloat16 *out,
-                           cudaStream_t s);
+                           cudaStream_t s, const int *count = nullptr, int count_base = 0);
 // Writes the layer output (L3 rows) or, for the fused head, the head output
 // before its bias into parts[boards*361] (tc_head_parts() = 1 array).
 // Returns LG_ERR_ARG if no kernel covers the shape.
@@ -109,6 +119,11 @@ struct TcTrunk {
     // wait for a flag that nothing publishes (-1: none)
     uint32_t wait_limit = 0, poll_limit = 0;
     int stall_item = -1;
+    // device-side batch size: with count set, only the first
+    // *count - count_base boards of the rows are computed (rows and rows5
+    // give the buffers' extent)
+    const int *count = nullptr;
+    int count_base = 0;
 };
 // flags: trunk_flag_ints(rows, rows5) ints of device scratch (reset by the launch).
 int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
@@ -176,6 +191,32 @@ int lat_init_device();
 int lat_grid(int B, int sm_count);
 // mode 0: FP32 nets; 1 / 2: BF16 / FP16 activations on the layers marked mma
 int launch_lat(const LatParams &p, int mode, int sm_count, cudaStream_t s);
+
+// ------------------------------------------- distilled student (fast_net.cu)
+//
+// The fused BF16 student trunk + both 1x1 heads, then softmax (+ entropy)
+// and the value FC: four launches for B positions.  The gate kernels pick the
+// positions whose entropy is above a threshold, gather their planes, and put
+// the full nets' answers back in place; all counts stay on the device.
+struct GateScratch {
+    uint8_t *planes_p, *planes_v;
+    float *probs, *value, *entropy;
+    int *idx, *count;
+    uint8_t *fallback;
+    int max_batch, device, c_in;
+};
+int fast_forward(lg_fast *f, const uint8_t *planes, int B, float T, float *probs, float *logits, float *value,
+                 float *entropy, cudaStream_t s, int *nlaunch);
+int fast_gate_scratch(lg_fast *f, size_t bytes_p, size_t bytes_v, GateScratch *g);
+std::mutex &fast_mutex(lg_fast *f);
+int fast_status_word(lg_fast *f);
+int fast_init_device();
+int launch_gate(const float *entropy, int B, float threshold, uint8_t *fallback, int *idx, int *count,
+                int *count_out, cudaStream_t s);
+int launch_gate_gather(const uint8_t *src, int bytes, const int *idx, const int *count, int B, uint8_t *dst,
+                       cudaStream_t s);
+int launch_gate_scatter(const float *fprobs, const float *fvalue, const int *idx, const int *count, int B,
+                        float *probs, float *value, cudaStream_t s);
 
 // 8-symmetry ensemble helpers (ensemble.cu).
 int ensemble_init_tables();

@@ -688,6 +688,8 @@ struct TrunkParams {
     uint32_t wait_limit;  // polls of one mbarrier wait before it gives up
     uint32_t poll_limit;  // polls of one dependency flag before it gives up
     int stall_item;       // test hook: this item waits for a flag nothing sets (-1: none)
+    const int *count;     // device-side batch size (boards), or null: all of rows
+    int count_base;       // boards before this launch's first
 };
 
 // Shared memory of kernel "trunk": window slots sized for the first layer's
@@ -773,11 +775,21 @@ __global__ void __maxnreg__(96)
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 #define WAIT_LIM (p.wait_limit)  // mbarrier waits (try_wait polls): read from the parameter bank at each use
-    const int n3 = (p.rows + C::TP - 1) / C::TP;
-    const int n5 = p.rows5 > 0 ? (p.rows5 + C::TP - 1) / C::TP : 0;
-    const int first = n5 > 0 ? 1 : 0;
+    // rows / rows5: the rows this launch computes (with a device-side count,
+    // the first *count - count_base boards); the flag layout follows the
+    // buffers' extent p.rows
+    int rows = p.rows, rows5 = p.rows5;
+    if (p.count) {
+        const int nb = min(p.rows / kL3Board, max(0, *p.count - p.count_base));
+        rows = nb * kL3Board;
+        rows5 = p.rows5 > 0 ? nb * kL5Board : 0;
+    }
+    const int n3L = (p.rows + C::TP - 1) / C::TP;
+    const int n3 = (rows + C::TP - 1) / C::TP;
+    const int n5 = rows5 > 0 ? (rows5 + C::TP - 1) / C::TP : 0;
+    const int first = p.rows5 > 0 ? 1 : 0;
     const int nitems = n5 + p.nl * n3;
-    int *const flags0 = p.flags + n3 + 1;
+    int *const flags0 = p.flags + n3L + 1;
     // item -> (layer l, chunk j); layer 0 is the first layer when fused
     auto decode = [&](int it, int &l, int &j) {
         if (it < n5) {
@@ -850,7 +862,7 @@ __global__ void __maxnreg__(96)
                 ok = ok && mbar_wait(&win_empty[ws0], ((wn / C::NWIN) & 1) ^ 1, WAIT_LIM);
                 int it = -1;
                 if (ok && !abort_flag) {
-                    it = atomicAdd(p.flags + n3, 1);
+                    it = atomicAdd(p.flags + n3L, 1);
                     if (it >= nitems) it = -1;
                 } else if (!ok) {
                     fail(72);
@@ -867,9 +879,9 @@ __global__ void __maxnreg__(96)
                     // [256j - 24, 256j + 280): an L5 row is the L3 row minus
                     // (board + y), board + y <= rows / 400 + 19
                     const int lo3 = max(0, j * C::TP - C0::WPRE);
-                    const int hi3 = min(p.rows, j * C::TP + C::TP + C0::WPRE);
+                    const int hi3 = min(rows, j * C::TP + C::TP + C0::WPRE);
                     const int lo5 = max(0, lo3 - (hi3 - 1) / kL3Board - kBoard);
-                    const int hi5 = min(p.rows5 - 1, hi3 - 1);
+                    const int hi5 = min(rows5 - 1, hi3 - 1);
                     for (int jj = lo5 / C::TP; jj <= hi5 / C::TP; ++jj)
                         if (!poll_flag(flags0 + jj, 1, p.poll_limit)) {
                             fail(71);
@@ -956,7 +968,7 @@ __global__ void __maxnreg__(96)
                 const bool fl = first && l == 0;
                 // N: the item's rows, rounded up to the MMA's multiple of 16
                 // (rows past the tensor are zero-filled and not stored)
-                const int nrows = fl ? min(C::TP, (p.rows5 - j * C::TP + 15) / 16 * 16) : min(C::TP, p.rows - j * C::TP);
+                const int nrows = fl ? min(C::TP, (rows5 - j * C::TP + 15) / 16 * 16) : min(C::TP, rows - j * C::TP);
                 const uint32_t idesc = idesc_16(128, nrows, F16);
                 const int acc = q & 1;
                 const uint32_t ak = (uint32_t)(q >> 1);
@@ -1010,7 +1022,7 @@ __global__ void __maxnreg__(96)
                                    : (p.scale ? __ldg(p.scale + k * NO + o) : 1.0f);
             const bool head_layer = HEAD && !fl && k == p.nl - 1;
             const CUtensorMap *om = (k & 1) ? &out_a : &out_b;
-            const int rows_l = fl ? p.rows5 : p.rows;
+            const int rows_l = fl ? rows5 : rows;
             const int nrows = min(C::TP, rows_l - cs);
             const int nhalf = max(0, min(2, (nrows - rq * 64 + 31) / 32));
             const int acc = q & 1;
@@ -1122,7 +1134,7 @@ __global__ void __maxnreg__(96)
 #pragma unroll
                     for (int jj = 0; jj < 32; ++jj)
                         f[jj] = act_apply(fmaf(__uint_as_float(v[jj]), scale, bias), p.act) * hw;
-                    head_store<0>(warp_transpose_sum(f, lane), quarter, q_base + c * 32 + lane, p.rows, p.parts,
+                    head_store<0>(warp_transpose_sum(f, lane), quarter, q_base + c * 32 + lane, rows, p.parts,
                                   p.part_stride);
                 } else {
                     const uint32_t use = uses++;
@@ -1140,7 +1152,7 @@ __global__ void __maxnreg__(96)
                     bool valid_lane;
                     if (fl) {
                         int point;
-                        row_target<1>(row_lane, p.rows5, orow, valid_lane, point);
+                        row_target<1>(row_lane, rows5, orow, valid_lane, point);
                     } else {
                         const int rl = row_lane % kL3Board;
                         valid_lane = (rl % kL3Pitch) < kBoard && (rl / kL3Pitch) < kBoard;
@@ -1259,10 +1271,11 @@ __global__ void __maxnreg__(96)
 constexpr int kPackMaxC = 64;
 __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__restrict__ planes, int B,
                                                              int C, int halves, int f16,
-                                                             __nv_bfloat16 *__restrict__ out) {
+                                                             __nv_bfloat16 *__restrict__ out,
+                                                             const int *__restrict__ count, int count_base) {
     __shared__ __align__(16) uint8_t sp[kPackMaxC * kPoints];
     const int b = blockIdx.x;
-    if (b >= B) return;
+    if (b >= B || (count && b >= *count - count_base)) return;
     const uint8_t *src = planes + (size_t)b * C * kPoints;
     const int nbytes = C * kPoints;
     if (((uintptr_t)src & 7) == 0) {
@@ -1323,9 +1336,9 @@ __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__re
 }
 
 void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, bool f16, __nv_bfloat16 *out,
-                           cudaStream_t s) {
+                           cudaStream_t s, const int *count, int count_base) {
     // four CTAs per board, each writing a quarter of its rows
-    pack_planes_l5_kernel<<<dim3(B, 4), 256, 0, s>>>(planes, B, C, halves, f16 ? 1 : 0, out);
+    pack_planes_l5_kernel<<<dim3(B, 4), 256, 0, s>>>(planes, B, C, halves, f16 ? 1 : 0, out, count, count_base);
 }
 
 // ------------------------------------------------------------------ launch
@@ -1438,6 +1451,8 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     p.nl = T.nl;
     p.parts = parts;
     p.part_stride = part_stride;
+    p.count = T.count;
+    p.count_base = T.count_base;
     p.flags = flags;
     p.err = err;
     p.wait_limit = T.wait_limit ? T.wait_limit : kWaitLimit;

@@ -39,6 +39,15 @@ def _bind():
     L.lg_student_train_step.argtypes = [vp, vp, i32, vp, vp, f32, f32, vp, vp]
     L.lg_student_grads.argtypes = [vp, vp, i32, vp, vp, f32, vp, vp]
     L.lg_student_forward.argtypes = [vp, vp, i32, vp, vp, vp]
+    L.lg_fast_param_count.argtypes = [i32, i32, i32]
+    L.lg_fast_param_count.restype = ctypes.c_size_t
+    L.lg_fast_create.argtypes = [i32, i32, i32, i32, i32, vp, P(vp)]
+    L.lg_fast_set_weights.argtypes = [vp, vp]
+    L.lg_fast_destroy.argtypes = [vp]
+    L.lg_fast_destroy.restype = None
+    L.lg_fast_device.argtypes = [vp, vp, i32, f32, vp, vp, vp, vp, vp]
+    L.lg_fast_status.argtypes = [vp, vp]
+    L.lg_gated_device.argtypes = [vp, vp, vp, vp, i32, f32, f32, vp, vp, vp, vp, vp]
     L._student_bound = True
     return L
 
@@ -171,39 +180,81 @@ def entropy(probs):
     return -(probs * torch.log(p)).sum(dim=1)
 
 
-class GatedEvaluator:
-    """Student first (BF16, both heads), full nets for the positions whose
-    student policy entropy exceeds `threshold` nats."""
+class FastNet:
+    """The student served by the fused BF16 kernel (lg_fast_*): trunk and
+    both heads in one launch, then softmax (+ entropy) and the value FC.
+    `params` in the Student flat layout (width 64)."""
 
-    def __init__(self, student_ctx: Context, full_ctx: Context, threshold: float = 2.5):
-        self.s = student_ctx
+    def __init__(self, params, c_in=24, n3x3=5, fc_hidden=64, max_batch=8192, device=0):
+        L = _bind()
+        self.shape = dict(c_in=c_in, n3x3=n3x3, fc_hidden=fc_hidden)
+        self.max_batch = max_batch
+        n = int(L.lg_fast_param_count(c_in, n3x3, fc_hidden))
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != n:
+            raise ValueError(f"student weights have {p.size} floats, the shape needs {n}")
+        self._h = ctypes.c_void_p()
+        _check(L.lg_fast_create(device, c_in, n3x3, fc_hidden, max_batch, p.ctypes.data, ctypes.byref(self._h)))
+
+    def set_weights(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        _check(library().lg_fast_set_weights(self._h, p.ctypes.data))
+
+    def device(self, planes_ptr, B, probs_ptr, value_ptr, temperature=1.0, logits_ptr=None, entropy_ptr=None,
+               stream=None):
+        _check(library().lg_fast_device(self._h, planes_ptr, B, temperature, probs_ptr, logits_ptr, value_ptr,
+                                        entropy_ptr, stream))
+
+    def status(self, stream=None):
+        _check(library().lg_fast_status(self._h, stream))
+
+    def close(self):
+        if self._h:
+            library().lg_fast_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GatedEvaluator:
+    """The learned fast path (lg_gated_device): the student answers every
+    position, positions whose student policy entropy exceeds `threshold`
+    nats are handed to the full nets on the device -- compaction, the full
+    nets' batch sizes and the write-back all stay on the GPU, with no host
+    synchronisation."""
+
+    def __init__(self, fast: FastNet, full_ctx: Context, threshold: float = 2.5):
+        self.s = fast
         self.f = full_ctx
         self.threshold = threshold
 
-    def evaluate(self, planes_p, planes_v, stream=None):
+    def evaluate(self, planes_p, planes_v, stream=None, out=None, temperature=1.0):
         """planes_p / planes_v: device uint8 [B][24][361] (policy / value
-        planes of the same positions).  Returns (probs, values, fallback mask)."""
+        planes of the same positions).  Returns device tensors (probs [B][361],
+        values [B], fallback [B] uint8, count [1] int32); `out`, a tuple of
+        those four, is reused when given."""
         import torch
         B = planes_p.shape[0]
         dev = planes_p.device
-        sp = torch.empty((B, 361), device=dev)
-        sv = torch.empty(B, device=dev)
+        if out is None:
+            out = (torch.empty((B, 361), device=dev), torch.empty(B, device=dev),
+                   torch.empty(B, dtype=torch.uint8, device=dev), torch.empty(1, dtype=torch.int32, device=dev))
+        probs, values, fb, cnt = out
         s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        self.s.policy_device(planes_p.data_ptr(), B, sp.data_ptr(), 1.0, None, s)
-        self.s.value_device(planes_p.data_ptr(), B, sv.data_ptr(), s)
-        mask = entropy(sp) > self.threshold
-        idx = torch.nonzero(mask).flatten()
-        k = int(idx.numel())
-        if k:
-            fp = planes_p.index_select(0, idx).contiguous()
-            fv = planes_v.index_select(0, idx).contiguous()
-            op = torch.empty((k, 361), device=dev)
-            ov = torch.empty(k, device=dev)
-            self.f.policy_device(fp.data_ptr(), k, op.data_ptr(), 1.0, None, s)
-            self.f.value_device(fv.data_ptr(), k, ov.data_ptr(), s)
-            sp.index_copy_(0, idx, op)
-            sv.index_copy_(0, idx, ov)
-        return sp, sv, mask
+        _check(_bind().lg_gated_device(self.s._h, self.f._h, planes_p.data_ptr(), planes_v.data_ptr(), B,
+                                       temperature, self.threshold, probs.data_ptr(), values.data_ptr(),
+                                       fb.data_ptr(), cnt.data_ptr(), s))
+        return probs, values, fb, cnt
 
 
 def calibrate_threshold(entropy_np, agree_np, target=0.97):
@@ -222,73 +273,64 @@ def calibrate_threshold(entropy_np, agree_np, target=0.97):
     return thr, k / n, 1.0 - wrong[k - 1] / n
 
 
-def run_config4(planes_p, planes_v, position_index, mc_winrate, wp, wv, device=0,
-                train_positions=896, steps=3000, time_budget_s=30.0, teacher_temperature=1.0,
-                threshold=2.5, batch=256, seed=0):
-    """Distillation experiment (a distilled 64-wide student with an entropy
-    gate, at the scale of the fixture positions): labels = the full FP32 policy net's softmax at
-    teacher_temperature and 2*mc_owner-1 values; train on positions
-    < train_positions (all symmetries), evaluate on the rest.  Reports the
-    student's top-1 agreement with the full BF16 net, the fallback rate at
-    `threshold` nats and at a threshold calibrated for >= 97% agreement, and
-    leaf evaluations per second of the gated evaluator against the full net
-    alone (inputs resident on the GPU, batches of `batch`)."""
+def run_config4(squares, to_move, mc_winrate, wp, wv, device=0, holdout=65536, train_steps=6000,
+                batch=512, lr=1e-3, teacher_temperatures=(1.0, 0.05), time_budget_s=240.0,
+                eval_batch=8192, seed=0):
+    """The learned fast path at the scale of its configuration.
+
+    Positions: squares [N][361] / to_move [N] (host), planes 0..23 of both
+    sets gathered on the GPU.  Labels: the full FP32 policy net's softmax at
+    each teacher temperature, and 2 * mc_winrate - 1 (Playout::mc_owner(64)
+    win rates of the side to move).  The student (5x5 24->64, 5x 3x3
+    64->64, two heads) is trained by this library's FP32 kernels on the
+    first N - holdout positions and judged on the last `holdout` by the
+    full BF16 nets, as served.  Reports, per teacher temperature: training
+    cost, the student's top-1 agreement with the full net, the fallback rate
+    and agreement of the gate at 2.5 nats and at the threshold calibrated
+    for 97% agreement, and leaf evaluations per second of the full pair,
+    the student alone and the gated path (inputs resident on the GPU,
+    batches of `eval_batch`)."""
     import torch
+    from . import gather_device
     dev = torch.device("cuda", device)
-    N = planes_p.shape[0]
-    d_pp = torch.from_numpy(np.ascontiguousarray(planes_p)).to(dev)
-    d_pv = torch.from_numpy(np.ascontiguousarray(planes_v)).to(dev)
+    N = squares.shape[0]
     stream = torch.cuda.current_stream(dev).cuda_stream
-    with Context(policy=NetDesc.config1_policy(wp, "fp32"), device=device, max_batch=256) as t32:
-        logits = torch.empty((N, 361), device=dev)
-        probs = torch.empty((N, 361), device=dev)
-        t32.policy_device(d_pp.data_ptr(), N, probs.data_ptr(), 1.0, logits.data_ptr(), stream)
-    target = torch.softmax(logits / teacher_temperature, dim=1).contiguous()
-    vt = torch.from_numpy((2.0 * mc_winrate[position_index] - 1.0).astype(np.float32)).to(dev)
-    train_idx = torch.from_numpy(np.nonzero(position_index < train_positions)[0]).to(dev)
-    test_idx = torch.from_numpy(np.nonzero(position_index >= train_positions)[0]).to(dev)
-    st = Student(max_batch=batch, device=device)
-    st.init_he(seed)
+    d_sq = torch.from_numpy(np.ascontiguousarray(squares)).to(dev)
+    d_tm = torch.from_numpy(np.ascontiguousarray(to_move)).to(dev)
+    d_pp = torch.empty((N, 24, 361), dtype=torch.uint8, device=dev)
+    d_pv = torch.empty((N, 24, 361), dtype=torch.uint8, device=dev)
+    gather_device(d_sq.data_ptr(), d_tm.data_ptr(), N, 0, 24, d_pp.data_ptr(), stream)
+    gather_device(d_sq.data_ptr(), d_tm.data_ptr(), N, 1, 24, d_pv.data_ptr(), stream)
+    del d_sq, d_tm
+    ntr = N - holdout
+    vt = torch.from_numpy((2.0 * mc_winrate - 1.0).astype(np.float32)).to(dev)
     t0 = time.perf_counter()
-    log = train(st, d_pp.index_select(0, train_idx).contiguous(),
-                target.index_select(0, train_idx).contiguous(),
-                vt.index_select(0, train_idx).contiguous(), steps, batch=batch, lr=1e-3,
-                seed=seed, log_every=250, time_budget_s=time_budget_s)
-    train_s = time.perf_counter() - t0
-    params = st.get_params()
-    st.close()
-    tp = d_pp.index_select(0, test_idx).contiguous()
-    tv = d_pv.index_select(0, test_idx).contiguous()
-    T = tp.shape[0]
-    T = (T // batch) * batch
-    tp, tv = tp[:T], tv[:T]
-    shape = STUDENT_SHAPE
-    sdesc = dict(policy=NetDesc(params[:_policy_len(shape)], shape["c_in"], shape["width"],
-                                shape["width"], shape["n3x3"], 1, LG_ACT_RELU, 0, 0,
-                                precision="bf16"),
-                 value=NetDesc(_value_part(params, shape), shape["c_in"], shape["width"],
-                               shape["width"], shape["n3x3"], 1, LG_ACT_RELU, 0, 1,
-                               shape["fc_hidden"], 0, precision="bf16"))
-    with Context(device=device, max_batch=batch, **sdesc) as cs, \
-            Context(policy=NetDesc.config1_policy(wp, "bf16"),
-                    value=NetDesc.config1_value(wv, "bf16"), device=device,
-                    max_batch=batch) as cf:
-        # both nets with their kernel choices tuned, as a serving context runs
-        cs.autotune()
-        cf.autotune()
-        sp = torch.empty((T, 361), device=dev)
+    logits = torch.empty((N, 361), device=dev)
+    with Context(policy=NetDesc.config1_policy(wp, "fp32"), device=device, max_batch=1024) as t32:
+        probs = torch.empty((min(N, 65536), 361), device=dev)
+        for b0 in range(0, N, 65536):
+            nb = min(65536, N - b0)
+            t32.policy_device(d_pp[b0].data_ptr(), nb, probs.data_ptr(), 1.0, logits[b0].data_ptr(), stream)
+        del probs
+    torch.cuda.synchronize()
+    label_s = time.perf_counter() - t0
+    te_p, te_v = d_pp[ntr:], d_pv[ntr:]
+    T = (holdout // eval_batch) * eval_batch
+    te_p, te_v = te_p[:T], te_v[:T]
+    out = {"positions": int(N), "train_positions": int(ntr), "holdout_positions": int(T),
+           "teacher_label_seconds": label_s, "value_labels": "2 * mc_owner(64) - 1 (reference Playout.cpp)"}
+    with Context(policy=NetDesc.config1_policy(wp, "bf16"), value=NetDesc.config1_value(wv, "bf16"),
+                 device=device, max_batch=1024) as cf:
+        for b in (256, 1024):
+            cf.set_tuning(b, 3, 0)
         fp = torch.empty((T, 361), device=dev)
         fv = torch.empty(T, device=dev)
-        cs.policy_device(tp.data_ptr(), T, sp.data_ptr(), 1.0, None, stream)
-        cf.policy_device(tp.data_ptr(), T, fp.data_ptr(), 1.0, None, stream)
-        torch.cuda.synchronize()
-        ent = entropy(sp).cpu().numpy()
-        agree = (sp.argmax(1) == fp.argmax(1)).cpu().numpy()
-        thr_cal, share_cal, agree_cal = calibrate_threshold(ent, agree)
+        cf.policy_device(te_p.data_ptr(), T, fp.data_ptr(), 1.0, None, stream)
+        cf.value_device(te_v.data_ptr(), T, fv.data_ptr(), stream)
+        full_top1 = fp.argmax(1)
 
         def timed(fn, reps=3):
-            for _ in range(2):
-                fn()
+            fn()
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
@@ -298,45 +340,79 @@ def run_config4(planes_p, planes_v, position_index, mc_winrate, wp, wv, device=0
             torch.cuda.synchronize()
             return reps * T / (e0.elapsed_time(e1) / 1e3)
 
-        def full_only():
-            for b0 in range(0, T, batch):
-                cf.policy_device(tp[b0].data_ptr(), batch, fp[b0].data_ptr(), 1.0, None, stream)
-                cf.value_device(tv[b0].data_ptr(), batch, fv[b0:].data_ptr(), stream)
+        def full_pair():
+            cf.policy_device(te_p.data_ptr(), T, fp.data_ptr(), 1.0, None, stream)
+            cf.value_device(te_v.data_ptr(), T, fv.data_ptr(), stream)
 
-        def gated(thr):
-            g = GatedEvaluator(cs, cf, thr)
+        out["full_pair_evals_per_s"] = timed(full_pair)
+        for tt in teacher_temperatures:
+            target = torch.softmax(logits[:ntr] / tt, dim=1)
+            st = Student(max_batch=batch, device=device)
+            st.init_he(seed)
+            t0 = time.perf_counter()
+            log = train(st, d_pp[:ntr], target, vt[:ntr], train_steps, batch=batch, lr=lr, seed=seed,
+                        log_every=500, time_budget_s=time_budget_s)
+            train_s = time.perf_counter() - t0
+            del target
+            params = st.get_params()
+            te_t = torch.softmax(logits[ntr:ntr + T] / tt, dim=1)
+            kl, mse = heldout_loss(st, te_p, te_t, vt[ntr:ntr + T], batch=batch)
+            st.close()
+            del te_t
+            res = {"train_steps": int(log[-1][0]) + 1, "batch": batch, "train_seconds": train_s,
+                   "samples_per_s": (int(log[-1][0]) + 1) * batch / train_s,
+                   "heldout_policy_kl": kl, "heldout_value_mse": mse,
+                   "loss_first_last": [log[0], log[-1]]}
+            with FastNet(params, max_batch=eval_batch, device=device) as fast:
+                sp = torch.empty((T, 361), device=dev)
+                sv = torch.empty(T, device=dev)
+                se = torch.empty(T, device=dev)
+                for b0 in range(0, T, eval_batch):
+                    fast.device(te_p[b0].data_ptr(), eval_batch, sp[b0].data_ptr(), sv[b0:].data_ptr(), 1.0,
+                                None, se[b0:].data_ptr(), stream)
+                fast.status(stream)
+                ent = se.cpu().numpy()
+                agree = (sp.argmax(1) == full_top1).cpu().numpy()
+                res["student_top1_agreement_with_full_net"] = float(agree.mean())
+                res["student_value_mae_vs_full_net"] = float((sv - fv).abs().mean().item())
+                res["student_entropy_nats"] = {"p10": float(np.percentile(ent, 10)),
+                                               "median": float(np.median(ent)),
+                                               "p90": float(np.percentile(ent, 90))}
+                thr_cal, share_cal, agree_cal = calibrate_threshold(ent, agree)
 
-            def run():
-                fb = 0
-                for b0 in range(0, T, batch):
-                    _, _, m = g.evaluate(tp[b0:b0 + batch], tv[b0:b0 + batch], stream)
-                    fb += int(m.sum())
-                return fb
-            return run
+                def student_only():
+                    for b0 in range(0, T, eval_batch):
+                        fast.device(te_p[b0].data_ptr(), eval_batch, sp[b0].data_ptr(), sv[b0:].data_ptr(), 1.0,
+                                    None, se[b0:].data_ptr(), stream)
 
-        full_rate = timed(full_only)
-        student_rate = timed(gated(1e9))
-        spec_rate = timed(gated(threshold))
-        cal_rate = timed(gated(thr_cal)) if np.isfinite(thr_cal) else None
-    mask_spec = ent > threshold
-    return {
-        "positions_train": int(train_idx.numel()), "positions_test": int(T),
-        "teacher_temperature": teacher_temperature, "train_steps": int(log[-1][0]) + 1,
-        "train_seconds": train_s, "loss_log": log[::max(1, len(log) // 6)] + [log[-1]],
-        "student_top1_agreement_with_full_net": float(agree.mean()),
-        "student_entropy_nats": {"p10": float(np.percentile(ent, 10)),
-                                 "median": float(np.median(ent)),
-                                 "p90": float(np.percentile(ent, 90))},
-        "gate_spec": {"threshold_nats": threshold, "fallback_rate": float(mask_spec.mean()),
-                      "top1_agreement": float(1.0 - (~agree & ~mask_spec).mean()),
-                      "leaf_evals_per_s": spec_rate,
-                      "speedup_vs_full_net": spec_rate / full_rate},
-        "gate_calibrated_97": {"threshold_nats": thr_cal, "fallback_rate": 1.0 - share_cal,
-                               "top1_agreement": agree_cal, "leaf_evals_per_s": cal_rate,
-                               "speedup_vs_full_net": (cal_rate / full_rate) if cal_rate else None},
-        "student_only_leaf_evals_per_s": student_rate,
-        "full_net_leaf_evals_per_s": full_rate,
-    }
+                res["student_only_evals_per_s"] = timed(student_only)
+                for name, thr in (("gate_2.5", 2.5), ("gate_calibrated_97", thr_cal)):
+                    if not np.isfinite(thr):
+                        res[name] = {"threshold_nats": None, "note": "no threshold keeps 97% agreement"}
+                        continue
+                    g = GatedEvaluator(fast, cf, thr)
+                    bufs = [None]
+                    counts = torch.zeros(T // eval_batch, dtype=torch.int32, device=dev)
+
+                    def gated():
+                        for i, b0 in enumerate(range(0, T, eval_batch)):
+                            bufs[0] = g.evaluate(te_p[b0:b0 + eval_batch], te_v[b0:b0 + eval_batch], stream,
+                                                 bufs[0])
+                            counts[i:i + 1].copy_(bufs[0][3])
+
+                    rate = timed(gated)
+                    fb = float(counts.sum().item()) / T
+                    mask = ent > thr
+                    res[name] = {"threshold_nats": float(thr), "fallback_rate": fb,
+                                 "fallback_rate_host_check": float(mask.mean()),
+                                 "top1_agreement": float(1.0 - (~agree & ~mask).mean()),
+                                 "leaf_evals_per_s": rate,
+                                 "speedup_vs_full_pair": rate / out["full_pair_evals_per_s"]}
+                res["student_only_speedup_vs_full_pair"] = res["student_only_evals_per_s"] / out[
+                    "full_pair_evals_per_s"]
+            out[f"teacher_T{tt:g}"] = res
+            torch.cuda.synchronize()
+    return out
 
 
 def _policy_len(shape):

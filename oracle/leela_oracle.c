@@ -966,3 +966,12 @@ int or_config_board(uint64_t seed, int kmax, int8_t *squares, int32_t *moves) {
     moves[3] = 1;
     return color;
 }
+
+/* Positions start .. start + n - 1 of stream `base` (position i from seed
+ * base + i, as or_config_board): squares [n][361], moves [n][4], to_move [n]. */
+void or_config_boards(uint64_t base, int start, int n, int kmax, int8_t *squares, int32_t *moves,
+                      int8_t *to_move) {
+    for (int i = 0; i < n; ++i)
+        to_move[i] = (int8_t)or_config_board(base + (uint64_t)(start + i), kmax, squares + (size_t)i * OR_POINTS,
+                                             moves + (size_t)i * 4);
+}

@@ -151,6 +151,8 @@ int or_random_board(uint64_t seed, int k, int8_t *squares);
  * squares[361] and moves[4] (last move, the move before it, ko point,
  * white-has-komi flag); returns the side to move. */
 int or_config_board(uint64_t seed, int kmax, int8_t *squares, int32_t *moves);
+void or_config_boards(uint64_t base, int start, int n, int kmax, int8_t *squares, int32_t *moves,
+                      int8_t *to_move);
 
 #ifdef __cplusplus
 }

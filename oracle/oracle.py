@@ -118,6 +118,9 @@ def lib():
                                            ctypes.c_int, ctypes.c_void_p]
             L.or_random_board.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]
             L.or_config_board.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+            L.or_config_boards.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            L.or_config_boards.restype = None
             _lib = L
     return _lib
 
@@ -263,18 +266,35 @@ def random_boards(n: int, seed: int, kmax: int = 300):
     return sq, tm
 
 
-def config_boards(n: int, seed: int, kmax: int = 250, start: int = 0):
+def config_boards(n: int, seed: int, kmax: int = 250, start: int = 0, threads: int | None = None):
     """Positions n of the benchmark configurations' kind (empty board,
     k ~ U[0, kmax] uniform legal moves, simple ko, no suicide), position i
     drawn from stream seed * 2**32 + start + i: (squares [n][361] int8,
     to_move [n] int8, moves [n][4] int32 = last move, the move before it,
-    ko point, white-has-komi flag)."""
+    ko point, white-has-komi flag).  Large sets are generated in chunks on
+    `threads` host threads (the C generator runs without the GIL); every
+    position depends only on its own stream, so the result does not depend
+    on the thread count."""
     sq = np.empty((n, POINTS), dtype=np.int8)
     tm = np.empty(n, dtype=np.int8)
     mv = np.empty((n, 4), dtype=np.int32)
     L = lib()
-    for i in range(n):
-        tm[i] = L.or_config_board(ctypes.c_uint64((seed << 32) + start + i), kmax, _ptr(sq[i]), _ptr(mv[i]))
+    base = ctypes.c_uint64(seed << 32)
+    chunk = 4096
+
+    def run(c0):
+        c1 = min(n, c0 + chunk)
+        L.or_config_boards(base, start + c0, c1 - c0, kmax, _ptr(sq[c0:]), _ptr(mv[c0:]), _ptr(tm[c0:]))
+
+    starts = range(0, n, chunk)
+    nt = threads or min(16, os.cpu_count() or 1)
+    if n <= chunk or nt <= 1:
+        for c0 in starts:
+            run(c0)
+    else:
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(nt) as ex:
+            list(ex.map(run, starts))
     return sq, tm, mv
 
 

@@ -24,6 +24,10 @@
 //   elucheck WP                  bit-compare the harness conv (ELU) with the
 //                                reference convolve<5,24,128>/<3,128,128>
 //   mcowner  N SEED PLAYOUTS THREADS OUT   Playout::mc_owner labels
+//   mcfile   SQ TM MV N PLAYOUTS THREADS OUT  Playout::mc_owner labels of N
+//                                positions given as files: squares int8
+//                                [N][361], to_move int8 [N], moves int32
+//                                [N][4] (last, before last, ko point, komi flag)
 //   time     N SEED THREADS SECS WP WV     reference CPU pos/s, config-1 nets
 #include <algorithm>
 #include <array>
@@ -441,6 +445,62 @@ int cmd_mcowner(int n, int seed, int playouts, const std::string &out) {
     return 0;
 }
 
+// Labels for positions that come as boards (the oracle's generator at scale,
+// where replaying every move list here would be the slow part).  Each
+// position is set up by placing its stones on an empty board: placing the
+// stones of a legal position in any order captures nothing and is never a
+// suicide (a partial string always touches an empty point: one of its final
+// liberties, or a stone of its string not yet placed), so FastState's own
+// play_move builds the same strings, liberties and hashes.  The side to
+// move, the ko point and the last two moves are then set as given.
+// Positions are spread over THREADS caller threads; each calls mc_owner with
+// cfg_num_threads = 1, so every label is exactly PLAYOUTS playouts, run on
+// the engine's thread pool (THREADS workers).
+int cmd_mcfile(const char *sqf, const char *tmf, const char *mvf, int n, int playouts, int threads,
+               const std::string &out) {
+    auto read_all = [](const char *path, size_t bytes) {
+        std::vector<char> v(bytes);
+        std::ifstream f(path, std::ios::binary);
+        if (!f || !f.read(v.data(), (std::streamsize)bytes)) {
+            std::fprintf(stderr, "cannot read %zu bytes from %s\n", bytes, path);
+            std::exit(2);
+        }
+        return v;
+    };
+    const std::vector<char> sq = read_all(sqf, (size_t)n * 361);
+    const std::vector<char> tm = read_all(tmf, (size_t)n);
+    const std::vector<char> mvb = read_all(mvf, (size_t)n * 16);
+    const int32_t *mv = reinterpret_cast<const int32_t *>(mvb.data());
+    std::vector<float> w(n);
+    cfg_num_threads = 1;
+    std::atomic<int> next{0};
+    std::vector<std::thread> ts;
+    for (int t = 0; t < threads; ++t)
+        ts.emplace_back([&]() {
+            for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+                FastState fs;
+                fs.init_game(19, 7.5f);
+                auto vtx = [&](int p) { return p < 0 ? 0 : fs.board.get_vertex(p % 19, p / 19); };
+                for (int p = 0; p < 361; ++p) {
+                    const int c = sq[(size_t)i * 361 + p];
+                    if (c == FastBoard::BLACK || c == FastBoard::WHITE) fs.play_move(c, vtx(p));
+                }
+                fs.set_to_move(tm[i]);
+                fs.m_lastmove = vtx(mv[i * 4 + 0]);
+                fs.m_onebutlastmove = vtx(mv[i * 4 + 1]);
+                fs.m_komove = vtx(mv[i * 4 + 2]);
+                fs.m_passes = 0;
+                fs.m_last_was_capture = false;
+                w[i] = Playout::mc_owner(fs, playouts);
+            }
+        });
+    for (auto &th : ts) th.join();
+    FILE *f = open_out(out, ".mcowner");
+    std::fwrite(w.data(), sizeof(float), (size_t)n, f);
+    std::fclose(f);
+    return 0;
+}
+
 int cmd_time(int n, int seed, int threads, double secs, const char *wp, const char *wv) {
     Config1Net pol{read_floats(wp), false}, val{read_floats(wv), true};
     PositionStream ps(seed);
@@ -481,13 +541,14 @@ int cmd_time(int n, int seed, int threads, double secs, const char *wp, const ch
 
 int main(int argc, char **argv) {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: ref_harness gen|refexact|config|elucheck|mcowner|time ...\n");
+        std::fprintf(stderr, "usage: ref_harness gen|refexact|config|elucheck|mcowner|mcfile|time ...\n");
         return 2;
     }
     std::string cmd = argv[1];
     int threads = 1;
     if (cmd == "mcowner" && argc >= 7) threads = std::atoi(argv[5]);
     if (cmd == "time" && argc >= 5) threads = std::atoi(argv[4]);
+    if (cmd == "mcfile" && argc >= 8) threads = std::atoi(argv[7]);
     init_engine(threads);
     if (cmd == "gen" && argc == 5) return cmd_gen(std::atoi(argv[2]), std::atoi(argv[3]), argv[4]);
     if (cmd == "refexact" && argc == 6)
@@ -498,6 +559,8 @@ int main(int argc, char **argv) {
     if (cmd == "elucheck" && argc == 3) return cmd_elucheck(argv[2]);
     if (cmd == "mcowner" && argc == 7)
         return cmd_mcowner(std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]), argv[6]);
+    if (cmd == "mcfile" && argc == 9)
+        return cmd_mcfile(argv[2], argv[3], argv[4], std::atoi(argv[5]), std::atoi(argv[6]), threads, argv[8]);
     if (cmd == "time" && argc == 8)
         return cmd_time(std::atoi(argv[2]), std::atoi(argv[3]), threads, std::atof(argv[5]), argv[6],
                         argv[7]);

@@ -83,27 +83,68 @@ def test_exported_nets_match_the_student_forward(student_mod, gpu_lib, positions
     st.close()
 
 
-def test_gate_routes_by_entropy(student_mod, gpu_lib, weights, positions):
+@pytest.mark.parametrize("B", [40, 300])
+def test_gate_routes_by_entropy(student_mod, gpu_lib, weights, positions, B):
+    """lg_gated_device: with a threshold no entropy reaches, the student's
+    answers (bit-identical to lg_fast_device); with one below every entropy,
+    the full nets' answers for every position (bit-identical to the full
+    context on the persistent trunk); at the median entropy, each position
+    from the side its entropy picks, and the device-side count equal to the
+    number of fallbacks.  B = 300 spans two chunks of the full context."""
     import torch
     lg = gpu_lib
-    st = student_mod.Student(max_batch=64)
+    st = student_mod.Student(max_batch=8)
     st.init_he(4)
-    pp = torch.from_numpy(np.ascontiguousarray(positions["planes_p"][:40, :24])).cuda()
-    pv = torch.from_numpy(np.ascontiguousarray(positions["planes_v"][:40, :24])).cuda()
-    with lg.Context(policy=st.policy_desc("bf16"), value=st.value_desc("bf16"), max_batch=64) as cs, \
+    params = st.get_params()
+    st.close()
+    idx = np.arange(B) % 1024
+    pp = torch.from_numpy(np.ascontiguousarray(positions["planes_p"][idx, :24])).cuda()
+    pv = torch.from_numpy(np.ascontiguousarray(positions["planes_v"][idx, :24])).cuda()
+    with student_mod.FastNet(params, max_batch=512) as fast, \
             lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
                        value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"),
-                       max_batch=64) as cf:
-        never = student_mod.GatedEvaluator(cs, cf, threshold=1e9)
-        p, v, m = never.evaluate(pp, pv)
-        assert not m.any().item()
-        assert np.array_equal(p.cpu().numpy(), cs.policy(pp.cpu().numpy()))
-        always = student_mod.GatedEvaluator(cs, cf, threshold=-1.0)
-        p, v, m = always.evaluate(pp, pv)
-        assert m.all().item()
-        assert np.array_equal(p.cpu().numpy(), cf.policy(pp.cpu().numpy()))
-        assert np.array_equal(v.cpu().numpy(), cf.value(pv.cpu().numpy()))
-    st.close()
+                       max_batch=256) as cf:
+        sp = torch.empty((B, 361), device="cuda")
+        sv = torch.empty(B, device="cuda")
+        se = torch.empty(B, device="cuda")
+        fast.device(pp.data_ptr(), B, sp.data_ptr(), sv.data_ptr(), 1.0, None, se.data_ptr())
+        fast.status()
+        sp, sv, se = sp.cpu().numpy(), sv.cpu().numpy(), se.cpu().numpy()
+        # the full nets as the gated path runs them: persistent trunk with
+        # the first layer inside, chunks of 256
+        for b in (B % 256 or 256, 256):
+            cf.set_tuning(b, 3, 0)
+        fp = cf.policy(pp.cpu().numpy())
+        fv = cf.value(pv.cpu().numpy())
+        for thr, expect in ((1e9, "student"), (-1.0, "full"), (float(np.median(se)), "mixed")):
+            g = student_mod.GatedEvaluator(fast, cf, threshold=thr)
+            p, v, m, n = g.evaluate(pp, pv)
+            torch.cuda.synchronize()
+            fast.status()
+            p, v, m, n = p.cpu().numpy(), v.cpu().numpy(), m.cpu().numpy().astype(bool), int(n.item())
+            want = se > thr
+            assert np.array_equal(m, want), thr
+            assert n == int(want.sum())
+            assert np.array_equal(p[~want], sp[~want]) and np.array_equal(v[~want], sv[~want]), thr
+            assert np.array_equal(p[want], fp[want]) and np.array_equal(v[want], fv[want]), thr
+            if expect == "student":
+                assert n == 0
+            elif expect == "full":
+                assert n == B
+            else:
+                assert 0 < n < B
+
+
+def test_gate_needs_tensor_core_full_nets(student_mod, gpu_lib, weights, positions):
+    import torch
+    lg = gpu_lib
+    n = int(student_mod._bind().lg_fast_param_count(24, 5, 64))
+    pp = torch.zeros((4, 24, 361), dtype=torch.uint8, device="cuda")
+    with student_mod.FastNet(np.zeros(n, np.float32), max_batch=8) as fast, \
+            lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "fp32"),
+                       value=lg.NetDesc.config1_value(weights["cfg_v"][1], "fp32"), max_batch=8) as c32:
+        with pytest.raises(lg.LeelaGPUError):
+            student_mod.GatedEvaluator(fast, c32, 2.5).evaluate(pp, pp)
 
 
 def test_training_gains_over_the_untrained_student(student_mod, gpu_lib, weights, positions):
