@@ -109,6 +109,22 @@ __device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
     return d;
 }
 
+// The MMAs of one weight slice against all 7 row tiles: A = the buffer rows
+// from descriptor a0 on (tile t 128 rows further: 1024 units of 16 bytes),
+// B = the slice at b0; K steps of 16 channels = 32 bytes = 2 units.  The
+// descriptors are a base plus compile-time offsets, so the issuing thread
+// spends an add per operand and MMA.  FIRST: the slice starts every
+// accumulator.
+template <bool FIRST>
+__device__ __forceinline__ void fast_slice(uint32_t tmem, uint64_t a0, uint64_t b0, uint32_t idesc) {
+#pragma unroll
+    for (int t = 0; t < kFTiles; ++t)
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+            mma_bf16(tmem + (uint32_t)(kFW * t), a0 + (uint64_t)(t * 1024 + 2 * kk), b0 + (uint64_t)(2 * kk), idesc,
+                     (FIRST && kk == 0) ? 0u : 1u);
+}
+
 __global__ void __launch_bounds__(kFThreads, 1)
     fast_trunk_kernel(const __grid_constant__ CUtensorMap w_map, const FastParams p) {
     extern __shared__ uint8_t smem_raw[];
@@ -192,7 +208,8 @@ __global__ void __launch_bounds__(kFThreads, 1)
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(128, kFW);
-            const uint32_t buf_a = smem_u32(buf);
+            const uint64_t a_base = sdesc_sw128(smem_u32(buf));
+            const uint64_t b_base = sdesc_sw128(smem_u32(wst));
             uint32_t g = 0, n_stage = 0, n_act = 0;
             for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
                 // first layer: two 64-channel halves of the expanded rows
@@ -205,15 +222,12 @@ __global__ void __launch_bounds__(kFThreads, 1)
                         const uint32_t k = g / kFStages;
                         if (!mbar_wait(&w_full[st], k & 1, WL)) { fail(93); goto done_mma; }
                         tc_fence_after();
-                        const uint32_t b_base = smem_u32(wst + st * kFSlice);
-                        for (int t = 0; t < kFTiles; ++t) {
-                            const uint32_t a_base =
-                                buf_a + (uint32_t)(kFPre + 128 * t + kFPitch * (dy - 2)) * 128u;
-#pragma unroll
-                            for (int kk = 0; kk < 4; ++kk)
-                                mma_bf16(tmem + (uint32_t)(kFW * t), sdesc_sw128(a_base + kk * 32),
-                                         sdesc_sw128(b_base + kk * 32), idesc, (h | dy | kk) ? 1u : 0u);
-                        }
+                        const uint64_t a0 = a_base + (uint64_t)((kFPre + kFPitch * (dy - 2)) * 8);
+                        const uint64_t b0 = b_base + (uint64_t)(st * (kFSlice >> 4));
+                        if (h == 0 && dy == 0)
+                            fast_slice<true>(tmem, a0, b0, idesc);
+                        else
+                            fast_slice<false>(tmem, a0, b0, idesc);
                         mma_commit(&w_empty[st]);
                     }
                     if (h == 0) mma_commit(&half_done);
@@ -228,15 +242,13 @@ __global__ void __launch_bounds__(kFThreads, 1)
                         const uint32_t k = g / kFStages;
                         if (!mbar_wait(&w_full[st], k & 1, WL)) { fail(95); goto done_mma; }
                         tc_fence_after();
-                        const uint32_t b_base = smem_u32(wst + st * kFSlice);
                         const int shift = kFPitch * (tap / 3 - 1) + (tap % 3 - 1);
-                        for (int t = 0; t < kFTiles; ++t) {
-                            const uint32_t a_base = buf_a + (uint32_t)(kFPre + 128 * t + shift) * 128u;
-#pragma unroll
-                            for (int kk = 0; kk < 4; ++kk)
-                                mma_bf16(tmem + (uint32_t)(kFW * t), sdesc_sw128(a_base + kk * 32),
-                                         sdesc_sw128(b_base + kk * 32), idesc, (tap | kk) ? 1u : 0u);
-                        }
+                        const uint64_t a0 = a_base + (uint64_t)((kFPre + shift) * 8);
+                        const uint64_t b0 = b_base + (uint64_t)(st * (kFSlice >> 4));
+                        if (tap == 0)
+                            fast_slice<true>(tmem, a0, b0, idesc);
+                        else
+                            fast_slice<false>(tmem, a0, b0, idesc);
                         mma_commit(&w_empty[st]);
                     }
                     mma_commit(&acc_full);
@@ -338,38 +350,47 @@ __global__ void __launch_bounds__(kFThreads, 1)
                 tc_fence_after();
                 const bool last = l == nl - 1;
                 const float *bias = s_bias + l * kFW + chh * 32;
-                for (int t = 0; t < kFTiles; ++t) {
-                    const int q = 128 * t + 32 * qd + lane;
-                    const int b = q / kFRowsB, r = q - b * kFRowsB, y = r / kFPitch, x = r - y * kFPitch;
-                    const bool valid = b < nb && y < kBoard && x < kBoard;
-                    uint32_t v[32];
-                    tmem_ld32(tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(kFW * t + 32 * chh), v);
+                const uint32_t t_row = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(32 * chh);
+                // two tiles per TMEM round trip
+#pragma unroll
+                for (int t0 = 0; t0 < kFTiles; t0 += 2) {
+                    constexpr int kPair = 2;
+                    const int nt = (t0 + 1 < kFTiles) ? kPair : 1;
+                    uint32_t v[kPair][32];
+                    tmem_ld32(t_row + (uint32_t)(kFW * t0), v[0]);
+                    if (nt == 2) tmem_ld32(t_row + (uint32_t)(kFW * (t0 + 1)), v[1]);
                     tmem_ld_wait();
-                    if (!last) {
-                        uint32_t w[16];
 #pragma unroll
-                        for (int i = 0; i < 16; ++i)
-                            w[i] = valid ? relu_bf16x2(__uint_as_float(v[2 * i]) + bias[2 * i],
-                                                       __uint_as_float(v[2 * i + 1]) + bias[2 * i + 1])
-                                         : 0u;
-                        const int R = q + kFPre;
-                        uint8_t *row = buf + R * 128;
+                    for (int u = 0; u < nt; ++u) {
+                        const int q = 128 * (t0 + u) + 32 * qd + lane;
+                        const int b = q / kFRowsB, r = q - b * kFRowsB, y = r / kFPitch, x = r - y * kFPitch;
+                        const bool valid = b < nb && y < kBoard && x < kBoard;
+                        if (!last) {
+                            uint32_t w[16];
 #pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            *reinterpret_cast<uint4 *>(row + (((4 * chh + k) ^ (R & 7)) << 4)) =
-                                make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
-                    } else {
-                        float sp = 0.0f, sv = 0.0f;
+                            for (int i = 0; i < 16; ++i)
+                                w[i] = valid ? relu_bf16x2(__uint_as_float(v[u][2 * i]) + bias[2 * i],
+                                                           __uint_as_float(v[u][2 * i + 1]) + bias[2 * i + 1])
+                                             : 0u;
+                            const int R = q + kFPre;
+                            uint8_t *row = buf + R * 128;
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) {
-                            const float f = fmaxf(__uint_as_float(v[i]) + bias[i], 0.0f);
-                            sp = fmaf(f, s_wp[32 * chh + i], sp);
-                            sv = fmaf(f, s_wv[32 * chh + i], sv);
-                        }
-                        if (valid) {
-                            const size_t idx = (size_t)(grp * kFG + b) * kPoints + y * kBoard + x;
-                            p.parts_p[chh * p.part_stride + idx] = sp;
-                            p.parts_v[chh * p.part_stride + idx] = sv;
+                            for (int k = 0; k < 4; ++k)
+                                *reinterpret_cast<uint4 *>(row + (((4 * chh + k) ^ (R & 7)) << 4)) =
+                                    make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+                        } else {
+                            float sp = 0.0f, sv = 0.0f;
+#pragma unroll
+                            for (int i = 0; i < 32; ++i) {
+                                const float f = fmaxf(__uint_as_float(v[u][i]) + bias[i], 0.0f);
+                                sp = fmaf(f, s_wp[32 * chh + i], sp);
+                                sv = fmaf(f, s_wv[32 * chh + i], sv);
+                            }
+                            if (valid) {
+                                const size_t idx = (size_t)(grp * kFG + b) * kPoints + y * kBoard + x;
+                                p.parts_p[chh * p.part_stride + idx] = sp;
+                                p.parts_v[chh * p.part_stride + idx] = sv;
+                            }
                         }
                     }
                 }
