@@ -344,6 +344,15 @@ __global__ void __launch_bounds__(kFThreads, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(&stage_full);
 
+            // which of this thread's 7 rows (one per tile) are board points,
+            // and for those the point's index in the batch
+            uint32_t vmask = 0;
+#pragma unroll
+            for (int t = 0; t < kFTiles; ++t) {
+                const int q = 128 * t + 32 * qd + lane;
+                const int b = q / kFRowsB, r = q - b * kFRowsB, y = r / kFPitch, x = r - y * kFPitch;
+                if (b < nb && y < kBoard && x < kBoard) vmask |= 1u << t;
+            }
             for (int l = 0; l < nl; ++l) {
                 if (!mbar_wait(&acc_full, n_acc & 1, WL)) { fail(98); goto done_epi; }
                 ++n_acc;
@@ -363,8 +372,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
 #pragma unroll
                     for (int u = 0; u < nt; ++u) {
                         const int q = 128 * (t0 + u) + 32 * qd + lane;
-                        const int b = q / kFRowsB, r = q - b * kFRowsB, y = r / kFPitch, x = r - y * kFPitch;
-                        const bool valid = b < nb && y < kBoard && x < kBoard;
+                        const bool valid = (vmask >> (t0 + u)) & 1u;
                         if (!last) {
                             uint32_t w[16];
 #pragma unroll
@@ -387,6 +395,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
                                 sv = fmaf(f, s_wv[32 * chh + i], sv);
                             }
                             if (valid) {
+                                const int b = q / kFRowsB, r = q - b * kFRowsB, y = r / kFPitch, x = r - y * kFPitch;
                                 const size_t idx = (size_t)(grp * kFG + b) * kPoints + y * kBoard + x;
                                 p.parts_p[chh * p.part_stride + idx] = sp;
                                 p.parts_v[chh * p.part_stride + idx] = sv;

@@ -162,3 +162,49 @@ def test_config2_generator_reproduces_the_fixture(oracle_mod):
     assert hashlib.sha256(tm.tobytes()).hexdigest()[:16] == str(d["to_move_sha256"])
     # positions of the configurations' kind: stone density near the fixture's
     assert 0.2 < (sq != 2).mean() < 0.45 and (mv[:, 3] == 1).all()
+
+
+def test_config4_labels_fixture(oracle_mod):
+    """The learned fast path's value labels (tests/golden/make_config4.py):
+    one Playout::mc_owner(64) win rate of the side to move per position of
+    oracle.config_boards(n, seed 4), stored exactly as multiples of 1/128;
+    the generator reproduces the boards they belong to."""
+    import hashlib
+    d = np.load(os.path.join(GOLDEN, "config4_mcowner.npz"))
+    n = int(d["n"])
+    w = d["winrate_x128"]
+    assert n == 1 << 20 and w.shape == (n,) and int(d["playouts"]) == 64
+    assert w.max() <= 128 and 0.45 < w.mean() / 128 < 0.55
+    sq, tm, _ = oracle_mod.config_boards(n, int(d["seed"]))
+    assert hashlib.sha256(sq.tobytes()).hexdigest()[:16] == str(d["squares_sha256"])
+    assert hashlib.sha256(tm.tobytes()).hexdigest()[:16] == str(d["to_move_sha256"])
+
+
+def test_config4_labels_agree_with_a_fresh_reference_labelling(oracle_mod):
+    """Where the reference sources are at hand (LEELA_REF), the reference's
+    own mc_owner(64) run again on the first 512 positions (other random
+    playouts) agrees with the stored labels as two 64-playout estimates of
+    one win rate do: mean absolute difference below 0.1, correlation above
+    0.8."""
+    import subprocess
+    import tempfile
+    ref = os.environ.get("LEELA_REF")
+    if not ref or not os.path.isdir(ref):
+        pytest.skip("LEELA_REF not set")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(root, "oracle"), "ref", f"REF={ref}"], check=True)
+    d = np.load(os.path.join(GOLDEN, "config4_mcowner.npz"))
+    n = 512
+    sq, tm, mv = oracle_mod.config_boards(n, int(d["seed"]))
+    with tempfile.TemporaryDirectory() as td:
+        pre = os.path.join(td, "c")
+        sq.tofile(pre + ".sq")
+        tm.tofile(pre + ".tm")
+        mv.tofile(pre + ".mv")
+        subprocess.run([os.path.join(root, "oracle", "_ref", "ref_harness"), "mcfile", pre + ".sq", pre + ".tm",
+                        pre + ".mv", str(n), "64", str(min(8, os.cpu_count() or 1)), pre], check=True,
+                       stderr=subprocess.DEVNULL)
+        w = np.fromfile(pre + ".mcowner", np.float32)
+    stored = d["winrate_x128"][:n] / 128.0
+    assert np.abs(w - stored).mean() < 0.1
+    assert np.corrcoef(w, stored)[0, 1] > 0.8
