@@ -420,7 +420,15 @@ def summarize(x, value):
     if b1:
         out["fp32_batch1_pairs_per_s"] = r(b1.get("small_batch_device_pairs_per_s"), 1)
         out["fp32_batch1_host_api_pairs_per_s"] = r(b1.get("small_batch_host_api_pairs_per_s"), 1)
+        # the headline value (a step of 8192 through batches of 256) and the
+        # autotuned batch-256 pair rates of BF16 and FP16 against FP32 at batch 1
         out["ratio_bf16_b256_vs_fp32_b1"] = r(value / b1["small_batch_device_pairs_per_s"], 1)
+        if "bf16_by_batch_positions_per_s" in x:
+            out["ratio_bf16_b256_pair_rate_vs_fp32_b1"] = r(
+                x["bf16_by_batch_positions_per_s"]["256"] / b1["small_batch_device_pairs_per_s"], 1)
+        if "fp16_b256_pairs_per_s" in x:
+            out["ratio_fp16_b256_pair_rate_vs_fp32_b1"] = r(
+                x["fp16_b256_pairs_per_s"] / b1["small_batch_device_pairs_per_s"], 1)
     if "bf16_by_batch_positions_per_s" in x:
         out["bf16_pairs_per_s_by_batch"] = {k: round(v) for k, v in x["bf16_by_batch_positions_per_s"].items()}
     if "fp16_b256_pairs_per_s" in x:
@@ -794,12 +802,13 @@ def student_run(reps):
 
 def distill_rates(wp, wv, planes_p, planes_v, device, N=8192):
     """Leaf evaluations per second of the learned fast path's pieces on the
-    8192 benchmark inputs (resident on the GPU): the full BF16 pair as the
-    headline serves it (autotuned, batches of 256), the student alone (fused
-    kernel, one call of 8192), and the gated path at fallback rates of 0%,
-    ~10% and 100% (thresholds at entropy percentiles of this student).  The
-    speed does not depend on what the student learned -- the fallback rate
-    does (the trained students: bench.py --distill-run)."""
+    8192 benchmark inputs (resident on the GPU): the full BF16 pair
+    (autotuned, batches of up to 1024, its fastest serving size here), the
+    student alone (fused kernel, one call of 8192), and the gated path at
+    fallback rates of 0%, ~10% and 100% (thresholds at entropy percentiles
+    of this student).  The speed does not depend on what the student
+    learned -- the fallback rate does (the trained students: bench.py
+    --distill-run)."""
     import tempfile
 
     import torch
@@ -829,8 +838,8 @@ def distill_rates(wp, wv, planes_p, planes_v, device, N=8192):
 
     out = {}
     with lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"), value=lg.NetDesc.config1_value(wv, "bf16"),
-                    device=device, max_batch=BATCH) as cf, distill.FastNet(params, max_batch=N, device=device) as fast:
-        cf.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{BATCH}.json"))
+                    device=device, max_batch=1024) as cf, distill.FastNet(params, max_batch=N, device=device) as fast:
+        cf.autotune(os.path.join(tempfile.gettempdir(), "leela_gb300_tune_1024.json"))
         fp = torch.empty((N, 361), device=dev)
         fv = torch.empty(N, device=dev)
         se = torch.empty(N, device=dev)

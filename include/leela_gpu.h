@@ -295,9 +295,11 @@ LG_API int lg_student_forward(lg_student *st, const uint8_t *planes, int B, floa
  * multiple of 4 up to 24.  No reference counterpart: the engine evaluates
  * every leaf with the full nets (UCTNode.cpp:74-121, Network.cpp:590-674).
  *
- * lg_fast_device is asynchronous on `stream` (device pointers; logits and
- * entropy may be NULL); lg_fast_status waits for the stream and reports a
- * kernel's error word (LG_ERR_DEVICE) if one gave up a bounded wait. */
+ * lg_fast_device is asynchronous on `stream` (device pointers; planes
+ * 4-byte aligned, bytes 0 or 1 -- other values are read as their lowest
+ * bit; logits and entropy may be NULL); lg_fast_status waits for the
+ * stream and reports a kernel's error word (LG_ERR_DEVICE) if one gave up a
+ * bounded wait. */
 typedef struct lg_fast lg_fast;
 LG_API size_t lg_fast_param_count(int c_in, int n3x3, int fc_hidden);
 LG_API int lg_fast_create(int device, int c_in, int n3x3, int fc_hidden, int max_batch, const float *weights,

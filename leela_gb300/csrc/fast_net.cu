@@ -7,31 +7,33 @@
 // Network.cpp:590-674).  The student (5x5 c_in -> 64, n3x3 x 3x3 64 -> 64,
 // ReLU; a 1x1 policy head and a 1x1 value head on the same trunk) is small
 // enough that a layer-per-launch schedule is all overhead, so one kernel
-// runs the whole trunk for two boards at a time with the activations never
-// leaving shared memory:
+// runs the whole trunk with the activations never leaving shared memory:
 //
-//   * layout: a group of two boards is 840 rows of pitch 20 (19 points + a
-//     zero column) and 21 rows per board (19 + two zero rows), so both the
-//     3x3 taps (row shifts 20*dy + dx) and the 5x5 first layer's vertical
-//     taps (shifts 20*dy, |dy| <= 2) stay inside a board or land on its
-//     zero rows.  Rows are 128 bytes (64 BF16 channels) in the 128-byte
-//     swizzled form the tensor core reads, with 40 rows of margin before and
-//     after: 976 rows, 122 KB, one buffer per CTA;
-//   * the MMA: M = 128 rows (7 tiles cover the group), N = 64 output
+//   * layout: a board is 420 rows of pitch 20 (19 points + a zero column)
+//     and 21 rows (19 + two zero rows), so both the 3x3 taps (row shifts
+//     20*dy + dx) and the 5x5 first layer's vertical taps (shifts 20*dy,
+//     |dy| <= 2) stay inside the board or land on its zero rows.  Rows are
+//     128 bytes (64 BF16 channels) in the 128-byte swizzled form the tensor
+//     core reads, with 40 rows of margin before and after: 592 rows (74 KB)
+//     per board;
+//   * two boards ("slots") are in flight per CTA, each with its own buffer
+//     and its own 256 TMEM columns: the MMA thread issues layer l of slot 0,
+//     layer l of slot 1, layer l + 1 of slot 0, ..., so one slot's epilogue
+//     (or plane staging) runs while the tensor core works on the other's;
+//   * the MMA: M = 128 rows (4 tiles cover a board), N = 64 output
 //     channels, K = 16 per instruction; A = the activation rows read at the
 //     tap's row shift, B = one tap's weights (64 x 64, 8 KB) streamed by TMA
-//     through a ring of 4 stages.  Taps are the outer loop, so each weight
-//     slice is loaded once per group and all 7 tile accumulators (7 x 64
-//     TMEM columns) are live together;
+//     through a ring of 4 stages.  Taps are the outer loop within a job, so
+//     all 4 tile accumulators of the slot are live together;
 //   * the first layer is the 5x5 conv as 5 vertical taps over rows that
 //     hold the 5 horizontal taps x c_in planes side by side (channel
 //     dx * c_in + c = plane c at (y, x + dx - 2)), 128 channels staged in
-//     two 64-channel halves: the second half is staged once the first
+//     two 64-channel halves: a slot's second half is staged once its first
 //     half's MMAs have completed;
 //   * each layer's epilogue (TMEM -> + bias -> ReLU -> BF16) writes its
-//     output back into the same buffer in place: it runs only after every
-//     MMA of the layer has completed, and the next layer's MMAs start once
-//     all epilogue warps have written and fenced their rows;
+//     output back into the slot's buffer in place: it runs only after every
+//     MMA of that slot's layer has completed, and the slot's next layer
+//     starts once all epilogue warps have written and fenced their rows;
 //   * the last layer's epilogue applies both 1x1 heads to its row and
 //     writes two partial sums per head (one per 32-channel half) to global
 //     memory; the softmax and the value FC run as the library's finish
@@ -57,13 +59,13 @@ using namespace ptx;
 namespace {
 
 constexpr int kFW = 64;                              // trunk width
-constexpr int kFG = 2;                               // boards per group
+constexpr int kFSlots = 2;                           // boards in flight per CTA
 constexpr int kFPitch = 20;
 constexpr int kFRowsB = 21 * kFPitch;                // 420 rows per board
-constexpr int kFRows = kFG * kFRowsB;                // 840
-constexpr int kFTiles = (kFRows + 127) / 128;        // 7
+constexpr int kFTiles = (kFRowsB + 127) / 128;       // 4 row tiles per board
 constexpr int kFPre = 40;                            // margin rows before / after
-constexpr int kFBufRows = kFPre + kFTiles * 128 + kFPre;  // 976
+constexpr int kFBufRows = kFPre + kFTiles * 128 + kFPre;  // 592
+constexpr int kFBufBytes = kFBufRows * 128;
 constexpr int kFStages = 4;
 constexpr int kFSlice = kFW * 128;                   // 64 outputs x 64 K, BF16
 constexpr int kFMaxCin = 24;
@@ -73,17 +75,18 @@ constexpr int kFEpiThreads = kFEpiWarps * 32;
 constexpr int kFThreads = 64 + kFEpiThreads;         // 320
 constexpr uint32_t kFWaitLimit = 1u << 26;
 
-constexpr int OFF_BUF = 0;
-constexpr int OFF_WST = OFF_BUF + kFBufRows * 128;                     // 124,928
+constexpr int OFF_BUF = 0;                                             // kFSlots x 592 rows
+constexpr int OFF_WST = OFF_BUF + kFSlots * kFBufBytes;                // 151,552
 constexpr int OFF_PL = OFF_WST + kFStages * kFSlice;                   // planes of a group
-constexpr int OFF_MASK = OFF_PL + ((kFG * kFMaxCin * kPoints + 127) / 128) * 128;
-constexpr int OFF_LUT = OFF_MASK + ((kFG * kPoints * 4 + 127) / 128) * 128;
+constexpr int OFF_MASK = OFF_PL + ((kFSlots * kFMaxCin * kPoints + 127) / 128) * 128;
+constexpr int OFF_LUT = OFF_MASK + ((kFSlots * kPoints * 4 + 127) / 128) * 128;
 constexpr int OFF_BIAS = OFF_LUT + 256 * 16;
 constexpr int OFF_HEAD = OFF_BIAS + kFMaxLayers * kFW * 4;
 constexpr int SMEM_USED = OFF_HEAD + 2 * kFW * 4;
 constexpr int kFSmem = 1024 + SMEM_USED;
-static_assert(OFF_WST % 1024 == 0, "weight stages keep the 1024-byte swizzle alignment");
+static_assert(kFBufBytes % 1024 == 0 && OFF_WST % 1024 == 0, "buffers keep the 1024-byte swizzle alignment");
 static_assert(kFSmem <= 227 * 1024, "shared memory budget");
+static_assert(kFSlots * kFTiles * kFW <= 512, "accumulators fit the tensor memory");
 
 struct FastParams {
     const uint8_t *planes;   // [B][c_in][361]
@@ -109,12 +112,12 @@ __device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
     return d;
 }
 
-// The MMAs of one weight slice against all 7 row tiles: A = the buffer rows
-// from descriptor a0 on (tile t 128 rows further: 1024 units of 16 bytes),
-// B = the slice at b0; K steps of 16 channels = 32 bytes = 2 units.  The
-// descriptors are a base plus compile-time offsets, so the issuing thread
-// spends an add per operand and MMA.  FIRST: the slice starts every
-// accumulator.
+// The MMAs of one weight slice against a board's 4 row tiles: A = the
+// buffer rows from descriptor a0 on (tile t 128 rows further: 1024 units of
+// 16 bytes), B = the slice at b0; K steps of 16 channels = 32 bytes = 2
+// units.  The descriptors are a base plus compile-time offsets, so the
+// issuing thread spends an add per operand and MMA.  FIRST: the slice
+// starts every accumulator.
 template <bool FIRST>
 __device__ __forceinline__ void fast_slice(uint32_t tmem, uint64_t a0, uint64_t b0, uint32_t idesc) {
 #pragma unroll
@@ -125,6 +128,11 @@ __device__ __forceinline__ void fast_slice(uint32_t tmem, uint64_t a0, uint64_t 
                      (FIRST && kk == 0) ? 0u : 1u);
 }
 
+// Two boards in flight per CTA, each in its own buffer (slot) and its own
+// 256 TMEM columns, so that one board's epilogue (or plane staging) runs
+// while the tensor core works on the other's layer: the MMA thread issues
+// (layer l, slot 0), (l, slot 1), (l + 1, slot 0), ... and each job waits
+// only for its own slot's previous epilogue.
 __global__ void __launch_bounds__(kFThreads, 1)
     fast_trunk_kernel(const __grid_constant__ CUtensorMap w_map, const FastParams p) {
     extern __shared__ uint8_t smem_raw[];
@@ -139,14 +147,16 @@ __global__ void __launch_bounds__(kFThreads, 1)
     float *s_wv = s_wp + kFW;
 
     __shared__ uint64_t w_full[kFStages], w_empty[kFStages];
-    __shared__ uint64_t stage_full, half_done, acc_full, act_ready, epi_bar, mma_done;
+    __shared__ uint64_t stage_full[kFSlots], half_done[kFSlots], acc_full[kFSlots], act_ready[kFSlots];
+    __shared__ uint64_t epi_bar, mma_done;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    const int ngroups = (p.B + kFG - 1) / kFG;
+    const int ngroups = (p.B + kFSlots - 1) / kFSlots;
     const int nl = p.n3 + 1;
     const int nslices = 10 + 9 * p.n3;
+    const int G = gridDim.x;
     const uint32_t WL = p.wait_limit;
 
     if (tid == 0) {
@@ -154,10 +164,12 @@ __global__ void __launch_bounds__(kFThreads, 1)
             mbar_init(&w_full[i], 1);
             mbar_init(&w_empty[i], 1);
         }
-        mbar_init(&stage_full, kFEpiWarps);
-        mbar_init(&half_done, 1);
-        mbar_init(&acc_full, 1);
-        mbar_init(&act_ready, kFEpiWarps);
+        for (int i = 0; i < kFSlots; ++i) {
+            mbar_init(&stage_full[i], kFEpiWarps);
+            mbar_init(&half_done[i], 1);
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&act_ready[i], kFEpiWarps);
+        }
         mbar_init(&epi_bar, kFEpiWarps);
         mbar_init(&mma_done, 1);
         abort_flag = 0;
@@ -189,12 +201,22 @@ __global__ void __launch_bounds__(kFThreads, 1)
     auto aborted = [&]() { return *(volatile int *)&abort_flag != 0; };
 
     if (warp == 0) {
-        // ------------------------------------------------ weight slices
+        // ------------------------------------------------ weight slices, in
+        // the MMA thread's order: first layer (half, slot, tap), then per
+        // 3x3 layer (slot, tap)
         if (lane == 0) {
             uint32_t g = 0;
-            for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-                for (int s = 0; s < nslices; ++s, ++g) {
+            for (int grp = blockIdx.x; grp < ngroups; grp += G) {
+                for (int j = 0; j < kFSlots * nslices; ++j, ++g) {
                     if (aborted()) goto done_producer;
+                    int s;
+                    if (j < 10 * kFSlots) {
+                        const int h = j / (5 * kFSlots), dy = j % 5;
+                        s = h * 5 + dy;
+                    } else {
+                        const int r = j - 10 * kFSlots, l = r / (9 * kFSlots), tap = r % 9;
+                        s = 10 + 9 * l + tap;
+                    }
                     const int st = g % kFStages;
                     const uint32_t k = g / kFStages;
                     if (!mbar_wait(&w_empty[st], (k & 1) ^ 1, WL)) { fail(91); goto done_producer; }
@@ -208,51 +230,55 @@ __global__ void __launch_bounds__(kFThreads, 1)
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(128, kFW);
-            const uint64_t a_base = sdesc_sw128(smem_u32(buf));
             const uint64_t b_base = sdesc_sw128(smem_u32(wst));
-            uint32_t g = 0, n_stage = 0, n_act = 0;
-            for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+            uint32_t g = 0, n_stage[kFSlots] = {0, 0}, n_act[kFSlots] = {0, 0};
+            for (int grp = blockIdx.x; grp < ngroups; grp += G) {
                 // first layer: two 64-channel halves of the expanded rows
-                for (int h = 0; h < 2; ++h) {
-                    if (!mbar_wait(&stage_full, n_stage & 1, WL)) { fail(92); goto done_mma; }
-                    ++n_stage;
-                    tc_fence_after();
-                    for (int dy = 0; dy < 5; ++dy, ++g) {
-                        const int st = g % kFStages;
-                        const uint32_t k = g / kFStages;
-                        if (!mbar_wait(&w_full[st], k & 1, WL)) { fail(93); goto done_mma; }
+                for (int h = 0; h < 2; ++h)
+                    for (int sl = 0; sl < kFSlots; ++sl) {
+                        if (!mbar_wait(&stage_full[sl], n_stage[sl] & 1, WL)) { fail(92); goto done_mma; }
+                        ++n_stage[sl];
                         tc_fence_after();
-                        const uint64_t a0 = a_base + (uint64_t)((kFPre + kFPitch * (dy - 2)) * 8);
-                        const uint64_t b0 = b_base + (uint64_t)(st * (kFSlice >> 4));
-                        if (h == 0 && dy == 0)
-                            fast_slice<true>(tmem, a0, b0, idesc);
-                        else
-                            fast_slice<false>(tmem, a0, b0, idesc);
-                        mma_commit(&w_empty[st]);
+                        const uint64_t a_base = sdesc_sw128(smem_u32(buf + sl * kFBufBytes));
+                        const uint32_t tm = tmem + (uint32_t)(sl * kFTiles * kFW);
+                        for (int dy = 0; dy < 5; ++dy, ++g) {
+                            const int st = g % kFStages;
+                            const uint32_t k = g / kFStages;
+                            if (!mbar_wait(&w_full[st], k & 1, WL)) { fail(93); goto done_mma; }
+                            tc_fence_after();
+                            const uint64_t a0 = a_base + (uint64_t)((kFPre + kFPitch * (dy - 2)) * 8);
+                            const uint64_t b0 = b_base + (uint64_t)(st * (kFSlice >> 4));
+                            if (h == 0 && dy == 0)
+                                fast_slice<true>(tm, a0, b0, idesc);
+                            else
+                                fast_slice<false>(tm, a0, b0, idesc);
+                            mma_commit(&w_empty[st]);
+                        }
+                        mma_commit(h == 0 ? &half_done[sl] : &acc_full[sl]);
                     }
-                    if (h == 0) mma_commit(&half_done);
-                }
-                mma_commit(&acc_full);
-                for (int l = 1; l < nl; ++l) {
-                    if (!mbar_wait(&act_ready, n_act & 1, WL)) { fail(94); goto done_mma; }
-                    ++n_act;
-                    tc_fence_after();
-                    for (int tap = 0; tap < 9; ++tap, ++g) {
-                        const int st = g % kFStages;
-                        const uint32_t k = g / kFStages;
-                        if (!mbar_wait(&w_full[st], k & 1, WL)) { fail(95); goto done_mma; }
+                for (int l = 1; l < nl; ++l)
+                    for (int sl = 0; sl < kFSlots; ++sl) {
+                        if (!mbar_wait(&act_ready[sl], n_act[sl] & 1, WL)) { fail(94); goto done_mma; }
+                        ++n_act[sl];
                         tc_fence_after();
-                        const int shift = kFPitch * (tap / 3 - 1) + (tap % 3 - 1);
-                        const uint64_t a0 = a_base + (uint64_t)((kFPre + shift) * 8);
-                        const uint64_t b0 = b_base + (uint64_t)(st * (kFSlice >> 4));
-                        if (tap == 0)
-                            fast_slice<true>(tmem, a0, b0, idesc);
-                        else
-                            fast_slice<false>(tmem, a0, b0, idesc);
-                        mma_commit(&w_empty[st]);
+                        const uint64_t a_base = sdesc_sw128(smem_u32(buf + sl * kFBufBytes));
+                        const uint32_t tm = tmem + (uint32_t)(sl * kFTiles * kFW);
+                        for (int tap = 0; tap < 9; ++tap, ++g) {
+                            const int st = g % kFStages;
+                            const uint32_t k = g / kFStages;
+                            if (!mbar_wait(&w_full[st], k & 1, WL)) { fail(95); goto done_mma; }
+                            tc_fence_after();
+                            const int shift = kFPitch * (tap / 3 - 1) + (tap % 3 - 1);
+                            const uint64_t a0 = a_base + (uint64_t)((kFPre + shift) * 8);
+                            const uint64_t b0 = b_base + (uint64_t)(st * (kFSlice >> 4));
+                            if (tap == 0)
+                                fast_slice<true>(tm, a0, b0, idesc);
+                            else
+                                fast_slice<false>(tm, a0, b0, idesc);
+                            mma_commit(&w_empty[st]);
+                        }
+                        mma_commit(&acc_full[sl]);
                     }
-                    mma_commit(&acc_full);
-                }
             }
         done_mma:
             // every MMA this thread issued has completed before the CTA can
@@ -266,7 +292,8 @@ __global__ void __launch_bounds__(kFThreads, 1)
         const int qd = warp & 3;          // TMEM lane quarter this warp may read
         const int chh = (warp - 2) >> 2;  // channels 32*chh .. 32*chh + 31
         const int c_in = p.c_in;
-        uint32_t n_half = 0, n_acc = 0, n_epi = 0;
+        uint32_t n_half[kFSlots] = {0, 0}, n_acc[kFSlots] = {0, 0}, n_epi = 0;
+        auto boards = [&](int grp) { return min(kFSlots, p.B - grp * kFSlots); };
 
         // barrier of the 8 staging / epilogue warps (bounded)
         auto epi_sync = [&]() -> bool {
@@ -278,23 +305,40 @@ __global__ void __launch_bounds__(kFThreads, 1)
             return ok;
         };
         auto copy_planes = [&](int grp) {
-            const int nb = min(kFG, p.B - grp * kFG);
-            const uint8_t *src = p.planes + (size_t)grp * kFG * c_in * kPoints;
-            const int words = nb * c_in * kPoints / 4;
+            const uint8_t *src = p.planes + (size_t)grp * kFSlots * c_in * kPoints;
+            const int words = boards(grp) * c_in * kPoints / 4;
             for (int i = e; i < words; i += kFEpiThreads) cp_async4(pl + 4 * i, src + 4 * i);
             cp_async_commit();
         };
-        // Expanded first-layer rows, 64-channel half h, for every buffer row:
-        // channel dx * c_in + c = plane c at (y, x + dx - 2); zero rows off
-        // the boards.
-        auto stage = [&](int h, int nb) {
+        // per point of the group's boards: bit c = plane c (planes already in
+        // shared memory); the barriers order it against the staging that
+        // reads the masks and the copy that overwrites the planes
+        auto build_masks = [&](int grp) -> bool {
+            cp_async_wait0();
+            if (!epi_sync()) return false;
+            const int nb = boards(grp);
+            for (int i = e; i < nb * kPoints; i += kFEpiThreads) {
+                const int b = i / kPoints, pt = i - b * kPoints;
+                const uint8_t *src = pl + (size_t)b * c_in * kPoints + pt;
+                uint32_t m = 0;
+                for (int c = 0; c < c_in; ++c) m |= (uint32_t)(src[c * kPoints] & 1) << c;
+                mask[i] = m;
+            }
+            return epi_sync();
+        };
+        // Expanded first-layer rows of slot sl, 64-channel half h, for every
+        // buffer row: channel dx * c_in + c = plane c at (y, x + dx - 2);
+        // zero rows off the board (and for a slot without a board).
+        auto stage = [&](int sl, int h, int nb) {
+            uint8_t *sbuf = buf + sl * kFBufBytes;
+            const uint32_t *mb = mask + sl * kPoints;
             for (int R = e; R < kFBufRows; R += kFEpiThreads) {
                 const int q = R - kFPre;
                 uint64_t lo = 0, hi = 0;
-                if (q >= 0) {
-                    const int b = q / kFRowsB, r = q - b * kFRowsB, y = r / kFPitch, x = r - y * kFPitch;
-                    if (b < nb && y < kBoard && x < kBoard) {
-                        const uint32_t *m = mask + b * kPoints + y * kBoard;
+                if (sl < nb && q >= 0 && q < kFRowsB) {
+                    const int y = q / kFPitch, x = q - y * kFPitch;
+                    if (y < kBoard && x < kBoard) {
+                        const uint32_t *m = mb + y * kBoard;
 #pragma unroll
                         for (int dx = 0; dx < 5; ++dx) {
                             const int xx = x + dx - 2;
@@ -310,104 +354,126 @@ __global__ void __launch_bounds__(kFThreads, 1)
                     }
                 }
                 const uint64_t half = h ? hi : lo;
-                uint8_t *row = buf + R * 128;
+                uint8_t *row = sbuf + R * 128;
 #pragma unroll
                 for (int j = 0; j < 8; ++j)
                     *reinterpret_cast<uint4 *>(row + ((j ^ (R & 7)) << 4)) = lut[(half >> (8 * j)) & 0xFF];
             }
         };
-
-        if ((int)blockIdx.x < ngroups) copy_planes(blockIdx.x);
-        for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-            const int nb = min(kFG, p.B - grp * kFG);
-            cp_async_wait0();
-            if (!epi_sync()) break;
-            // per point: bit c = plane c
-            for (int i = e; i < nb * kPoints; i += kFEpiThreads) {
-                const int b = i / kPoints, pt = i - b * kPoints;
-                const uint8_t *src = pl + (size_t)b * c_in * kPoints + pt;
-                uint32_t m = 0;
-                for (int c = 0; c < c_in; ++c) m |= (uint32_t)(src[c * kPoints] & 1) << c;
-                mask[i] = m;
+        auto stage_done = [&](int sl) {
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&stage_full[sl]);
+        };
+        // both halves of group grp's first-layer rows, slot by slot, each
+        // second half once that slot's first-half MMAs have completed
+        auto stage_second_halves = [&](int grp) -> bool {
+            for (int sl = 0; sl < kFSlots; ++sl) {
+                if (!mbar_wait(&half_done[sl], n_half[sl] & 1, WL)) { fail(97); return false; }
+                ++n_half[sl];
+                stage(sl, 1, boards(grp));
+                stage_done(sl);
             }
-            if (!epi_sync()) break;
-            if (grp + (int)gridDim.x < ngroups) copy_planes(grp + gridDim.x);
+            return true;
+        };
 
-            stage(0, nb);
-            fence_proxy_async();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&stage_full);
-            if (!mbar_wait(&half_done, n_half & 1, WL)) { fail(97); break; }
-            ++n_half;
-            stage(1, nb);
-            fence_proxy_async();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&stage_full);
-
-            // which of this thread's 7 rows (one per tile) are board points,
-            // and for those the point's index in the batch
+        const int g0 = blockIdx.x;
+        if (g0 < ngroups) {
+            copy_planes(g0);
+            if (!build_masks(g0)) goto done_epi;
+            if (g0 + G < ngroups) copy_planes(g0 + G);
+            for (int sl = 0; sl < kFSlots; ++sl) {
+                stage(sl, 0, boards(g0));
+                stage_done(sl);
+            }
+            if (!stage_second_halves(g0)) goto done_epi;
+            if (g0 + G < ngroups) {
+                if (!build_masks(g0 + G)) goto done_epi;
+                if (g0 + 2 * G < ngroups) copy_planes(g0 + 2 * G);
+            }
+        }
+        for (int grp = g0; grp < ngroups; grp += G) {
+            const int nb = boards(grp);
+            const int nxt = grp + G;
+            const bool has_next = nxt < ngroups;
+            // which of this thread's rows (one per tile) are board points
             uint32_t vmask = 0;
 #pragma unroll
             for (int t = 0; t < kFTiles; ++t) {
                 const int q = 128 * t + 32 * qd + lane;
-                const int b = q / kFRowsB, r = q - b * kFRowsB, y = r / kFPitch, x = r - y * kFPitch;
-                if (b < nb && y < kBoard && x < kBoard) vmask |= 1u << t;
+                const int y = q / kFPitch, x = q - y * kFPitch;
+                if (q < kFRowsB && y < kBoard && x < kBoard) vmask |= 1u << t;
             }
             for (int l = 0; l < nl; ++l) {
-                if (!mbar_wait(&acc_full, n_acc & 1, WL)) { fail(98); goto done_epi; }
-                ++n_acc;
-                tc_fence_after();
                 const bool last = l == nl - 1;
                 const float *bias = s_bias + l * kFW + chh * 32;
-                const uint32_t t_row = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(32 * chh);
-                // two tiles per TMEM round trip
+                for (int sl = 0; sl < kFSlots; ++sl) {
+                    if (!mbar_wait(&acc_full[sl], n_acc[sl] & 1, WL)) { fail(98); goto done_epi; }
+                    ++n_acc[sl];
+                    tc_fence_after();
+                    const uint32_t vm = sl < nb ? vmask : 0u;
+                    const uint32_t t_row = tmem + ((uint32_t)(32 * qd) << 16) +
+                                           (uint32_t)(sl * kFTiles * kFW + 32 * chh);
+                    uint8_t *sbuf = buf + sl * kFBufBytes;
 #pragma unroll
-                for (int t0 = 0; t0 < kFTiles; t0 += 2) {
-                    constexpr int kPair = 2;
-                    const int nt = (t0 + 1 < kFTiles) ? kPair : 1;
-                    uint32_t v[kPair][32];
-                    tmem_ld32(t_row + (uint32_t)(kFW * t0), v[0]);
-                    if (nt == 2) tmem_ld32(t_row + (uint32_t)(kFW * (t0 + 1)), v[1]);
-                    tmem_ld_wait();
+                    for (int t0 = 0; t0 < kFTiles; t0 += 2) {
+                        uint32_t v[2][32];
+                        tmem_ld32(t_row + (uint32_t)(kFW * t0), v[0]);
+                        tmem_ld32(t_row + (uint32_t)(kFW * (t0 + 1)), v[1]);
+                        tmem_ld_wait();
 #pragma unroll
-                    for (int u = 0; u < nt; ++u) {
-                        const int q = 128 * (t0 + u) + 32 * qd + lane;
-                        const bool valid = (vmask >> (t0 + u)) & 1u;
-                        if (!last) {
-                            uint32_t w[16];
+                        for (int u = 0; u < 2; ++u) {
+                            const int q = 128 * (t0 + u) + 32 * qd + lane;
+                            const bool valid = (vm >> (t0 + u)) & 1u;
+                            if (!last) {
+                                uint32_t w[16];
 #pragma unroll
-                            for (int i = 0; i < 16; ++i)
-                                w[i] = valid ? relu_bf16x2(__uint_as_float(v[u][2 * i]) + bias[2 * i],
-                                                           __uint_as_float(v[u][2 * i + 1]) + bias[2 * i + 1])
-                                             : 0u;
-                            const int R = q + kFPre;
-                            uint8_t *row = buf + R * 128;
+                                for (int i = 0; i < 16; ++i)
+                                    w[i] = valid ? relu_bf16x2(__uint_as_float(v[u][2 * i]) + bias[2 * i],
+                                                               __uint_as_float(v[u][2 * i + 1]) + bias[2 * i + 1])
+                                                 : 0u;
+                                const int R = q + kFPre;
+                                uint8_t *row = sbuf + R * 128;
 #pragma unroll
-                            for (int k = 0; k < 4; ++k)
-                                *reinterpret_cast<uint4 *>(row + (((4 * chh + k) ^ (R & 7)) << 4)) =
-                                    make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
-                        } else {
-                            float sp = 0.0f, sv = 0.0f;
+                                for (int k = 0; k < 4; ++k)
+                                    *reinterpret_cast<uint4 *>(row + (((4 * chh + k) ^ (R & 7)) << 4)) =
+                                        make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+                            } else {
+                                float sp = 0.0f, sv = 0.0f;
 #pragma unroll
-                            for (int i = 0; i < 32; ++i) {
-                                const float f = fmaxf(__uint_as_float(v[u][i]) + bias[i], 0.0f);
-                                sp = fmaf(f, s_wp[32 * chh + i], sp);
-                                sv = fmaf(f, s_wv[32 * chh + i], sv);
-                            }
-                            if (valid) {
-                                const int b = q / kFRowsB, r = q - b * kFRowsB, y = r / kFPitch, x = r - y * kFPitch;
-                                const size_t idx = (size_t)(grp * kFG + b) * kPoints + y * kBoard + x;
-                                p.parts_p[chh * p.part_stride + idx] = sp;
-                                p.parts_v[chh * p.part_stride + idx] = sv;
+                                for (int i = 0; i < 32; ++i) {
+                                    const float f = fmaxf(__uint_as_float(v[u][i]) + bias[i], 0.0f);
+                                    sp = fmaf(f, s_wp[32 * chh + i], sp);
+                                    sv = fmaf(f, s_wv[32 * chh + i], sv);
+                                }
+                                if (valid) {
+                                    const int y = q / kFPitch, x = q - y * kFPitch;
+                                    const size_t idx = (size_t)(grp * kFSlots + sl) * kPoints + y * kBoard + x;
+                                    p.parts_p[chh * p.part_stride + idx] = sp;
+                                    p.parts_v[chh * p.part_stride + idx] = sv;
+                                }
                             }
                         }
                     }
+                    tc_fence_before();
+                    if (!last) {
+                        fence_proxy_async();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&act_ready[sl]);
+                    } else if (has_next) {
+                        // this slot's buffer and accumulators are free: the
+                        // next group's first half goes in while the tensor
+                        // core finishes the other slot
+                        stage(sl, 0, boards(nxt));
+                        stage_done(sl);
+                    }
                 }
-                tc_fence_before();
-                if (!last) {
-                    fence_proxy_async();
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(&act_ready);
+            }
+            if (has_next) {
+                if (!stage_second_halves(nxt)) goto done_epi;
+                if (nxt + G < ngroups) {
+                    if (!build_masks(nxt + G)) goto done_epi;
+                    if (nxt + 2 * G < ngroups) copy_planes(nxt + 2 * G);
                 }
             }
         }
@@ -670,7 +736,7 @@ int fast_forward(lg_fast *f, const uint8_t *planes, int B, float T, float *probs
     p.parts_v = f->parts + 2 * p.part_stride;
     p.err = f->err;
     p.wait_limit = kFWaitLimit;
-    const int groups = (B + kFG - 1) / kFG;
+    const int groups = (B + kFSlots - 1) / kFSlots;
     const int grid = groups < f->sm_count ? groups : f->sm_count;
     fast_trunk_kernel<<<grid, kFThreads, kFSmem, s>>>(f->w_map, p);
     HeadIn hp{p.parts_p, 2, p.part_stride, f->bp, 0, LG_ACT_RELU, logits};

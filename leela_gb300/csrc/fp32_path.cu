@@ -277,8 +277,8 @@ __global__ void __launch_bounds__(384) softmax_kernel(const HeadIn h, int B, flo
 // fixed order plus b1, applies the activation, reduces w2 . hidden over the
 // block in a fixed order, adds b2 and applies the value map.  The split does
 // not depend on B, so a board's value does not depend on its batch.
-constexpr int kFcBoards = 32, kFcUnits = 64, kFcSplit = 4;
-constexpr int kFcK = (kPoints + kFcSplit - 1) / kFcSplit;  // 91
+constexpr int kFcBoards = 32, kFcUnits = 64, kFcSplit = 8;
+constexpr int kFcK = (kPoints + kFcSplit - 1) / kFcSplit;  // 46
 constexpr int kFcXPitch = 36;  // floats; rows 16-byte aligned, 4-way store conflicts at most
 
 __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
     const int k0 = ks * kFcK, nk = min(kPoints, k0 + kFcK) - k0;
     // W1 slice rows k0 .. k0+nk-1: contiguous, float4 loads
     const float4 *wsrc = reinterpret_cast<const float4 *>(w1s + ((size_t)slice * kPoints + k0) * kFcUnits);
-    constexpr int kWPer = (kFcK * kFcUnits / 4 + 255) / 256;  // 6
+    constexpr int kWPer = (kFcK * kFcUnits / 4 + 255) / 256;  // 3
     float4 wv[kWPer];
 #pragma unroll
     for (int j = 0; j < kWPer; ++j) {
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(256) value_fc1_kernel(const HeadIn h, int B,
     }
     // head outputs, read along k for each board: every load of the thread is
     // issued before the first store, so the loop waits out one round trip
-    constexpr int kPer = (kFcBoards * kFcK + 255) / 256;  // 12
+    constexpr int kPer = (kFcBoards * kFcK + 255) / 256;  // 6
     float xv[kPer];
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {

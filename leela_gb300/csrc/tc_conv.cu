@@ -1300,12 +1300,67 @@ __global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__re
     } else {
         for (int i = threadIdx.x; i < nbytes; i += blockDim.x) sp[i] = src[i];
     }
-    __syncthreads();
     const int groups = halves * 8;
     __nv_bfloat16 *dst = out + (size_t)b * kL5Board * groups * 8;
     const bool aligned = (C % 8) == 0;  // then a group of 8 channels shares one dx
     const int per = (kL5Board * groups + gridDim.y - 1) / gridDim.y;
     const int i0 = blockIdx.y * per, i1 = min(kL5Board * groups, i0 + per);
+    if (aligned && C <= 32) {
+        // Per point a bit mask of its C planes, and a table from 8 bits to
+        // 8 values 0 / 1 in the operand type: a 16-byte group of a row is
+        // then one mask load, one shift and one table load.  Boards whose
+        // planes hold other byte values take the byte-by-byte path below.
+        __shared__ uint32_t mask[kPoints];
+        __shared__ uint4 lut[256];
+        const uint32_t one = f16 ? 0x3C00u : 0x3F80u;
+        {
+            const int t = threadIdx.x;
+            uint32_t w[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                w[k] = (((t >> (2 * k)) & 1) ? one : 0u) | (((t >> (2 * k + 1)) & 1) ? (one << 16) : 0u);
+            lut[t] = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        __syncthreads();
+        uint32_t other = 0;
+        for (int pt = threadIdx.x; pt < kPoints; pt += blockDim.x) {
+            uint32_t m = 0;
+            for (int c = 0; c < C; ++c) {
+                const uint32_t v = sp[c * kPoints + pt];
+                m |= (v & 1u) << c;
+                other |= v > 1u;
+            }
+            mask[pt] = m;
+        }
+        if (!__syncthreads_or((int)other)) {
+            for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+                const int r = i / groups, g = i - (i / groups) * groups;
+                const int y = r / kL5Pitch, x = r - y * kL5Pitch;
+                const int ch0 = g * 8;
+                const int dx = ch0 / C, c0 = ch0 - dx * C;
+                const int sx = x + dx - 2;
+                const bool in = y < kBoard && ch0 < 5 * C && sx >= 0 && sx < kBoard;
+                const uint32_t bits = in ? (mask[y * kBoard + sx] >> c0) & 0xFFu : 0u;
+                *reinterpret_cast<uint4 *>(dst + (size_t)i * 8) = lut[bits];
+            }
+        } else {
+            for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+                const int r = i / groups, g = i % groups;
+                const int y = r / kL5Pitch, x = r % kL5Pitch;
+                const int ch0 = g * 8;
+                const int dx = ch0 / C, c0 = ch0 - dx * C;
+                const int sx = x + dx - 2;
+                const bool in = y < kBoard && ch0 < 5 * C && sx >= 0 && sx < kBoard;
+                const uint8_t *col = sp + c0 * kPoints + y * kBoard + sx;
+                __align__(16) uint16_t v[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) v[j] = round16(in ? (float)col[j * kPoints] : 0.0f, f16);
+                *reinterpret_cast<uint4 *>(dst + (size_t)i * 8) = *reinterpret_cast<const uint4 *>(v);
+            }
+        }
+        return;
+    }
+    __syncthreads();
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const int r = i / groups, g = i % groups;
         const int y = r / kL5Pitch, x = r % kL5Pitch;
