@@ -20,12 +20,12 @@ import subprocess
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("LEELA_REF") or "/root/reference"
+REF = os.environ.get("LEELA_REF")
 
 
 @pytest.fixture(scope="module")
 def driver():
-    if not os.path.isdir(REF) or not os.path.exists(os.path.join(REF, "UCTSearch.cpp")):
+    if not REF or not os.path.isdir(REF) or not os.path.exists(os.path.join(REF, "UCTSearch.cpp")):
         pytest.skip("reference sources not present (set LEELA_REF)")
     if not shutil.which("g++"):
         pytest.skip("no g++")
