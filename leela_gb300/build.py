@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libleela_gb300.so")
 SOURCES = ["lg_api.cu", "fp32_path.cu", "tc_conv.cu", "distill.cu", "ensemble.cu", "weights_io.cu", "gather.cu",
-           "latency.cu", "fast_net.cu"]
+           "latency.cu", "fast_net.cu", "finish.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
          "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]

@@ -603,6 +603,7 @@ struct lg_fast {
     float b2 = 0.0f;
     float *parts = nullptr;      // [4][max_batch * 361]: policy halves, value halves
     float *fcpart = nullptr;
+    int *fccnt = nullptr;        // value-head group counters, zero between launches
     float *entropy = nullptr;    // [max_batch]
     int *err = nullptr;
     CUtensorMap w_map{};
@@ -742,8 +743,8 @@ int fast_forward(lg_fast *f, const uint8_t *planes, int B, float T, float *probs
     HeadIn hp{p.parts_p, 2, p.part_stride, f->bp, 0, LG_ACT_RELU, logits};
     launch_softmax(hp, B, T, probs, s, entropy ? entropy : f->entropy);
     HeadIn hv{p.parts_v, 2, p.part_stride, f->bv, 0, LG_ACT_RELU, nullptr};
-    launch_value_fc(hv, B, f->w1s, f->b1, f->w2, f->b2, f->H, LG_ACT_RELU, 0, value, f->fcpart, s);
-    *nlaunch = 4;
+    launch_value_fc(hv, B, f->w1s, f->b1, f->w2, f->b2, f->H, LG_ACT_RELU, 0, value, f->fcpart, f->fccnt, s);
+    *nlaunch = 3;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         lg_set_error("lg_fast: launch failed: %s", cudaGetErrorString(e));
@@ -846,6 +847,9 @@ extern "C" LG_API int lg_fast_create(int device, int c_in, int n3x3, int fc_hidd
     if (!rc) rc = fast_alloc(f, &f->w2, fc_hidden);
     if (!rc) rc = fast_alloc(f, &f->parts, 4 * (size_t)max_batch * kPoints);
     if (!rc) rc = fast_alloc(f, &f->fcpart, value_fc_part_floats(max_batch, fc_hidden));
+    if (!rc) rc = fast_alloc(f, &f->fccnt, value_fc_counter_ints(max_batch, fc_hidden));
+    if (!rc && cudaMemset(f->fccnt, 0, sizeof(int) * value_fc_counter_ints(max_batch, fc_hidden)) != cudaSuccess)
+        rc = LG_ERR_CUDA;
     if (!rc) rc = fast_alloc(f, &f->entropy, max_batch);
     if (!rc) rc = fast_alloc(f, &f->err, 1);
     if (!rc && cudaMemset(f->err, 0, sizeof(int)) != cudaSuccess) rc = LG_ERR_CUDA;

@@ -137,6 +137,7 @@ struct lg_ctx {
     float *d_logits = nullptr, *d_probs = nullptr, *d_value = nullptr;
     float *d_parts = nullptr;  // fused-head partial sums, [4][max_batch * 361]
     float *d_fcpart = nullptr; // value-head FC partial sums
+    int *d_fccnt = nullptr;    // value-head group counters, zero between launches
     int *d_flags = nullptr;    // chunk flags and item counter of the persistent trunk kernel
     // pinned staging of the blocking calls, two slots so that chunk k+1 is
     // packed while chunk k runs: planes, outputs, logits, completion events
@@ -648,9 +649,9 @@ int forward_fp32(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float
             launch_softmax(h, B, T, probs, s);
         else
             launch_value_fc(h, B, n.w1s, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
-                            c->d_fcpart, s);
+                            c->d_fcpart, c->d_fccnt, s);
     }
-    L += d.value_head ? 2 : 1;
+    ++L;
     *nlaunch = L;
     return LG_OK;
 }
@@ -666,9 +667,12 @@ bool trunk_fusable(const Net &n) {
            n.tc[0].cout == 128;
 }
 
+// next (optional): the following batch's planes, packed into c->l5 by the
+// CTAs of this batch's finish launch (the trunk has read c->l5 by then).
 int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
                float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof,
-               bool l5_ready = false, const int *count = nullptr, int count_base = 0) {
+               bool l5_ready = false, const int *count = nullptr, int count_base = 0,
+               const PackJob *next = nullptr) {
     if (!count && use_lat(c, n, B) && !l5_ready)
         return forward_lat(c, n, planes, B, T, probs, logits_out, value, s, nlaunch, prof);
     if (count && !trunk_fusable(n)) {
@@ -731,7 +735,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
                 rc = launch_tc_trunk(tt, c->d_parts, part_stride, c->d_flags, c->d_err, s, c->sm_count);
             }
             if (rc) return rc;
-            L += 2;
+            L += 1;
             break;
         }
         TcLayer tl{};
@@ -762,24 +766,43 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
         ProfScope ps(c, prof, LG_PROF_TAIL, s);
         HeadIn h{c->d_parts, tc_head_parts(d.width, use_trunk ? 0 : var3), part_stride, n.head_b, d.act_head,
                  d.act, lg, count, count_base};
-        if (!d.value_head)
+        if (next) {
+            FinishJob j{};
+            j.h = h;
+            j.B = B;
+            j.value_head = d.value_head;
+            j.temperature = T;
+            j.probs = probs;
+            j.w1s = n.w1s;
+            j.b1 = n.b1;
+            j.w2 = n.w2;
+            j.b2 = n.b2;
+            j.H = d.fc_hidden;
+            j.act = d.act;
+            j.value_map = d.value_map;
+            j.value = value;
+            j.part = c->d_fcpart;
+            j.cnt = c->d_fccnt;
+            launch_finish_pack(j, *next, s);
+        } else if (!d.value_head) {
             launch_softmax(h, B, T, probs, s);
-        else
+        } else {
             launch_value_fc(h, B, n.w1s, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
-                            c->d_fcpart, s);
+                            c->d_fcpart, c->d_fccnt, s);
+        }
     }
-    L += d.value_head ? 2 : 1;
+    ++L;
     *nlaunch = L;
     return LG_OK;
 }
 
 int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
             float *logits, float *value, cudaStream_t s, int *nlaunch, bool prof = false,
-            bool l5_ready = false) {
+            bool l5_ready = false, const PackJob *next = nullptr) {
     Net &n = c->nets[net];
     if (n.d.precision == LG_FP32)
         return forward_fp32(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof);
-    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof, l5_ready);
+    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof, l5_ready, nullptr, 0, next);
 }
 
 // Host call: chunks of up to max_batch positions go through a cached CUDA
@@ -959,13 +982,31 @@ int run_device(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float 
     if (rc) return rc;
     cudaSetDevice(c->device);
     size_t per_in = (size_t)n.d.c_in * kPoints;
+    // Tensor-core nets: the finish launch of chunk k also packs chunk k+1's
+    // planes (when neither chunk runs on the small-batch kernel), so a chunk
+    // costs a trunk launch and a finish launch.
+    const bool tc = n.d.precision != LG_FP32;
+    bool l5_ready = false;
     for (int b0 = 0; b0 < B; b0 += c->max_batch) {
         int nb = std::min(c->max_batch, B - b0);
+        const int nb1 = std::min(c->max_batch, B - b0 - nb);
+        PackJob pk{};
+        const PackJob *next = nullptr;
+        if (tc && nb1 > 0 && (l5_ready || !use_lat(c, n, nb)) && !use_lat(c, n, nb1)) {
+            pk.planes = planes + (size_t)(b0 + nb) * per_in;
+            pk.B = nb1;
+            pk.C = n.d.c_in;
+            pk.halves = n.tc[0].halves;
+            pk.f16 = n.d.precision == LG_FP16 ? 1 : 0;
+            pk.out = c->l5;
+            next = &pk;
+        }
         int nl = 0;
         rc = forward(c, net, planes + (size_t)b0 * per_in, nb, T,
                      probs ? probs + (size_t)b0 * kPoints : nullptr,
                      logits ? logits + (size_t)b0 * kPoints : nullptr, value ? value + b0 : nullptr,
-                     s, &nl, c->profiling);
+                     s, &nl, c->profiling, l5_ready, next);
+        l5_ready = next != nullptr;
         if (rc) return rc;
         c->launches += nl;
         cudaError_t e = cudaGetLastError();
@@ -1290,9 +1331,15 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
         (rc = dev_alloc(c, &c->d_value, mb)) || (rc = dev_alloc(c, &c->d_err, 1)) ||
         (rc = dev_alloc(c, &c->d_parts, 4 * mb * kPoints)) ||
         (rc = dev_alloc(c, &c->d_fcpart, value_fc_part_floats(max_batch, std::max(max_fc, 1)))) ||
-        (rc = dev_alloc(c, &c->d_flags, std::max<size_t>(1024, trunk_flag_ints(max_batch * kL3Board, max_batch * kL5Board)))))
+        (rc = dev_alloc(c, &c->d_fccnt, value_fc_counter_ints(max_batch, std::max(max_fc, 1)))) ||
+        (rc = dev_alloc(c, &c->d_flags, trunk_flag_ints(max_batch * kL3Board, max_batch * kL5Board))))
         return fail(rc);
-    if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) return fail(LG_ERR_CUDA);
+    // the counters and flags start at zero; every launch leaves them so
+    if (cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess ||
+        cudaMemset(c->d_fccnt, 0, sizeof(int) * value_fc_counter_ints(max_batch, std::max(max_fc, 1))) != cudaSuccess ||
+        cudaMemset(c->d_flags, 0, sizeof(int) * trunk_flag_ints(max_batch * kL3Board, max_batch * kL5Board)) !=
+            cudaSuccess)
+        return fail(LG_ERR_CUDA);
     if (cudaMallocHost(&c->h_planes, mb * max_c_in * kPoints) != cudaSuccess ||
         cudaMallocHost(&c->h_out, mb * kPoints * sizeof(float)) != cudaSuccess ||
         cudaMallocHost(&c->h_out2, mb * kPoints * sizeof(float)) != cudaSuccess ||

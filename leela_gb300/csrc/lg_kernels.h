@@ -3,9 +3,24 @@
 #include "../../include/leela_gpu.h"
 #include "lg_common.cuh"
 
+#include <cuda_fp16.h>
+
 #include <mutex>
 
 namespace lg {
+
+__device__ __forceinline__ float act_fn(float v, int act) {
+    // ELU exactly as the reference writes it: x > 0 ? x : exp(x) - 1.
+    if (act == LG_ACT_ELU) return (v > 0.0f) ? v : (expf(v) - 1.0f);
+    if (act == LG_ACT_RELU) return (v > 0.0f) ? v : 0.0f;
+    return v;  // any other code: identity (used by the training kernels)
+}
+
+// One value rounded to nearest even in the operand type (FP16 when f16, else
+// BF16), as its 16 bits.
+__device__ __forceinline__ uint16_t round16(float v, bool f16) {
+    return f16 ? __half_as_ushort(__float2half_rn(v)) : __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
 
 // ------------------------------------------------------------ FP32 path
 int conv_f32_splits(int M, int O, int C, int k);
@@ -35,15 +50,41 @@ struct HeadIn {
 // entropy (optional): -sum p ln p of each board's probabilities, in nats.
 void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s,
                     float *entropy = nullptr);
-// Value head: two launches (tiled split-K FC1 pre-activations, then a
-// fixed-order sum, b1, activation, FC2 and the value map); `part` holds
-// value_fc_part_floats(B, H) floats.  w1s is W1 sliced by
+// Value head, one launch (tiled split-K FC1 pre-activations; the CTAs that
+// finish last add them in a fixed order and run b1, the activation, FC2 and
+// the value map); `part` holds value_fc_part_floats(B, H) floats, `cnt`
+// value_fc_counter_ints(B, H) ints that are zero before the first launch
+// (each launch leaves them zero).  w1s is W1 sliced by
 // value_fc_slice_units() hidden units: [ceil(H/64)][361][64], zero-padded.
 void launch_value_fc(const HeadIn &h, int B, const float *w1s, const float *b1, const float *w2,
-                     float b2, int H, int act, int value_map, float *value, float *part,
+                     float b2, int H, int act, int value_map, float *value, float *part, int *cnt,
                      cudaStream_t s);
 size_t value_fc_part_floats(int B, int H);
+size_t value_fc_counter_ints(int B, int H);
 int value_fc_slice_units();
+
+// The finish of one batch (softmax, or the value head as launch_value_fc)
+// and the packing of the next batch's planes into the L5 rows
+// (launch_pack_planes_l5's output) in one launch; the two touch disjoint
+// memory.
+struct FinishJob {
+    HeadIn h;
+    int B;
+    int value_head;
+    float temperature;  // policy
+    float *probs, *entropy;
+    const float *w1s, *b1, *w2;  // value
+    float b2;
+    int H, act, value_map;
+    float *value, *part;
+    int *cnt;
+};
+struct PackJob {
+    const uint8_t *planes;  // [B][C][361]
+    int B, C, halves, f16;
+    __nv_bfloat16 *out;
+};
+void launch_finish_pack(const FinishJob &j, const PackJob &pk, cudaStream_t s);
 
 // ------------------------------------------------- tensor-core (tcgen05) path
 //
@@ -125,7 +166,8 @@ struct TcTrunk {
     const int *count = nullptr;
     int count_base = 0;
 };
-// flags: trunk_flag_ints(rows, rows5) ints of device scratch (reset by the launch).
+// flags: trunk_flag_ints(rows, rows5) ints of device scratch, zero before the first
+// launch; the launch's last CTA leaves them zero again (no memset between launches).
 int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
                     cudaStream_t s, int sm_count);
 size_t trunk_flag_ints(int rows, int rows5);

@@ -79,11 +79,6 @@ __device__ __forceinline__ uint32_t pack_relu_f16x2(float lo, float hi) {
     return d;
 }
 
-// One value rounded to nearest even in the operand type (FP16 when f16, else
-// BF16), as its 16 bits.
-__device__ __forceinline__ uint16_t round16(float v, bool f16) {
-    return f16 ? __half_as_ushort(__float2half_rn(v)) : __bfloat16_as_ushort(__float2bfloat16_rn(v));
-}
 
 // Two fused multiply-adds in one packed FP32 instruction (fma.rn.f32x2,
 // sm_100 family): d_i = a_i * b + c, each rounded as fmaf.
@@ -683,7 +678,8 @@ struct TrunkParams {
     int nl;               // 3x3 layers
     float *parts;
     size_t part_stride;
-    int *flags;           // [n3] chunk flags, the item counter, [n5] first-layer chunk flags
+    int *flags;           // [n3] chunk flags, the item counter, [n5] first-layer chunk flags, the
+                          // exit counter: zero at entry, and the last CTA to leave zeroes them
     int *err;
     uint32_t wait_limit;  // polls of one mbarrier wait before it gives up
     uint32_t poll_limit;  // polls of one dependency flag before it gives up
@@ -1259,142 +1255,23 @@ __global__ void __maxnreg__(96)
     tc_fence_after();
     if (warp == 1) tmem_dealloc(tmem, 512);
     if (warp == 1) tmem_relinquish();
-}
-#undef WAIT_LIM
-
-// ------------------------------------------------------------------ packing
-
-// planes [B][C][361] bytes -> L5 rows [B*399][halves*64] BF16, channel
-// dx*C + c = plane c at (y, x + dx - 2); zero rows y = 19, 20 and zero
-// channels >= 5C.  One CTA per board: the board's planes are staged in
-// shared memory, then every 16-byte group of every row is written once.
-constexpr int kPackMaxC = 64;
-__global__ void __launch_bounds__(256) pack_planes_l5_kernel(const uint8_t *__restrict__ planes, int B,
-                                                             int C, int halves, int f16,
-                                                             __nv_bfloat16 *__restrict__ out,
-                                                             const int *__restrict__ count, int count_base) {
-    __shared__ __align__(16) uint8_t sp[kPackMaxC * kPoints];
-    const int b = blockIdx.x;
-    if (b >= B || (count && b >= *count - count_base)) return;
-    const uint8_t *src = planes + (size_t)b * C * kPoints;
-    const int nbytes = C * kPoints;
-    if (((uintptr_t)src & 7) == 0) {
-        // 8-byte words, four loads in flight per thread before the stores
-        const int n8 = nbytes / 8;
-        const uint2 *s8 = reinterpret_cast<const uint2 *>(src);
-        uint2 *d8 = reinterpret_cast<uint2 *>(sp);
-        for (int base = 0; base < n8; base += 4 * 256) {
-            uint2 r[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int i = base + j * 256 + (int)threadIdx.x;
-                if (i < n8) r[j] = s8[i];
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int i = base + j * 256 + (int)threadIdx.x;
-                if (i < n8) d8[i] = r[j];
-            }
-        }
-        for (int i = n8 * 8 + threadIdx.x; i < nbytes; i += blockDim.x) sp[i] = src[i];
-    } else {
-        for (int i = threadIdx.x; i < nbytes; i += blockDim.x) sp[i] = src[i];
-    }
-    const int groups = halves * 8;
-    __nv_bfloat16 *dst = out + (size_t)b * kL5Board * groups * 8;
-    const bool aligned = (C % 8) == 0;  // then a group of 8 channels shares one dx
-    const int per = (kL5Board * groups + gridDim.y - 1) / gridDim.y;
-    const int i0 = blockIdx.y * per, i1 = min(kL5Board * groups, i0 + per);
-    if (aligned && C <= 32) {
-        // Per point a bit mask of its C planes, and a table from 8 bits to
-        // 8 values 0 / 1 in the operand type: a 16-byte group of a row is
-        // then one mask load, one shift and one table load.  Boards whose
-        // planes hold other byte values take the byte-by-byte path below.
-        __shared__ uint32_t mask[kPoints];
-        __shared__ uint4 lut[256];
-        const uint32_t one = f16 ? 0x3C00u : 0x3F80u;
-        {
-            const int t = threadIdx.x;
-            uint32_t w[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                w[k] = (((t >> (2 * k)) & 1) ? one : 0u) | (((t >> (2 * k + 1)) & 1) ? (one << 16) : 0u);
-            lut[t] = make_uint4(w[0], w[1], w[2], w[3]);
-        }
-        __syncthreads();
-        uint32_t other = 0;
-        for (int pt = threadIdx.x; pt < kPoints; pt += blockDim.x) {
-            uint32_t m = 0;
-            for (int c = 0; c < C; ++c) {
-                const uint32_t v = sp[c * kPoints + pt];
-                m |= (v & 1u) << c;
-                other |= v > 1u;
-            }
-            mask[pt] = m;
-        }
-        if (!__syncthreads_or((int)other)) {
-            for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-                const int r = i / groups, g = i - (i / groups) * groups;
-                const int y = r / kL5Pitch, x = r - y * kL5Pitch;
-                const int ch0 = g * 8;
-                const int dx = ch0 / C, c0 = ch0 - dx * C;
-                const int sx = x + dx - 2;
-                const bool in = y < kBoard && ch0 < 5 * C && sx >= 0 && sx < kBoard;
-                const uint32_t bits = in ? (mask[y * kBoard + sx] >> c0) & 0xFFu : 0u;
-                *reinterpret_cast<uint4 *>(dst + (size_t)i * 8) = lut[bits];
-            }
-        } else {
-            for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-                const int r = i / groups, g = i % groups;
-                const int y = r / kL5Pitch, x = r % kL5Pitch;
-                const int ch0 = g * 8;
-                const int dx = ch0 / C, c0 = ch0 - dx * C;
-                const int sx = x + dx - 2;
-                const bool in = y < kBoard && ch0 < 5 * C && sx >= 0 && sx < kBoard;
-                const uint8_t *col = sp + c0 * kPoints + y * kBoard + sx;
-                __align__(16) uint16_t v[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) v[j] = round16(in ? (float)col[j * kPoints] : 0.0f, f16);
-                *reinterpret_cast<uint4 *>(dst + (size_t)i * 8) = *reinterpret_cast<const uint4 *>(v);
-            }
-        }
-        return;
+    // The last CTA to leave (every other one has left its loops, so nothing
+    // reads the flags any more) zeroes the flags and counters for the next
+    // launch: no memset between launches.  CTAs that gave up after a timeout
+    // leave through here too.
+    const int n5L = p.rows5 > 0 ? (p.rows5 + C::TP - 1) / C::TP : 0;
+    int *const exit_ctr = flags0 + n5L;
+    __shared__ int last_out;
+    if (tid == 0) {
+        __threadfence();
+        last_out = atomicAdd(exit_ctr, 1) == (int)gridDim.x - 1;
+        if (last_out) __threadfence();
     }
     __syncthreads();
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        const int r = i / groups, g = i % groups;
-        const int y = r / kL5Pitch, x = r % kL5Pitch;
-        __align__(16) uint16_t v[8];
-        if (aligned) {
-            const int ch0 = g * 8;
-            const int dx = ch0 / C, c0 = ch0 - dx * C;
-            const int sx = x + dx - 2;
-            const bool in = y < kBoard && ch0 < 5 * C && sx >= 0 && sx < kBoard;
-            const uint8_t *col = sp + c0 * kPoints + y * kBoard + sx;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) v[j] = round16(in ? (float)col[j * kPoints] : 0.0f, f16);
-        } else {
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int ch = g * 8 + j;
-                float val = 0.0f;
-                if (y < kBoard && ch < 5 * C) {
-                    const int dx = ch / C, c = ch % C;
-                    const int sx = x + dx - 2;
-                    if (sx >= 0 && sx < kBoard) val = (float)sp[c * kPoints + y * kBoard + sx];
-                }
-                v[j] = round16(val, f16);
-            }
-        }
-        *reinterpret_cast<uint4 *>(dst + (size_t)i * 8) = *reinterpret_cast<const uint4 *>(v);
-    }
+    if (last_out)
+        for (int i = tid; i <= n3L + 1 + n5L; i += blockDim.x) p.flags[i] = 0;
 }
-
-void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, bool f16, __nv_bfloat16 *out,
-                           cudaStream_t s, const int *count, int count_base) {
-    // four CTAs per board, each writing a quarter of its rows
-    pack_planes_l5_kernel<<<dim3(B, 4), 256, 0, s>>>(planes, B, C, halves, f16 ? 1 : 0, out, count, count_base);
-}
+#undef WAIT_LIM
 
 // ------------------------------------------------------------------ launch
 
@@ -1434,7 +1311,9 @@ int tc_init_device() {
 int tc_head_parts(int n, int variant) { return (n == 128 && variant != 1) ? 4 : 1; }
 
 size_t trunk_flag_ints(int rows, int rows5) {
-    return (size_t)(rows + TrunkCfg::TP - 1) / TrunkCfg::TP + 1 + (size_t)(rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP;
+    // chunk flags, item counter, first-layer chunk flags, exit counter
+    return (size_t)(rows + TrunkCfg::TP - 1) / TrunkCfg::TP + 1 + (size_t)(rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP +
+           1;
 }
 
 template <int N, int HALVES, int KIND, bool HEAD>
@@ -1516,10 +1395,6 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     const int n3 = (T.rows + TrunkCfg::TP - 1) / TrunkCfg::TP;
     const int n5 = fused ? (T.rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP : 0;
     const int grid = std::min(n5 + T.nl * n3, sm_count);
-    if (cudaMemsetAsync(flags, 0, sizeof(int) * (n3 + 1 + n5), s) != cudaSuccess) {
-        lg_set_error("launch_tc_trunk: flag reset failed");
-        return LG_ERR_CUDA;
-    }
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kTrunkThreads);

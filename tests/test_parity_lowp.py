@@ -100,6 +100,43 @@ def test_bf16_device_path(gpu_lib, weights, positions):
         assert np.array_equal(out.cpu().numpy(), host)
 
 
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_chunked_device_call_equals_one_call_per_chunk(gpu_lib, weights, positions, prec):
+    """A device call over several chunks packs chunk k+1's planes in the CTAs
+    of chunk k's finish launch (softmax, or the value head).  The results
+    equal those of calling each chunk alone, bit for bit: when every chunk
+    runs on the trunk, and when the last chunk runs on the small-batch
+    kernel (which reads the planes, so nothing is packed for it)."""
+    import torch
+    lg = gpu_lib
+    mb = 64
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], prec),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], prec), max_batch=mb) as c:
+        c.set_tuning(mb, 3, 0)  # buckets 33..64: the trunk with the first layer inside
+        c.set_tuning(5, 4, 0)   # buckets 5..8: the small-batch kernel
+        s = torch.cuda.current_stream()
+        for B in (4 * mb + 5, 3 * mb + 40):
+            pp = torch.from_numpy(np.ascontiguousarray(positions["planes_p"][:B, :24])).cuda()
+            pv = torch.from_numpy(np.ascontiguousarray(positions["planes_v"][:B, :24])).cuda()
+            probs = torch.empty((B, 361), device="cuda")
+            logits = torch.empty((B, 361), device="cuda")
+            vals = torch.empty(B, device="cuda")
+            c.policy_device(pp.data_ptr(), B, probs.data_ptr(), 1.0, logits.data_ptr(), s.cuda_stream)
+            c.value_device(pv.data_ptr(), B, vals.data_ptr(), s.cuda_stream)
+            probs1 = torch.empty_like(probs)
+            logits1 = torch.empty_like(logits)
+            vals1 = torch.empty_like(vals)
+            for b0 in range(0, B, mb):
+                nb = min(mb, B - b0)
+                c.policy_device(pp[b0].data_ptr(), nb, probs1[b0].data_ptr(), 1.0, logits1[b0].data_ptr(),
+                                s.cuda_stream)
+                c.value_device(pv[b0].data_ptr(), nb, vals1[b0].data_ptr(), s.cuda_stream)
+            s.synchronize()
+            assert torch.equal(probs, probs1), B
+            assert torch.equal(logits, logits1), B
+            assert torch.equal(vals, vals1), B
+
+
 def test_lowp_rejects_unsupported_shape(gpu_lib, weights):
     lg = gpu_lib
     with pytest.raises(lg.LeelaGPUError):
