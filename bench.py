@@ -277,7 +277,6 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     # ---------------- timed region: inputs resident in HBM (142 MB > L2)
     launches0 = ctx.stats()["kernel_launches"]
-    ctx.profile(True)
     clocks = ClockSampler(local)
     clocks.start()
     barrier(world)
@@ -292,6 +291,19 @@ def run_ours(args, world, rank, local):
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     gpu_launches = ctx.stats()["kernel_launches"] - launches0
+    # ---------------- the same steps again with CUDA events around every
+    # launch (per-kernel times: the roofline's trunk launches and the
+    # kernel-time shares); the events serialise the launches, so this
+    # region's step time is reported beside `value`, not as it
+    ctx.profile(True)
+    torch.cuda.synchronize()
+    ep0, ep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ep0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ep1.record(stream)
+    torch.cuda.synchronize()
+    ms_prof = ep0.elapsed_time(ep1)
     n3, ms3 = ctx.profile_read(lg.PROF_TC_3X3)
     nh, msh = ctx.profile_read(lg.PROF_TC_HEAD)
     nf, msf = ctx.profile_read(lg.PROF_TC_FIRST)
@@ -396,6 +408,7 @@ def run_ours(args, world, rank, local):
             ("tc_trunk", mstr), ("tc_3x3", ms3 + msh), ("tc_5x5_first", msf), ("pack_planes", mspk),
             ("softmax_value_fc", mstl), ("other", mso)) if v},
         "kernel_choice_batch256": tuning,
+        "ms_per_step_with_launch_events": ms_prof / args.steps,
         "clocks": clk,
         "gpu_launches": gpu_launches,
         "pair_flop_rate_tflops": FLOP_PAIR_PER_POS * value / world / 1e12,

@@ -828,6 +828,7 @@ extern "C" LG_API int lg_fast_create(int device, int c_in, int n3x3, int fc_hidd
         lg_set_error("lg_fast_create: the fused student kernel needs an sm_10x GPU (got sm_%d%d)", major, minor);
         return LG_ERR_ARG;
     }
+    if (int rc0 = finish_init_device()) return rc0;
     lg_fast *f = new lg_fast();
     f->device = device;
     f->c_in = c_in;

@@ -128,7 +128,9 @@ struct lg_ctx {
     float *lat_fcv = nullptr;
     // tensor-core buffers
     __nv_bfloat16 *l3[2] = {nullptr, nullptr};
-    __nv_bfloat16 *l5 = nullptr;
+    // the first layer's expanded input rows; a chunked device call alternates
+    // l5 and l5b, so the next chunk is packed while a trunk reads the other
+    __nv_bfloat16 *l5 = nullptr, *l5b = nullptr;
     int *d_err = nullptr;
     // shared
     uint8_t *d_planes = nullptr;
@@ -667,12 +669,17 @@ bool trunk_fusable(const Net &n) {
            n.tc[0].cout == 128;
 }
 
-// next (optional): the following batch's planes, packed into c->l5 by the
-// CTAs of this batch's finish launch (the trunk has read c->l5 by then).
+// next (optional): the following batch's planes, packed by CTAs of this
+// batch's finish launch into next->out, which must not be this batch's l5.
+// l5buf: this batch's first-layer rows (default c->l5).  pdl: the trunk and
+// the finish are launched as programmatic dependents of the kernel before
+// them (the trunk's prologue overlaps that kernel's end, the packing CTAs
+// of the finish start as the trunk's CTAs leave).
 int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
                float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof,
                bool l5_ready = false, const int *count = nullptr, int count_base = 0,
-               const PackJob *next = nullptr) {
+               const PackJob *next = nullptr, __nv_bfloat16 *l5buf = nullptr, bool pdl = false) {
+    __nv_bfloat16 *const L5 = l5buf ? l5buf : c->l5;
     if (!count && use_lat(c, n, B) && !l5_ready)
         return forward_lat(c, n, planes, B, T, probs, logits_out, value, s, nlaunch, prof);
     if (count && !trunk_fusable(n)) {
@@ -685,7 +692,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
     const TcConv &first = n.tc[0];
     if (!l5_ready) {
         ProfScope ps(c, prof, LG_PROF_PACK, s);
-        launch_pack_planes_l5(planes, B, d.c_in, first.halves, f16 != 0, c->l5, s, count, count_base);
+        launch_pack_planes_l5(planes, B, d.c_in, first.halves, f16 != 0, L5, s, count, count_base);
         ++L;
     }
     float *lg = logits_out ? logits_out : c->d_logits;
@@ -705,7 +712,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
             // (or runs as the launch's first items)
             TcTrunk tt{};
             if (fuse_first) {
-                tt.buf5 = c->l5;
+                tt.buf5 = L5;
                 tt.rows5 = B * kL5Board;
                 tt.w0 = first.w;
                 tt.bias0 = first.bias;
@@ -723,6 +730,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
             tt.f16 = f16;
             tt.count = count;
             tt.count_base = count_base;
+            tt.pdl = pdl;
             if (c->stall_kind == 0) {
                 // the first item of the second 3x3 layer
                 tt.stall_item = (fuse_first ? (tt.rows5 + 255) / 256 : 0) + (tt.rows + 255) / 256;
@@ -739,7 +747,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
             break;
         }
         TcLayer tl{};
-        tl.in = (l == 0) ? (const void *)c->l5 : (const void *)c->l3[cur];
+        tl.in = (l == 0) ? (const void *)L5 : (const void *)c->l3[cur];
         tl.w = t.w;
         tl.bias = t.bias;
         tl.scale = t.scale;
@@ -783,12 +791,12 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
             j.value = value;
             j.part = c->d_fcpart;
             j.cnt = c->d_fccnt;
-            launch_finish_pack(j, *next, s);
+            launch_finish_pack(j, *next, s, pdl);
         } else if (!d.value_head) {
-            launch_softmax(h, B, T, probs, s);
+            launch_softmax(h, B, T, probs, s, nullptr, pdl);
         } else {
             launch_value_fc(h, B, n.w1s, n.b1, n.w2, n.b2, d.fc_hidden, d.act, d.value_map, value,
-                            c->d_fcpart, c->d_fccnt, s);
+                            c->d_fcpart, c->d_fccnt, s, pdl);
         }
     }
     ++L;
@@ -798,11 +806,13 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
 
 int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs,
             float *logits, float *value, cudaStream_t s, int *nlaunch, bool prof = false,
-            bool l5_ready = false, const PackJob *next = nullptr) {
+            bool l5_ready = false, const PackJob *next = nullptr, __nv_bfloat16 *l5buf = nullptr,
+            bool pdl = false) {
     Net &n = c->nets[net];
     if (n.d.precision == LG_FP32)
         return forward_fp32(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof);
-    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof, l5_ready, nullptr, 0, next);
+    return forward_tc(c, n, planes, B, T, probs, logits, value, s, nlaunch, prof, l5_ready, nullptr, 0, next,
+                      l5buf, pdl);
 }
 
 // Host call: chunks of up to max_batch positions go through a cached CUDA
@@ -984,12 +994,21 @@ int run_device(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float 
     size_t per_in = (size_t)n.d.c_in * kPoints;
     // Tensor-core nets: the finish launch of chunk k also packs chunk k+1's
     // planes (when neither chunk runs on the small-batch kernel), so a chunk
-    // costs a trunk launch and a finish launch.
+    // costs a trunk launch and a finish launch; chunks alternate between the
+    // two first-layer buffers.  Trunk and finish are programmatic dependents
+    // of the kernel before them: the trunk's prologue overlaps the previous
+    // finish, and the next chunk's packing CTAs start on the SMs the trunk
+    // leaves.  Every kernel that reads another's results waits for it
+    // (griddepcontrol.wait), and each trunk signals its dependents only
+    // after its own wait, so a packing CTA of chunk k's finish starts only
+    // after chunk k-1's trunk -- the last reader of its buffer -- completed.
     const bool tc = n.d.precision != LG_FP32;
     bool l5_ready = false;
-    for (int b0 = 0; b0 < B; b0 += c->max_batch) {
+    int k = 0;
+    for (int b0 = 0; b0 < B; b0 += c->max_batch, ++k) {
         int nb = std::min(c->max_batch, B - b0);
         const int nb1 = std::min(c->max_batch, B - b0 - nb);
+        __nv_bfloat16 *const l5cur = (k & 1) ? c->l5b : c->l5, *const l5nxt = (k & 1) ? c->l5 : c->l5b;
         PackJob pk{};
         const PackJob *next = nullptr;
         if (tc && nb1 > 0 && (l5_ready || !use_lat(c, n, nb)) && !use_lat(c, n, nb1)) {
@@ -998,14 +1017,14 @@ int run_device(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float 
             pk.C = n.d.c_in;
             pk.halves = n.tc[0].halves;
             pk.f16 = n.d.precision == LG_FP16 ? 1 : 0;
-            pk.out = c->l5;
+            pk.out = l5nxt;
             next = &pk;
         }
         int nl = 0;
         rc = forward(c, net, planes + (size_t)b0 * per_in, nb, T,
                      probs ? probs + (size_t)b0 * kPoints : nullptr,
                      logits ? logits + (size_t)b0 * kPoints : nullptr, value ? value + b0 : nullptr,
-                     s, &nl, c->profiling, l5_ready, next);
+                     s, &nl, c->profiling, l5_ready, next, l5cur, tc);
         l5_ready = next != nullptr;
         if (rc) return rc;
         c->launches += nl;
@@ -1286,6 +1305,7 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
             max_tc_l5 = std::max(max_tc_l5, (size_t)n.tc[0].halves * 64);
         }
     }
+    if ((rc = finish_init_device())) return fail(rc);
     size_t mb = (size_t)max_batch;
     if (max_act) {
         if ((rc = dev_alloc(c, &c->act[0], mb * kPoints * max_act)) ||
@@ -1296,7 +1316,8 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
     if (max_tc_l3) {
         if ((rc = dev_alloc(c, &c->l3[0], mb * kL3Board * max_tc_l3)) ||
             (rc = dev_alloc(c, &c->l3[1], mb * kL3Board * max_tc_l3)) ||
-            (rc = dev_alloc(c, &c->l5, mb * kL5Board * max_tc_l5)))
+            (rc = dev_alloc(c, &c->l5, mb * kL5Board * max_tc_l5)) ||
+            (rc = dev_alloc(c, &c->l5b, mb * kL5Board * max_tc_l5)))
             return fail(rc);
         // Pad rows of the L3 buffers are read as zeros and never written
         // with anything else.

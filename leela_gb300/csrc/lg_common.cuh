@@ -71,6 +71,15 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
 
+// Programmatic dependent launch (sm_90+).  grid_dep_wait: wait until the
+// grids this one depends on have completed and their memory operations are
+// visible (returns at once when the grid was launched without a programmatic
+// dependency).  grid_dep_launch: allow the next grid in the stream, if it was
+// launched with programmatic stream serialization, to start before this one
+// completes (it still waits in its own grid_dep_wait).
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }

@@ -48,8 +48,10 @@ struct HeadIn {
     int count_base = 0;
 };
 // entropy (optional): -sum p ln p of each board's probabilities, in nats.
+// pdl: launched as a programmatic dependent of the previous kernel (the
+// finish kernels wait for it before reading anything).
 void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cudaStream_t s,
-                    float *entropy = nullptr);
+                    float *entropy = nullptr, bool pdl = false);
 // Value head, one launch (tiled split-K FC1 pre-activations; the CTAs that
 // finish last add them in a fixed order and run b1, the activation, FC2 and
 // the value map); `part` holds value_fc_part_floats(B, H) floats, `cnt`
@@ -58,8 +60,11 @@ void launch_softmax(const HeadIn &h, int B, float temperature, float *probs, cud
 // value_fc_slice_units() hidden units: [ceil(H/64)][361][64], zero-padded.
 void launch_value_fc(const HeadIn &h, int B, const float *w1s, const float *b1, const float *w2,
                      float b2, int H, int act, int value_map, float *value, float *part, int *cnt,
-                     cudaStream_t s);
+                     cudaStream_t s, bool pdl = false);
 size_t value_fc_part_floats(int B, int H);
+// Kernel attributes of the finish kernels (once per device, before the first
+// launch on it).
+int finish_init_device();
 size_t value_fc_counter_ints(int B, int H);
 int value_fc_slice_units();
 
@@ -84,7 +89,12 @@ struct PackJob {
     int B, C, halves, f16;
     __nv_bfloat16 *out;
 };
-void launch_finish_pack(const FinishJob &j, const PackJob &pk, cudaStream_t s);
+// (For a value head these are two launches: the packing, then the head.)
+// With pdl the launch is a programmatic dependent of the previous kernel
+// (the batch's trunk): the packing CTAs run as soon as they are scheduled --
+// `pk.out` must then be rows that kernel does not read -- and the finishing
+// CTAs wait for it.
+void launch_finish_pack(const FinishJob &j, const PackJob &pk, cudaStream_t s, bool pdl = false);
 
 // ------------------------------------------------- tensor-core (tcgen05) path
 //
@@ -125,8 +135,11 @@ int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t
 // when f16) with halves*64 channels: channel dx*C + c = plane c at
 // (y, x + dx - 2).
 // With count set, boards b >= *count - count_base are skipped.
+// With pdl the launch is a programmatic dependent of the previous kernel (a
+// trunk): it packs without waiting for it (`out` must be rows it does not
+// read) and waits for it before exiting.
 void launch_pack_planes_l5(const uint8_t *planes, int B, int C, int halves, bool f16, __nv_bfloat16 *out,
-                           cudaStream_t s, const int *count = nullptr, int count_base = 0);
+                           cudaStream_t s, const int *count = nullptr, int count_base = 0, bool pdl = false);
 // Writes the layer output (L3 rows) or, for the fused head, the head output
 // before its bias into parts[boards*361] (tc_head_parts() = 1 array).
 // Returns LG_ERR_ARG if no kernel covers the shape.
@@ -165,6 +178,9 @@ struct TcTrunk {
     // give the buffers' extent)
     const int *count = nullptr;
     int count_base = 0;
+    // launched as a programmatic dependent of the previous kernel in the
+    // stream (its prologue overlaps that kernel), instead of cooperatively
+    bool pdl = false;
 };
 // flags: trunk_flag_ints(rows, rows5) ints of device scratch, zero before the first
 // launch; the launch's last CTA leaves them zero again (no memset between launches).

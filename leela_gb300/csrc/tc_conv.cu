@@ -776,6 +776,7 @@ __global__ void __maxnreg__(96)
     // buffers' extent p.rows
     int rows = p.rows, rows5 = p.rows5;
     if (p.count) {
+        grid_dep_wait();  // the count was written by an earlier kernel
         const int nb = min(p.rows / kL3Board, max(0, *p.count - p.count_base));
         rows = nb * kL3Board;
         rows5 = p.rows5 > 0 ? nb * kL5Board : 0;
@@ -838,6 +839,12 @@ __global__ void __maxnreg__(96)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base;
+    // Launched as a programmatic dependent of the previous kernel, the
+    // prologue above (barriers, TMEM, tensor-map prefetch: no global memory)
+    // overlapped it; everything below may read what it wrote.  The next
+    // kernel may then be scheduled as this one's CTAs leave.
+    grid_dep_wait();
+    grid_dep_launch();
 
     auto fail = [&](int code) {
         atomicCAS(p.err, 0, code);
@@ -1401,8 +1408,16 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     cfg.dynamicSmemBytes = TrunkCfg::SMEM;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
+    if (T.pdl) {
+        // No co-residency is needed (items are claimed in order, so every
+        // item a claimed item waits for belongs to a running CTA): the
+        // launch may start while the previous kernel's CTAs still run.
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+    } else {
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+    }
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cudaError_t e;
