@@ -37,6 +37,7 @@
 #include "ladder.cuh"
 
 namespace lg {
+using namespace ptx;
 
 constexpr int kWords = (kPoints + 31) / 32;  // 12
 
@@ -86,11 +87,10 @@ __device__ void unite(int *par, int a, int b) {
 // 16-bit channels a row, 1.0 encoded as `one`: 0x3F80 for BF16, 0x3C00 for
 // FP16) instead of the planes
 template <int WHICH, bool EXTRA, bool L5>
-__global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict__ squares,
-                                                     const int8_t *__restrict__ to_move,
-                                                     const int32_t *__restrict__ moves, int B,
-                                                     int nplanes, uint8_t *__restrict__ planes, int halves,
-                                                     uint32_t one, uint4 *__restrict__ l5) {
+__device__ __forceinline__ void gather_board(const int8_t *__restrict__ squares, const int8_t *__restrict__ to_move,
+                                             const int32_t *__restrict__ moves, int B, int nplanes,
+                                             uint8_t *__restrict__ planes, int halves, uint32_t one,
+                                             uint4 *__restrict__ l5) {
     constexpr bool extra = EXTRA;
     constexpr int kCand = extra ? 2 * kPoints : 1;
     __shared__ uint32_t rowc[2][kBoard];  // row bitboard: bit x of rowc[c][y] = stone of colour c at (y, x)
@@ -360,19 +360,39 @@ __global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict
     for (int i = 0; i < nplanes; ++i) dst[(size_t)i * kPoints] = (uint8_t)((bits >> i) & 1u);
 }
 
+// Launched as a programmatic dependent of a trunk, the gather runs on the
+// SMs the trunk's CTAs leave (its output must be rows that trunk does not
+// read) and waits for the trunk only before it exits, so that a kernel which
+// waits for the gather has the trunk's results too.
+template <int WHICH, bool EXTRA, bool L5>
+__global__ void __launch_bounds__(384, 3) gather_kernel(const int8_t *__restrict__ squares,
+                                                     const int8_t *__restrict__ to_move,
+                                                     const int32_t *__restrict__ moves, int B,
+                                                     int nplanes, uint8_t *__restrict__ planes, int halves,
+                                                     uint32_t one, uint4 *__restrict__ l5) {
+    ptx::grid_dep_launch();
+    gather_board<WHICH, EXTRA, L5>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
+    ptx::grid_dep_wait();
+}
+
 template <bool L5>
 static void launch_gather_kernel(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B,
                                  int which, int nplanes, uint8_t *planes, int halves, uint32_t one, uint4 *l5,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, bool pdl) {
     const bool extra = nplanes > 24;
-    if (which == 0 && extra)
-        gather_kernel<0, true, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
-    else if (which == 0)
-        gather_kernel<0, false, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
-    else if (extra)
-        gather_kernel<1, true, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
-    else
-        gather_kernel<1, false, L5><<<B, 384, 0, s>>>(squares, to_move, moves, B, nplanes, planes, halves, one, l5);
+    void (*k)(const int8_t *, const int8_t *, const int32_t *, int, int, uint8_t *, int, uint32_t, uint4 *) =
+        which == 0 ? (extra ? gather_kernel<0, true, L5> : gather_kernel<0, false, L5>)
+                   : (extra ? gather_kernel<1, true, L5> : gather_kernel<1, false, L5>);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(B);
+    cfg.blockDim = dim3(384);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k, squares, to_move, moves, B, nplanes, planes, halves, one, l5);
 }
 
 static int check_gather(int B, int which, int nplanes, const int32_t *moves) {
@@ -385,14 +405,15 @@ static int check_gather(int B, int which, int nplanes, const int32_t *moves) {
 }
 
 int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
-                  int nplanes, uint8_t *planes, cudaStream_t s) {
+                  int nplanes, uint8_t *planes, cudaStream_t s, bool pdl) {
     if (int rc = check_gather(B, which, nplanes, moves)) return rc;
-    if (B > 0) launch_gather_kernel<false>(squares, to_move, moves, B, which, nplanes, planes, 0, 0u, nullptr, s);
+    if (B > 0)
+        launch_gather_kernel<false>(squares, to_move, moves, B, which, nplanes, planes, 0, 0u, nullptr, s, pdl);
     return LG_OK;
 }
 
 int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
-                     int nplanes, int halves, bool f16, __nv_bfloat16 *l5, cudaStream_t s) {
+                     int nplanes, int halves, bool f16, __nv_bfloat16 *l5, cudaStream_t s, bool pdl) {
     if (int rc = check_gather(B, which, nplanes, moves)) return rc;
     if (halves < 1 || 5 * nplanes > halves * 64) {
         lg_set_error("gather: %d planes need %d L5 channels, the layer has %d", nplanes, 5 * nplanes, halves * 64);
@@ -400,7 +421,7 @@ int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t
     }
     if (B > 0)
         launch_gather_kernel<true>(squares, to_move, moves, B, which, nplanes, nullptr, halves,
-                                   f16 ? 0x3C00u : 0x3F80u, reinterpret_cast<uint4 *>(l5), s);
+                                   f16 ? 0x3C00u : 0x3F80u, reinterpret_cast<uint4 *>(l5), s, pdl);
     return LG_OK;
 }
 

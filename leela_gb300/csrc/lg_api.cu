@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -146,6 +147,17 @@ struct lg_ctx {
     uint8_t *h_planes = nullptr, *h_planes_b = nullptr;
     float *h_out = nullptr, *h_out2 = nullptr, *h_out_b = nullptr, *h_out2_b = nullptr;
     cudaEvent_t host_done[2] = {nullptr, nullptr};
+    // board calls over several chunks of a tensor-core net (allocated on the
+    // first such call): a ring of kPipe slots, each holding one chunk's
+    // boards (pinned, device) and results (device, pinned, with the error
+    // word); a stream for the copies
+    static constexpr int kPipe = 4;
+    cudaStream_t copy_stream = nullptr;
+    size_t pl_in_bytes = 0, pl_out_floats = 0;
+    uint8_t *pl_h_in = nullptr;
+    int8_t *pl_d_in = nullptr;
+    float *pl_d_out = nullptr, *pl_h_out = nullptr;
+    cudaEvent_t pl_h2d[kPipe] = {}, pl_comp[kPipe] = {}, pl_d2h[kPipe] = {};
     int planes_c = 0;
     std::mutex mu;
     std::map<std::tuple<int, int, uint32_t, int>, std::pair<cudaGraphExec_t, int>> graphs;
@@ -671,6 +683,8 @@ bool trunk_fusable(const Net &n) {
 
 // next (optional): the following batch's planes, packed by CTAs of this
 // batch's finish launch into next->out, which must not be this batch's l5.
+// mid (optional): launches made between the layers and the finish (the
+// board pipeline's gather of the next chunk).
 // l5buf: this batch's first-layer rows (default c->l5).  pdl: the trunk and
 // the finish are launched as programmatic dependents of the kernel before
 // them (the trunk's prologue overlaps that kernel's end, the packing CTAs
@@ -678,7 +692,8 @@ bool trunk_fusable(const Net &n) {
 int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs,
                float *logits_out, float *value, cudaStream_t s, int *nlaunch, bool prof,
                bool l5_ready = false, const int *count = nullptr, int count_base = 0,
-               const PackJob *next = nullptr, __nv_bfloat16 *l5buf = nullptr, bool pdl = false) {
+               const PackJob *next = nullptr, __nv_bfloat16 *l5buf = nullptr, bool pdl = false,
+               const std::function<int()> *mid = nullptr) {
     __nv_bfloat16 *const L5 = l5buf ? l5buf : c->l5;
     if (!count && use_lat(c, n, B) && !l5_ready)
         return forward_lat(c, n, planes, B, T, probs, logits_out, value, s, nlaunch, prof);
@@ -770,6 +785,10 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
         ++L;
         if (l > 0) cur ^= 1;
     }
+    if (mid) {
+        const int rc = (*mid)();
+        if (rc) return rc;
+    }
     {
         ProfScope ps(c, prof, LG_PROF_TAIL, s);
         HeadIn h{c->d_parts, tc_head_parts(d.width, use_trunk ? 0 : var3), part_stride, n.head_b, d.act_head,
@@ -815,6 +834,166 @@ int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *pr
                       l5buf, pdl);
 }
 
+// ----------------------------------------------------- board-call pipeline
+
+constexpr int kPipeMaxBatch = 4096;  // larger contexts keep the per-chunk graphs
+
+size_t pipe_mv_off(size_t mb) { return (mb * (kPoints + 1) + 3) & ~(size_t)3; }
+
+int pipe_alloc(lg_ctx *c) {
+    if (c->pl_d_in) return LG_OK;
+    constexpr int R = lg_ctx::kPipe;
+    const size_t mb = (size_t)c->max_batch;
+    c->pl_in_bytes = (pipe_mv_off(mb) + mb * 16 + 255) & ~(size_t)255;
+    c->pl_out_floats = (2 * mb * kPoints + 64 + 63) & ~(size_t)63;  // probs, logits, the error word
+    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        lg_set_error("board pipeline: stream creation failed");
+        return LG_ERR_CUDA;
+    }
+    for (int r = 0; r < R; ++r)
+        if (cudaEventCreateWithFlags(&c->pl_h2d[r], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->pl_comp[r], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->pl_d2h[r], cudaEventDisableTiming) != cudaSuccess) {
+            lg_set_error("board pipeline: event creation failed");
+            return LG_ERR_CUDA;
+        }
+    if (cudaMallocHost(&c->pl_h_in, R * c->pl_in_bytes) != cudaSuccess ||
+        cudaMallocHost(&c->pl_h_out, R * c->pl_out_floats * sizeof(float)) != cudaSuccess) {
+        lg_set_error("board pipeline: cudaMallocHost failed");
+        return LG_ERR_ALLOC;
+    }
+    int8_t *din = nullptr;
+    float *dout = nullptr;
+    if (int rc = dev_alloc(c, &din, R * c->pl_in_bytes)) return rc;
+    if (int rc = dev_alloc(c, &dout, R * c->pl_out_floats)) return rc;
+    c->pl_d_in = din;
+    c->pl_d_out = dout;
+    return LG_OK;
+}
+
+// Board calls of a tensor-core net over more than one chunk.  Chunk k uses
+// slot k % kPipe: the host copies its boards into the slot's pinned buffer
+// and the copy stream moves them to the device; the compute stream runs the
+// trunk of chunk k, the gather of chunk k+1 (into the other first-layer
+// buffer) and the finish of chunk k as programmatic dependents, so that the
+// gather runs on the SMs the trunk's CTAs leave; the copy stream brings
+// chunk k's results (and the error word) back after the finish, and the
+// host hands them out two chunks later, after which the slot is reused.
+// The waits on the copy stream's events sit between a finish and the next
+// trunk, so no event separates a trunk from the gather and finish after it.
+int run_host_boards_pipe(lg_ctx *c, int net, int B, float T, float *probs, float *logits, float *value,
+                         const int8_t *squares, const int8_t *to_move, const int32_t *moves) {
+    constexpr int R = lg_ctx::kPipe;
+    Net &n = c->nets[net];
+    if (int rc = pipe_alloc(c)) return rc;
+    const int mb = c->max_batch, nchunks = (B + mb - 1) / mb;
+    const bool with_moves = n.d.c_in > 24, want_logits = logits != nullptr && !n.d.value_head;
+    const int which = net == LG_NET_POLICY ? 0 : 1;
+    const size_t mv_off = pipe_mv_off((size_t)mb);
+    cudaStream_t s = c->stream, cs = c->copy_stream;
+    auto nb_of = [&](int k) { return std::min(mb, B - k * mb); };
+    auto l5_of = [&](int k) { return (k & 1) ? c->l5b : c->l5; };
+    auto din = [&](int k) { return c->pl_d_in + (size_t)(k % R) * c->pl_in_bytes; };
+    auto hin = [&](int k) { return c->pl_h_in + (size_t)(k % R) * c->pl_in_bytes; };
+    auto dout = [&](int k) { return c->pl_d_out + (size_t)(k % R) * c->pl_out_floats; };
+    auto hout = [&](int k) { return c->pl_h_out + (size_t)(k % R) * c->pl_out_floats; };
+    const size_t err_off = 2 * (size_t)mb * kPoints;
+    auto stage_in = [&](int k) -> int {
+        const int nb = nb_of(k), b0 = k * mb;
+        uint8_t *h = hin(k);
+        std::memcpy(h, squares + (size_t)b0 * kPoints, (size_t)nb * kPoints);
+        std::memcpy(h + (size_t)mb * kPoints, to_move + b0, (size_t)nb);
+        if (with_moves) std::memcpy(h + mv_off, moves + (size_t)b0 * 4, (size_t)nb * 16);
+        LG_CUDA_TRY(cudaMemcpyAsync(din(k), h, c->pl_in_bytes, cudaMemcpyHostToDevice, cs));
+        LG_CUDA_TRY(cudaEventRecord(c->pl_h2d[k % R], cs));
+        return LG_OK;
+    };
+    auto gather = [&](int k, bool pdl) -> int {
+        const int8_t *d = din(k), *dtm = d + (size_t)mb * kPoints;
+        const int32_t *dmv = with_moves ? reinterpret_cast<const int32_t *>(d + mv_off) : nullptr;
+        const int nb = nb_of(k);
+        ++c->launches;
+        if (use_lat(c, n, nb))  // the small-batch kernel reads planes
+            return launch_gather(d, dtm, dmv, nb, which, n.d.c_in, c->d_planes, s, pdl);
+        return launch_gather_l5(d, dtm, dmv, nb, which, n.d.c_in, n.tc[0].halves, n.d.precision == LG_FP16,
+                                l5_of(k), s, pdl);
+    };
+    auto collect = [&](int k) -> int {
+        const int nb = nb_of(k), b0 = k * mb;
+        LG_CUDA_TRY(cudaEventSynchronize(c->pl_d2h[k % R]));
+        const float *h = hout(k);
+        int herr = 0;
+        std::memcpy(&herr, h + err_off, sizeof(int));
+        if (herr) {
+            lg_set_error("kernel reported error status %d", herr);
+            return LG_ERR_DEVICE;
+        }
+        if (n.d.value_head) {
+            std::memcpy(value + b0, h, (size_t)nb * sizeof(float));
+        } else {
+            std::memcpy(probs + (size_t)b0 * kPoints, h, (size_t)nb * kPoints * sizeof(float));
+            if (want_logits)
+                std::memcpy(logits + (size_t)b0 * kPoints, h + (size_t)mb * kPoints,
+                            (size_t)nb * kPoints * sizeof(float));
+        }
+        return LG_OK;
+    };
+    int rc = stage_in(0);
+    if (!rc) rc = stage_in(1);  // nchunks >= 2
+    if (!rc && cudaStreamWaitEvent(s, c->pl_h2d[0], 0) != cudaSuccess) rc = LG_ERR_CUDA;
+    if (!rc) rc = gather(0, false);
+    int collected = 0;
+    for (int k = 0; k < nchunks && !rc; ++k) {
+        const int nb = nb_of(k);
+        const bool more = k + 1 < nchunks;
+        if (more && cudaStreamWaitEvent(s, c->pl_h2d[(k + 1) % R], 0) != cudaSuccess) {
+            rc = LG_ERR_CUDA;
+            break;
+        }
+        const std::function<int()> mid = [&]() { return gather(k + 1, true); };
+        float *d = dout(k);
+        int nl = 0;
+        rc = forward_tc(c, n, c->d_planes, nb, T, d, want_logits ? d + (size_t)mb * kPoints : nullptr, d, s, &nl,
+                        false, !use_lat(c, n, nb), nullptr, 0, nullptr, l5_of(k), true, more ? &mid : nullptr);
+        if (rc) break;
+        c->launches += nl;
+        // chunk k's results (and the error word) back on the copy stream
+        float *h = hout(k);
+        const size_t nout = n.d.value_head ? (size_t)nb : (size_t)nb * kPoints;
+        if (cudaEventRecord(c->pl_comp[k % R], s) != cudaSuccess || cudaStreamWaitEvent(cs, c->pl_comp[k % R], 0) ||
+            cudaMemcpyAsync(h, d, nout * sizeof(float), cudaMemcpyDeviceToHost, cs) ||
+            (want_logits && cudaMemcpyAsync(h + (size_t)mb * kPoints, d + (size_t)mb * kPoints,
+                                            nout * sizeof(float), cudaMemcpyDeviceToHost, cs)) ||
+            cudaMemcpyAsync(h + err_off, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, cs) ||
+            cudaEventRecord(c->pl_d2h[k % R], cs)) {
+            lg_set_error("board pipeline: copy-back failed: %s", cudaGetErrorString(cudaGetLastError()));
+            rc = LG_ERR_CUDA;
+            break;
+        }
+        // slot (k + 2) % R held chunk k + 2 - R: hand it out, then stage
+        // chunk k + 2 there
+        if (k + 2 < nchunks) {
+            if (k + 2 - R >= 0) {
+                rc = collect(collected);
+                ++collected;
+                if (rc) break;
+            }
+            rc = stage_in(k + 2);
+        }
+    }
+    if (!rc) {
+        for (; collected < nchunks && !rc; ++collected) rc = collect(collected);
+    }
+    if (rc) {
+        // nothing may still use the slots or buffers when the call returns
+        cudaStreamSynchronize(s);
+        cudaStreamSynchronize(cs);
+        if (rc == LG_ERR_DEVICE) cudaMemset(c->d_err, 0, sizeof(int));
+        cudaGetLastError();
+    }
+    return rc;
+}
+
 // Host call: chunks of up to max_batch positions go through a cached CUDA
 // graph of copy-in + forward + copy-out (one graph per chunk size and
 // staging slot).  Two pinned slots alternate, so the host packs chunk k+1
@@ -852,6 +1031,9 @@ int run_host(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *p
     int rc = check_fault(c);
     if (rc) return rc;
     cudaSetDevice(c->device);
+    if (l5_boards && B > c->max_batch && c->max_batch <= kPipeMaxBatch && !use_lat(c, n, c->max_batch) &&
+        c->stall_kind < 0)
+        return run_host_boards_pipe(c, net, B, T, probs, logits, value, squares, to_move, moves);
     const size_t per_in = (size_t)n.d.c_in * kPoints;
     const bool want_logits = logits != nullptr && !n.d.value_head;
     uint32_t tbits;
@@ -1242,6 +1424,15 @@ extern "C" void lg_destroy(lg_ctx *c) {
     if (c->h_out2_b) cudaFreeHost(c->h_out2_b);
     for (int i = 0; i < 2; ++i)
         if (c->host_done[i]) cudaEventDestroy(c->host_done[i]);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    for (int i = 0; i < lg_ctx::kPipe; ++i) {
+        if (c->pl_h2d[i]) cudaEventDestroy(c->pl_h2d[i]);
+        if (c->pl_comp[i]) cudaEventDestroy(c->pl_comp[i]);
+        if (c->pl_d2h[i]) cudaEventDestroy(c->pl_d2h[i]);
+    }
+    if (c->pl_h_in) cudaFreeHost(c->pl_h_in);
+    if (c->pl_h_out) cudaFreeHost(c->pl_h_out);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     for (int i = 0; i < 2; ++i) {
         if (c->srv_planes[i]) cudaFreeHost(c->srv_planes[i]);
         if (c->srv_out[i]) cudaFreeHost(c->srv_out[i]);

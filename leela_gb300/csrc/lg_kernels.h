@@ -123,13 +123,16 @@ struct TcLayer {
 // move before it, ko point, white-has-komi flag; needed for planes 24..31);
 // planes [B][nplanes][361].
 constexpr int kGatherPlanes = 32;
+// pdl: launched as a programmatic dependent of the previous kernel (a trunk):
+// it gathers while that kernel's CTAs leave -- its output must be rows that
+// kernel does not read -- and waits for it before exiting.
 int launch_gather(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
-                  int nplanes, uint8_t *planes, cudaStream_t s);
+                  int nplanes, uint8_t *planes, cudaStream_t s, bool pdl = false);
 // The same planes written straight as the first layer's expanded input (the
 // rows launch_pack_planes_l5 makes from them, `halves` x 64 channels).
 // (BF16 rows, or FP16 when f16.)
 int launch_gather_l5(const int8_t *squares, const int8_t *to_move, const int32_t *moves, int B, int which,
-                     int nplanes, int halves, bool f16, __nv_bfloat16 *l5, cudaStream_t s);
+                     int nplanes, int halves, bool f16, __nv_bfloat16 *l5, cudaStream_t s, bool pdl = false);
 
 // Expanded 5x5 input: planes [B][C][361] bytes -> L5 rows (BF16, or FP16
 // when f16) with halves*64 channels: channel dx*C + c = plane c at
