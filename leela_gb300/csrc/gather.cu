@@ -329,6 +329,43 @@ __device__ __forceinline__ void gather_board(const int8_t *__restrict__ squares,
         const int groups = halves * 8;
         uint4 *dst = l5 + (size_t)b * kL5Board * groups;
         const bool aligned = (nplanes & 7) == 0;  // a group's 8 channels share one dx
+        if ((int)blockDim.x % groups == 0) {
+            // each thread keeps one 16-byte group of channels (their taps dx
+            // and planes are constants) and walks the rows: no division by
+            // the plane or group count in the loop
+            const int g = p % groups, rstep = (int)blockDim.x / groups;
+            int dxj[8], cj[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int ch = g * 8 + j;
+                dxj[j] = ch / nplanes;
+                cj[j] = ch - dxj[j] * nplanes;
+            }
+            for (int r = p / groups; r < kL5Board; r += rstep) {
+                const int y = r / kL5Pitch, x = r - y * kL5Pitch;
+                uint32_t w[4] = {0u, 0u, 0u, 0u};
+                if (y < kBoard) {
+                    if (aligned) {
+                        const int sx = x + dxj[0] - 2;
+                        if (dxj[0] < 5 && sx >= 0 && sx < kBoard) {
+                            const uint32_t v = pbits[y * kBoard + sx] >> cj[0];
+#pragma unroll
+                            for (int j = 0; j < 4; ++j)
+                                w[j] = ((v >> (2 * j)) & 1u) * one | ((v >> (2 * j + 1)) & 1u) * (one << 16);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const int sx = x + dxj[j] - 2;
+                            if (dxj[j] < 5 && sx >= 0 && sx < kBoard && ((pbits[y * kBoard + sx] >> cj[j]) & 1u))
+                                w[j >> 1] |= (j & 1) ? (one << 16) : one;
+                        }
+                    }
+                }
+                dst[(size_t)r * groups + g] = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+            return;
+        }
         for (int i = p; i < kL5Board * groups; i += blockDim.x) {
             const int r = i / groups, g = i - r * groups;
             const int y = r / kL5Pitch, x = r - y * kL5Pitch;
