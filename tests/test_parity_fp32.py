@@ -203,3 +203,28 @@ def test_small_batch_kernel_repeated_calls(gpu_lib, weights, positions):
             assert np.array_equal(c.policy(positions["planes_p"][:1, :24]), ref1)
             assert np.array_equal(c.policy(positions["planes_p"][:8, :24]), ref8)
             assert np.array_equal(c.value(positions["planes_v"][:8, :24]), vref)
+
+
+@pytest.mark.parametrize("fc_hidden", [64, 192, 256, 320])
+def test_value_head_widths_vs_fp64(gpu_lib, oracle_mod, positions, fc_hidden):
+    """The value head's FC chain at several widths against the FP64 oracle
+    (FP32 nets, small trunk): up to 256 hidden units it runs on clusters of
+    2 x ceil(H/64) CTAs (64 and 192 leave a partial or odd cluster), wider
+    heads on the split-K kernel whose last CTAs finish the reduction.  Over
+    more than one chunk (max_batch 32, 70 positions) and at batch 1."""
+    lg, O = gpu_lib, oracle_mod
+    shape = dict(c_in=24, width1=64, width=64, n3x3=2, head_k=1, act=O.RELU, act_head=1,
+                 value_head=1, fc_hidden=fc_hidden, value_map=0)
+    n = O.make_net(shape)
+    w = O.he_weights(n, 11)
+    src = positions["planes_v"][:70, :24]
+    O.enable_blas()
+    try:
+        ref = O.forward_f64(n, w, src)
+    finally:
+        O.disable_blas()
+    with lg.Context(value=lg.NetDesc(w, **shape, precision="fp32"), max_batch=32) as c:
+        v = c.value(src)
+        v1 = c.value(src[:1])
+    assert np.abs(v - ref).max() < 1e-5
+    assert np.abs(v1 - ref[:1]).max() < 1e-5
