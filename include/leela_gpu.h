@@ -203,6 +203,15 @@ LG_API int lg_poll(lg_ctx *ctx, void **tags, int max, int timeout_us);
  * count their kernels), and batches served by the batching server. */
 LG_API int lg_stats(lg_ctx *ctx, long long *kernel_launches, long long *batches);
 
+/* Device-side error of the device-pointer calls (no counterpart in the
+ * reference, whose OpenCL calls block).  lg_policy_device / lg_value_device
+ * return without waiting, so a kernel whose bounded wait ran out (what a
+ * blocking call reports as LG_ERR_DEVICE) only records a code in the
+ * context's error word.  After synchronizing the streams it used, the caller
+ * reads it here: LG_OK, or LG_ERR_DEVICE with the code in lg_last_error(),
+ * and the word is cleared. */
+LG_API int lg_device_error(lg_ctx *ctx);
+
 /* FP32 policy forward that allocates nothing (no counterpart in the
  * reference).  Same inputs, outputs and results as lg_policy_device on an
  * FP32 policy net, for callers that cannot call cudaMalloc at evaluation

@@ -57,7 +57,7 @@ _lib_lock = threading.Lock()
 
 EXPORTS = ["lg_weight_count", "lg_create", "lg_destroy", "lg_last_error", "lg_policy",
            "lg_value", "lg_policy_device", "lg_value_device", "lg_submit", "lg_poll",
-           "lg_stats", "lg_inject_fault", "lg_inject_stall", "lg_profile", "lg_profile_read",
+           "lg_stats", "lg_device_error", "lg_inject_fault", "lg_inject_stall", "lg_profile", "lg_profile_read",
            "lg_policy_device_static", "lg_autotune", "lg_tuning", "lg_set_tuning",
            "lg_policy_avg8_device", "lg_value_avg8_device", "lg_weights_save",
            "lg_weights_load"]
@@ -88,6 +88,7 @@ def library():
             L.lg_stats.argtypes = [vp, P(ctypes.c_longlong), P(ctypes.c_longlong)]
             L.lg_inject_fault.argtypes = [vp, i32]
             L.lg_inject_stall.argtypes = [vp, i32, i32]
+            L.lg_device_error.argtypes = [vp]
             L.lg_profile.argtypes = [vp, i32]
             L.lg_policy_device_static.argtypes = [vp, vp, i32, f32, vp, vp, vp]
             L.lg_autotune.argtypes = [vp, ctypes.c_char_p, i32]
@@ -302,6 +303,12 @@ class Context:
 
     def inject_fault(self, nth_call: int):
         _check(library().lg_inject_fault(self._h, nth_call))
+
+    def device_error(self) -> int:
+        """lg_device_error: after the streams of earlier device-pointer calls
+        were synchronized, LG_OK (0) or LG_ERR_DEVICE (-5) if one of their
+        kernels gave up a bounded wait; the error word is cleared."""
+        return int(library().lg_device_error(self._h))
 
     def inject_stall(self, kind: int, polls: int = 0):
         """lg_inject_stall: the next trunk (kind 0) or small-batch (kind 1)

@@ -1762,6 +1762,20 @@ extern "C" int lg_stats(lg_ctx *c, long long *kernel_launches, long long *batche
     return LG_OK;
 }
 
+extern "C" int lg_device_error(lg_ctx *c) {
+    if (!c) return LG_ERR_ARG;
+    std::lock_guard<std::mutex> g(c->mu);
+    cudaSetDevice(c->device);
+    int herr = 0;
+    LG_CUDA_TRY(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+        LG_CUDA_TRY(cudaMemset(c->d_err, 0, sizeof(int)));
+        lg_set_error("kernel reported error status %d", herr);
+        return LG_ERR_DEVICE;
+    }
+    return LG_OK;
+}
+
 extern "C" int lg_inject_fault(lg_ctx *c, int nth_call) {
     if (!c || nth_call < 0) return LG_ERR_ARG;
     c->fault_in = nth_call;

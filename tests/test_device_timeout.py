@@ -39,3 +39,49 @@ def test_device_wait_runs_out_and_the_context_survives(gpu_lib, weights, positio
         assert np.array_equal(c.policy(pp), good_p)
         assert np.array_equal(c.value(pv), good_v)
         print(f"{prec} kind {kind} B {B}: stalled call returned after {elapsed * 1e3:.1f} ms: {e.value}")
+
+
+@pytest.mark.parametrize("net", ["policy", "value"])
+def test_chained_device_call_wait_runs_out(gpu_lib, weights, positions, net):
+    """A device call over three chunks (each chunk's trunk, head and the next
+    chunk's packing launched as programmatic dependents) whose first trunk
+    gives up a wait: the chain still completes in bounded time, the later
+    chunks are right, lg_device_error reports the kernel's error word once,
+    and the next call gives the same results as before."""
+    import torch
+    lg = gpu_lib
+    mb, B = 256, 3 * 256
+    idx = np.arange(B) % 1024
+    key = "planes_p" if net == "policy" else "planes_v"
+    planes = torch.from_numpy(np.ascontiguousarray(positions[key][idx, :24])).cuda()
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"), max_batch=mb) as c:
+        c.set_tuning(mb, 3, 0)
+        s = torch.cuda.current_stream()
+
+        def run():
+            if net == "policy":
+                out = torch.empty((B, 361), device="cuda")
+                c.policy_device(planes.data_ptr(), B, out.data_ptr(), 1.0, None, s.cuda_stream)
+            else:
+                out = torch.empty(B, device="cuda")
+                c.value_device(planes.data_ptr(), B, out.data_ptr(), s.cuda_stream)
+            s.synchronize()
+            return out.cpu().numpy()
+
+        good = run()
+        assert c.device_error() == 0
+        c.inject_stall(0, 1 << 14)
+        t0 = time.perf_counter()
+        bad = run()
+        elapsed = time.perf_counter() - t0
+        assert elapsed < 20.0
+        assert c.device_error() == -5
+        assert b"error status" in lg.library().lg_last_error()
+        assert c.device_error() == 0  # cleared
+        # the stalled launch was the first chunk's trunk; the next chunks ran
+        # normally (the trunk's last CTA leaves its flags at zero)
+        assert np.array_equal(bad[mb:], good[mb:])
+        assert np.array_equal(run(), good)
+        assert c.device_error() == 0
+        print(f"{net}: chained call with a stalled trunk returned after {elapsed * 1e3:.1f} ms")
