@@ -240,7 +240,7 @@ LG_API int lg_policy_device_static(lg_ctx *ctx, const uint8_t *planes, int B, fl
  * tensor-core nets (0: one launch per layer with 256-row tiles on the
  * transposed kernel, 1: one launch per layer with 128-row tiles, which put
  * twice as many CTAs on a small batch, 2: all 3x3 layers in one persistent
- * cooperative launch, 3: as 2 with the 5x5 first layer in the same launch),
+ * launch, 3: as 2 with the 5x5 first layer in the same launch),
  * for the first layer (0: 256-row, 1: 128-row tiles; unused by choices 3
  * and 4), and -- for buckets of at most 8 positions -- choice 4: every layer
  * of the net in one small-batch launch (FP32 nets: 0 = the generic per-layer
@@ -347,7 +347,7 @@ LG_API int lg_gated_device(lg_fast *student, lg_ctx *full, const uint8_t *planes
 #define LG_PROF_OTHER 4    /* FP32 plane packing and head conv */
 #define LG_PROF_TC_TRUNK 5 /* persistent kernel running all 3x3 layers (incl. the fused head) */
 #define LG_PROF_PACK 6     /* tensor-core plane packing (planes -> expanded BF16 rows) */
-#define LG_PROF_TAIL 7     /* softmax, value FC1 + final */
+#define LG_PROF_TAIL 7     /* softmax or value head (with the next chunk's packing in chained calls) */
 #define LG_PROF_LAT 8      /* small-batch kernel: a whole net in one launch */
 #define LG_PROF_KINDS 9
 LG_API int lg_profile(lg_ctx *ctx, int enable);

@@ -120,7 +120,9 @@ __global__ void __launch_bounds__(kSoftmaxThreads) softmax_kernel(const HeadIn h
 // --------------------------------------------------------------- value head
 //
 // innerproduct<361,H> (+act) then innerproduct<H,1>, then tanh, (1+tanh)/2
-// (Network.cpp:395-423, 733-737) or no map (value_map 2).
+// (Network.cpp:395-423, 733-737) or no map (value_map 2).  Heads of up to
+// 256 hidden units run on clusters (value_fc_cluster_kernel below); wider
+// heads on this split-K kernel.
 // A CTA computes one FC1 tile: 32 boards x 64 hidden units x one of
 // kFcSplit fixed K ranges of the 361 inputs.  The 32 boards' head outputs
 // for the range are formed in shared memory from the head partial sums, the
