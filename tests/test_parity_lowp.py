@@ -225,3 +225,50 @@ def test_small_batch_kernel_lowp(gpu_lib, weights, positions, f64_refs, prec, B)
     assert np.abs(v4 - v64[:B]).max() <= vbar
     assert rel_logit_err(l4, l0).max() <= lbar
     assert np.abs(v4 - v0).max() <= vbar
+
+
+def test_chained_and_pipelined_calls_random_sizes(gpu_lib, weights, positions):
+    """Many call sizes (seeded: ragged last chunks, small-batch tails, one and
+    many chunks) through the chained device calls and the pipelined board
+    calls, each compared bit for bit with one call per chunk.  The launches
+    of a chained call overlap (programmatic dependent launches, two
+    first-layer buffers, a ring of board slots), so this guards the order
+    of their reads and writes."""
+    import torch
+    lg = gpu_lib
+    mb = 128
+    rng = np.random.default_rng(7)
+    sizes = [int(x) for x in rng.integers(1, 6 * mb, size=12)] + [mb + 1, 2 * mb, 3 * mb + 7]
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"), max_batch=mb) as c:
+        c.set_tuning(mb, 3, 0)     # buckets 65..128: the trunk
+        c.set_tuning(64, 3, 0)     # 33..64
+        c.set_tuning(32, 2, 0)     # 17..32: trunk, first layer in its own launch
+        c.set_tuning(16, 0, 0)     # 9..16: per-layer kernels
+        c.set_tuning(8, 4, 0)      # 1..8: the small-batch kernel
+        s = torch.cuda.current_stream()
+        for B in sizes:
+            idx = (np.arange(B) * 7 + B) % 1024
+            pp_h = np.ascontiguousarray(positions["planes_p"][idx, :24])
+            pv_h = np.ascontiguousarray(positions["planes_v"][idx, :24])
+            pp, pv = torch.from_numpy(pp_h).cuda(), torch.from_numpy(pv_h).cuda()
+            probs = torch.empty((B, 361), device="cuda")
+            vals = torch.empty(B, device="cuda")
+            c.policy_device(pp.data_ptr(), B, probs.data_ptr(), 1.0, None, s.cuda_stream)
+            c.value_device(pv.data_ptr(), B, vals.data_ptr(), s.cuda_stream)
+            p1 = torch.empty_like(probs)
+            v1 = torch.empty_like(vals)
+            for b0 in range(0, B, mb):
+                nb = min(mb, B - b0)
+                c.policy_device(pp[b0].data_ptr(), nb, p1[b0].data_ptr(), 1.0, None, s.cuda_stream)
+                c.value_device(pv[b0].data_ptr(), nb, v1[b0].data_ptr(), s.cuda_stream)
+            s.synchronize()
+            assert torch.equal(probs, p1), B
+            assert torch.equal(vals, v1), B
+            # the same positions from boards (pipelined when B > max_batch)
+            sq, tm = positions["squares"][idx], positions["meta"][idx, 0]
+            pb = c.policy_boards(sq, tm)
+            vb = c.value_boards(sq, tm)
+            assert np.array_equal(pb, p1.cpu().numpy()), B
+            assert np.array_equal(vb, v1.cpu().numpy()), B
+        assert c.device_error() == 0
