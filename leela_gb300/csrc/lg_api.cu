@@ -818,7 +818,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
                             c->d_fcpart, c->d_fccnt, s, pdl);
         }
     }
-    ++L;
+    L += (next && d.value_head) ? 2 : 1;  // a value head with the next chunk's packing: two launches
     *nlaunch = L;
     return LG_OK;
 }
