@@ -18,12 +18,17 @@ Reported (one JSON line on rank 0):
               the gather timed) -- the counterpart of get_scored_moves /
               get_value, whose gather runs on the host.  e2e_planes: the same
               through lg_policy / lg_value with host-gathered planes.
-  roofline    the dominant kernel (tensor-core 3x3 conv), CUDA-event timed
-              inside the timed region, against the measured BF16 peak
+  roofline    the dominant kernel (the persistent trunk), timed with CUDA
+              events around every launch in a second pass over the same
+              steps (the first pass, which gives `value`, has no events
+              between launches: they would serialise the programmatic
+              dependent launches), against the measured BF16 peak
   cpu_baseline  the reference algorithm (im2col + OpenBLAS sgemm, one
               position per thread) on this host's cores, bounded sample
-  fp32_plain_batch1  the plain FP32 drop-in path at batch 1 (the ratio
-              target's denominator), and top-1 agreement of BF16 vs FP64
+  summary     the plain FP32 drop-in path at batch 1 (the ratio target's
+              denominator), BF16 and FP16 at other batch sizes, the same step
+              in FP16 (the variant at >= 99% top-1 vs FP64), top-1 agreement
+              vs FP64 over 65,536 positions, serving and the distilled path
 
 --impl reference: the reference's CPU path (the C restatement of
 Network.cpp's im2col + sgemm + bias + activation over scipy's OpenBLAS; the
@@ -442,10 +447,15 @@ def summarize(x, value):
         if "fp16_b256_pairs_per_s" in x:
             out["ratio_fp16_b256_pair_rate_vs_fp32_b1"] = r(
                 x["fp16_b256_pairs_per_s"] / b1["small_batch_device_pairs_per_s"], 1)
+        if "fp16_step_positions_per_s" in x:
+            out["ratio_fp16_step_vs_fp32_b1"] = r(
+                x["fp16_step_positions_per_s"] / b1["small_batch_device_pairs_per_s"], 1)
     if "bf16_by_batch_positions_per_s" in x:
         out["bf16_pairs_per_s_by_batch"] = {k: round(v) for k, v in x["bf16_by_batch_positions_per_s"].items()}
     if "fp16_b256_pairs_per_s" in x:
         out["fp16_b256_pairs_per_s"] = round(x["fp16_b256_pairs_per_s"])
+    if "fp16_step_positions_per_s" in x:
+        out["fp16_step_positions_per_s"] = round(x["fp16_step_positions_per_s"])
     c2 = x.get("config2_vs_fp64", {})
     for prec, d in c2.items():
         if isinstance(d, dict) and "top1" in d:
@@ -650,6 +660,34 @@ def pair_rate_device(lg, wp, wv, prec, B, d_p, d_v, dev, sp, choice=None, reps=N
         return B * reps / (e0.elapsed_time(e1) / 1e3), cb.tuning(B)
 
 
+def step_rate_device(lg, wp, wv, prec, d_p, d_v, dev, sp, steps=10):
+    """The headline step (8192 positions through both nets in chained calls
+    of 256, inputs resident) at another precision: positions/s."""
+    import tempfile
+
+    import torch
+    with lg.Context(policy=lg.NetDesc.config1_policy(wp, prec),
+                    value=lg.NetDesc.config1_value(wv, prec), device=dev.index, max_batch=BATCH) as c:
+        c.autotune(os.path.join(tempfile.gettempdir(), f"leela_gb300_tune_{prec}_{BATCH}.json"))
+        probs = torch.empty((POSITIONS, 361), device=dev)
+        val = torch.empty(POSITIONS, device=dev)
+
+        def step():
+            c.policy_device(d_p.data_ptr(), POSITIONS, probs.data_ptr(), 1.0, None, sp)
+            c.value_device(d_v.data_ptr(), POSITIONS, val.data_ptr(), sp)
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        return POSITIONS * steps / (e0.elapsed_time(e1) / 1e3)
+
+
 def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp, quick=False):
     """FP32 batch 1 (the ratio's denominator), BF16 at the other batch sizes,
     FP16 at batch 256, the precision variants against FP64 over 65,536
@@ -680,6 +718,8 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
     out["bf16_by_batch_positions_per_s"] = by_batch
     out["bf16_kernel_choice_by_batch"] = choices
     out["fp16_b256_pairs_per_s"], _ = pair_rate_device(lg, wp, wv, "fp16", 256, d_p, d_v, dev, sp)
+    # the headline step itself in FP16 (the variant at >= 99% top-1 vs FP64)
+    out["fp16_step_positions_per_s"] = step_rate_device(lg, wp, wv, "fp16", d_p, d_v, dev, sp)
     out["ratio_bf16_batched_vs_fp32_batch1"] = by_batch["256"] / r_lat
     out["config2_vs_fp64"] = config2_vs_fp64(lg, wp, wv, dev.index, sp)
     if not quick:
