@@ -134,7 +134,14 @@ LG_API int lg_value(lg_ctx *ctx, const uint8_t *planes, int B, float *value);
 
 /* Device-resident variants: every pointer is device memory and the work is
  * enqueued on `stream` (a cudaStream_t, NULL = the legacy default stream);
- * the call returns without waiting.  B may exceed max_batch. */
+ * the call returns without waiting.  B may exceed max_batch: chunks of
+ * max_batch run back to back, each chunk's launches as programmatic
+ * dependents of the previous kernel on `stream`.  The calls of one context
+ * share its device buffers: calls whose work could overlap on the GPU (on
+ * different streams, or a blocking call while a device call still runs)
+ * must be ordered by the caller -- one stream per context, or a stream
+ * synchronisation between them.  A kernel's device-side error is read with
+ * lg_device_error. */
 LG_API int lg_policy_device(lg_ctx *ctx, const uint8_t *planes, int B, float temperature, float *probs,
                      float *logits, void *stream);
 LG_API int lg_value_device(lg_ctx *ctx, const uint8_t *planes, int B, float *value, void *stream);
