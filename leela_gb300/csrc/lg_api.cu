@@ -148,15 +148,17 @@ struct lg_ctx {
     float *h_out = nullptr, *h_out2 = nullptr, *h_out_b = nullptr, *h_out2_b = nullptr;
     cudaEvent_t host_done[2] = {nullptr, nullptr};
     // board calls over several chunks of a tensor-core net (allocated on the
-    // first such call): a ring of kPipe slots, each holding one chunk's
-    // boards (pinned, device) and results (device, pinned, with the error
-    // word); a stream for the copies
+    // first such call): a ring of kPipe slots, each holding one super-chunk's
+    // boards (pinned, device), input planes (device) and results (device,
+    // pinned, with the error word); a stream for the copies
     static constexpr int kPipe = 4;
     cudaStream_t copy_stream = nullptr;
     size_t pl_in_bytes = 0, pl_out_floats = 0;
     uint8_t *pl_h_in = nullptr;
     int8_t *pl_d_in = nullptr;
     float *pl_d_out = nullptr, *pl_h_out = nullptr;
+    uint8_t *pl_d_planes = nullptr;
+    size_t pl_planes_bytes = 0;
     cudaEvent_t pl_h2d[kPipe] = {}, pl_comp[kPipe] = {}, pl_d2h[kPipe] = {};
     int planes_c = 0;
     std::mutex mu;
@@ -836,16 +838,23 @@ int forward(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *pr
 
 // ----------------------------------------------------- board-call pipeline
 
-constexpr int kPipeMaxBatch = 4096;  // larger contexts keep the per-chunk graphs
+int run_device(lg_ctx *c, int net, const uint8_t *planes, int B, float T, float *probs, float *logits,
+               float *value, cudaStream_t s);
 
-size_t pipe_mv_off(size_t mb) { return (mb * (kPoints + 1) + 3) & ~(size_t)3; }
+constexpr int kPipeMaxBatch = 4096;    // larger contexts keep the per-chunk graphs
+constexpr int kPipeSuperTarget = 2048; // positions per super-chunk (a multiple of max_batch)
+
+size_t pipe_mv_off(size_t n) { return (n * (kPoints + 1) + 3) & ~(size_t)3; }
+
+int pipe_super(const lg_ctx *c) { return c->max_batch * std::max(1, kPipeSuperTarget / c->max_batch); }
 
 int pipe_alloc(lg_ctx *c) {
     if (c->pl_d_in) return LG_OK;
     constexpr int R = lg_ctx::kPipe;
-    const size_t mb = (size_t)c->max_batch;
-    c->pl_in_bytes = (pipe_mv_off(mb) + mb * 16 + 255) & ~(size_t)255;
-    c->pl_out_floats = (2 * mb * kPoints + 64 + 63) & ~(size_t)63;  // probs, logits, the error word
+    const size_t S = (size_t)pipe_super(c);
+    c->pl_in_bytes = (pipe_mv_off(S) + S * 16 + 255) & ~(size_t)255;
+    c->pl_out_floats = (2 * S * kPoints + 64 + 63) & ~(size_t)63;  // probs, logits, the error word
+    c->pl_planes_bytes = (S * (size_t)c->planes_c * kPoints + 255) & ~(size_t)255;
     if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
         lg_set_error("board pipeline: stream creation failed");
         return LG_ERR_CUDA;
@@ -864,64 +873,81 @@ int pipe_alloc(lg_ctx *c) {
     }
     int8_t *din = nullptr;
     float *dout = nullptr;
+    uint8_t *dpl = nullptr;
     if (int rc = dev_alloc(c, &din, R * c->pl_in_bytes)) return rc;
     if (int rc = dev_alloc(c, &dout, R * c->pl_out_floats)) return rc;
+    if (int rc = dev_alloc(c, &dpl, R * c->pl_planes_bytes)) return rc;
     c->pl_d_in = din;
     c->pl_d_out = dout;
+    c->pl_d_planes = dpl;
     return LG_OK;
 }
 
-// Board calls of a tensor-core net over more than one chunk.  Chunk k uses
-// slot k % kPipe: the host copies its boards into the slot's pinned buffer
-// and the copy stream moves them to the device; the compute stream runs the
-// trunk of chunk k, the gather of chunk k+1 (into the other first-layer
-// buffer) and the finish of chunk k as programmatic dependents, so that the
-// gather runs on the SMs the trunk's CTAs leave; the copy stream brings
-// chunk k's results (and the error word) back after the finish, and the
-// host hands them out two chunks later, after which the slot is reused.
-// The waits on the copy stream's events sit between a finish and the next
-// trunk, so no event separates a trunk from the gather and finish after it.
+// Board calls of a tensor-core net over more than one chunk, in super-chunks
+// of pipe_super(c) positions (a multiple of max_batch) through a ring of
+// kPipe slots.  For super-chunk j (slot j % kPipe): the host copies its
+// boards into the slot's pinned buffer and the copy stream moves them to the
+// device; the compute stream gathers the input planes of all its boards in
+// one launch (one CTA a board: enough boards to fill the GPU, where a
+// chunk's 256 would leave it waiting on one CTA's latency), then runs the
+// chained device path over them (run_device: per chunk the trunk, then the
+// head with the next chunk's packing, as programmatic dependents); the copy
+// stream brings the results and the error word back, and the host hands
+// them out one super-chunk later, while the GPU works on the next.
 int run_host_boards_pipe(lg_ctx *c, int net, int B, float T, float *probs, float *logits, float *value,
                          const int8_t *squares, const int8_t *to_move, const int32_t *moves) {
     constexpr int R = lg_ctx::kPipe;
     Net &n = c->nets[net];
     if (int rc = pipe_alloc(c)) return rc;
-    const int mb = c->max_batch, nchunks = (B + mb - 1) / mb;
+    const int S = pipe_super(c), nsup = (B + S - 1) / S;
     const bool with_moves = n.d.c_in > 24, want_logits = logits != nullptr && !n.d.value_head;
     const int which = net == LG_NET_POLICY ? 0 : 1;
-    const size_t mv_off = pipe_mv_off((size_t)mb);
+    const size_t mv_off = pipe_mv_off((size_t)S);
     cudaStream_t s = c->stream, cs = c->copy_stream;
-    auto nb_of = [&](int k) { return std::min(mb, B - k * mb); };
-    auto l5_of = [&](int k) { return (k & 1) ? c->l5b : c->l5; };
-    auto din = [&](int k) { return c->pl_d_in + (size_t)(k % R) * c->pl_in_bytes; };
-    auto hin = [&](int k) { return c->pl_h_in + (size_t)(k % R) * c->pl_in_bytes; };
-    auto dout = [&](int k) { return c->pl_d_out + (size_t)(k % R) * c->pl_out_floats; };
-    auto hout = [&](int k) { return c->pl_h_out + (size_t)(k % R) * c->pl_out_floats; };
-    const size_t err_off = 2 * (size_t)mb * kPoints;
-    auto stage_in = [&](int k) -> int {
-        const int nb = nb_of(k), b0 = k * mb;
-        uint8_t *h = hin(k);
+    auto nb_of = [&](int j) { return std::min(S, B - j * S); };
+    auto din = [&](int j) { return c->pl_d_in + (size_t)(j % R) * c->pl_in_bytes; };
+    auto hin = [&](int j) { return c->pl_h_in + (size_t)(j % R) * c->pl_in_bytes; };
+    auto dpl = [&](int j) { return c->pl_d_planes + (size_t)(j % R) * c->pl_planes_bytes; };
+    auto dout = [&](int j) { return c->pl_d_out + (size_t)(j % R) * c->pl_out_floats; };
+    auto hout = [&](int j) { return c->pl_h_out + (size_t)(j % R) * c->pl_out_floats; };
+    const size_t err_off = 2 * (size_t)S * kPoints;
+    auto stage_in = [&](int j) -> int {
+        const int nb = nb_of(j), b0 = j * S;
+        uint8_t *h = hin(j);
         std::memcpy(h, squares + (size_t)b0 * kPoints, (size_t)nb * kPoints);
-        std::memcpy(h + (size_t)mb * kPoints, to_move + b0, (size_t)nb);
+        std::memcpy(h + (size_t)S * kPoints, to_move + b0, (size_t)nb);
         if (with_moves) std::memcpy(h + mv_off, moves + (size_t)b0 * 4, (size_t)nb * 16);
-        LG_CUDA_TRY(cudaMemcpyAsync(din(k), h, c->pl_in_bytes, cudaMemcpyHostToDevice, cs));
-        LG_CUDA_TRY(cudaEventRecord(c->pl_h2d[k % R], cs));
+        LG_CUDA_TRY(cudaMemcpyAsync(din(j), h, c->pl_in_bytes, cudaMemcpyHostToDevice, cs));
+        LG_CUDA_TRY(cudaEventRecord(c->pl_h2d[j % R], cs));
         return LG_OK;
     };
-    auto gather = [&](int k, bool pdl) -> int {
-        const int8_t *d = din(k), *dtm = d + (size_t)mb * kPoints;
+    auto launch = [&](int j) -> int {
+        const int nb = nb_of(j);
+        const int8_t *d = din(j), *dtm = d + (size_t)S * kPoints;
         const int32_t *dmv = with_moves ? reinterpret_cast<const int32_t *>(d + mv_off) : nullptr;
-        const int nb = nb_of(k);
+        LG_CUDA_TRY(cudaStreamWaitEvent(s, c->pl_h2d[j % R], 0));
+        if (int rc = launch_gather(d, dtm, dmv, nb, which, n.d.c_in, dpl(j), s)) return rc;
         ++c->launches;
-        if (use_lat(c, n, nb))  // the small-batch kernel reads planes
-            return launch_gather(d, dtm, dmv, nb, which, n.d.c_in, c->d_planes, s, pdl);
-        return launch_gather_l5(d, dtm, dmv, nb, which, n.d.c_in, n.tc[0].halves, n.d.precision == LG_FP16,
-                                l5_of(k), s, pdl);
+        float *o = dout(j);
+        if (int rc = run_device(c, net, dpl(j), nb, T, o, want_logits ? o + (size_t)S * kPoints : nullptr, o, s))
+            return rc;
+        // the results (and the error word) back on the copy stream
+        float *h = hout(j);
+        const size_t nout = n.d.value_head ? (size_t)nb : (size_t)nb * kPoints;
+        LG_CUDA_TRY(cudaEventRecord(c->pl_comp[j % R], s));
+        LG_CUDA_TRY(cudaStreamWaitEvent(cs, c->pl_comp[j % R], 0));
+        LG_CUDA_TRY(cudaMemcpyAsync(h, o, nout * sizeof(float), cudaMemcpyDeviceToHost, cs));
+        if (want_logits)
+            LG_CUDA_TRY(cudaMemcpyAsync(h + (size_t)S * kPoints, o + (size_t)S * kPoints, nout * sizeof(float),
+                                        cudaMemcpyDeviceToHost, cs));
+        LG_CUDA_TRY(cudaMemcpyAsync(h + err_off, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, cs));
+        LG_CUDA_TRY(cudaEventRecord(c->pl_d2h[j % R], cs));
+        return LG_OK;
     };
-    auto collect = [&](int k) -> int {
-        const int nb = nb_of(k), b0 = k * mb;
-        LG_CUDA_TRY(cudaEventSynchronize(c->pl_d2h[k % R]));
-        const float *h = hout(k);
+    auto collect = [&](int j) -> int {
+        const int nb = nb_of(j), b0 = j * S;
+        LG_CUDA_TRY(cudaEventSynchronize(c->pl_d2h[j % R]));
+        const float *h = hout(j);
         int herr = 0;
         std::memcpy(&herr, h + err_off, sizeof(int));
         if (herr) {
@@ -933,57 +959,24 @@ int run_host_boards_pipe(lg_ctx *c, int net, int B, float T, float *probs, float
         } else {
             std::memcpy(probs + (size_t)b0 * kPoints, h, (size_t)nb * kPoints * sizeof(float));
             if (want_logits)
-                std::memcpy(logits + (size_t)b0 * kPoints, h + (size_t)mb * kPoints,
+                std::memcpy(logits + (size_t)b0 * kPoints, h + (size_t)S * kPoints,
                             (size_t)nb * kPoints * sizeof(float));
         }
         return LG_OK;
     };
+    // super-chunk j + 1 is staged before j is launched (its slot last held
+    // j + 1 - R, handed out by then), and j - 1 is handed out while j runs
     int rc = stage_in(0);
-    if (!rc) rc = stage_in(1);  // nchunks >= 2
-    if (!rc && cudaStreamWaitEvent(s, c->pl_h2d[0], 0) != cudaSuccess) rc = LG_ERR_CUDA;
-    if (!rc) rc = gather(0, false);
     int collected = 0;
-    for (int k = 0; k < nchunks && !rc; ++k) {
-        const int nb = nb_of(k);
-        const bool more = k + 1 < nchunks;
-        if (more && cudaStreamWaitEvent(s, c->pl_h2d[(k + 1) % R], 0) != cudaSuccess) {
-            rc = LG_ERR_CUDA;
-            break;
+    for (int j = 0; j < nsup && !rc; ++j) {
+        if (j + 1 < nsup) {
+            while (!rc && collected <= j + 1 - R) rc = collect(collected++);
+            if (!rc) rc = stage_in(j + 1);
         }
-        const std::function<int()> mid = [&]() { return gather(k + 1, true); };
-        float *d = dout(k);
-        int nl = 0;
-        rc = forward_tc(c, n, c->d_planes, nb, T, d, want_logits ? d + (size_t)mb * kPoints : nullptr, d, s, &nl,
-                        false, !use_lat(c, n, nb), nullptr, 0, nullptr, l5_of(k), true, more ? &mid : nullptr);
-        if (rc) break;
-        c->launches += nl;
-        // chunk k's results (and the error word) back on the copy stream
-        float *h = hout(k);
-        const size_t nout = n.d.value_head ? (size_t)nb : (size_t)nb * kPoints;
-        if (cudaEventRecord(c->pl_comp[k % R], s) != cudaSuccess || cudaStreamWaitEvent(cs, c->pl_comp[k % R], 0) ||
-            cudaMemcpyAsync(h, d, nout * sizeof(float), cudaMemcpyDeviceToHost, cs) ||
-            (want_logits && cudaMemcpyAsync(h + (size_t)mb * kPoints, d + (size_t)mb * kPoints,
-                                            nout * sizeof(float), cudaMemcpyDeviceToHost, cs)) ||
-            cudaMemcpyAsync(h + err_off, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, cs) ||
-            cudaEventRecord(c->pl_d2h[k % R], cs)) {
-            lg_set_error("board pipeline: copy-back failed: %s", cudaGetErrorString(cudaGetLastError()));
-            rc = LG_ERR_CUDA;
-            break;
-        }
-        // slot (k + 2) % R held chunk k + 2 - R: hand it out, then stage
-        // chunk k + 2 there
-        if (k + 2 < nchunks) {
-            if (k + 2 - R >= 0) {
-                rc = collect(collected);
-                ++collected;
-                if (rc) break;
-            }
-            rc = stage_in(k + 2);
-        }
+        if (!rc) rc = launch(j);
+        while (!rc && collected < j) rc = collect(collected++);
     }
-    if (!rc) {
-        for (; collected < nchunks && !rc; ++collected) rc = collect(collected);
-    }
+    while (!rc && collected < nsup) rc = collect(collected++);
     if (rc) {
         // nothing may still use the slots or buffers when the call returns
         cudaStreamSynchronize(s);
