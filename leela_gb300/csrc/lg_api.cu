@@ -899,12 +899,25 @@ int run_host_boards_pipe(lg_ctx *c, int net, int B, float T, float *probs, float
     constexpr int R = lg_ctx::kPipe;
     Net &n = c->nets[net];
     if (int rc = pipe_alloc(c)) return rc;
-    const int S = pipe_super(c), nsup = (B + S - 1) / S;
+    // Super-chunks of S positions, except the last ones: the host copies the
+    // last super-chunk's results out after the GPU is done, so the call ends
+    // with one of at most a quarter of S (whole chunks), the rest of the
+    // remainder before it.
+    const int S = pipe_super(c);
+    std::vector<int> sb{0};  // super-chunk starts, then B
+    {
+        const int q = std::max(c->max_batch, S / 4 / c->max_batch * c->max_batch);
+        int b = 0;
+        while (B - b > S + q) sb.push_back(b += S);
+        if (B - b > q) sb.push_back(b = B - q);
+        sb.push_back(B);
+    }
+    const int nsup = (int)sb.size() - 1;
     const bool with_moves = n.d.c_in > 24, want_logits = logits != nullptr && !n.d.value_head;
     const int which = net == LG_NET_POLICY ? 0 : 1;
     const size_t mv_off = pipe_mv_off((size_t)S);
     cudaStream_t s = c->stream, cs = c->copy_stream;
-    auto nb_of = [&](int j) { return std::min(S, B - j * S); };
+    auto nb_of = [&](int j) { return sb[j + 1] - sb[j]; };
     auto din = [&](int j) { return c->pl_d_in + (size_t)(j % R) * c->pl_in_bytes; };
     auto hin = [&](int j) { return c->pl_h_in + (size_t)(j % R) * c->pl_in_bytes; };
     auto dpl = [&](int j) { return c->pl_d_planes + (size_t)(j % R) * c->pl_planes_bytes; };
@@ -912,7 +925,7 @@ int run_host_boards_pipe(lg_ctx *c, int net, int B, float T, float *probs, float
     auto hout = [&](int j) { return c->pl_h_out + (size_t)(j % R) * c->pl_out_floats; };
     const size_t err_off = 2 * (size_t)S * kPoints;
     auto stage_in = [&](int j) -> int {
-        const int nb = nb_of(j), b0 = j * S;
+        const int nb = nb_of(j), b0 = sb[j];
         uint8_t *h = hin(j);
         std::memcpy(h, squares + (size_t)b0 * kPoints, (size_t)nb * kPoints);
         std::memcpy(h + (size_t)S * kPoints, to_move + b0, (size_t)nb);
@@ -945,7 +958,7 @@ int run_host_boards_pipe(lg_ctx *c, int net, int B, float T, float *probs, float
         return LG_OK;
     };
     auto collect = [&](int j) -> int {
-        const int nb = nb_of(j), b0 = j * S;
+        const int nb = nb_of(j), b0 = sb[j];
         LG_CUDA_TRY(cudaEventSynchronize(c->pl_d2h[j % R]));
         const float *h = hout(j);
         int herr = 0;
