@@ -855,31 +855,33 @@ int pipe_alloc(lg_ctx *c) {
     c->pl_in_bytes = (pipe_mv_off(S) + S * 16 + 255) & ~(size_t)255;
     c->pl_out_floats = (2 * S * kPoints + 64 + 63) & ~(size_t)63;  // probs, logits, the error word
     c->pl_planes_bytes = (S * (size_t)c->planes_c * kPoints + 255) & ~(size_t)255;
-    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // each resource is made once, so a call after a failed one (out of
+    // pinned memory, say) neither leaks nor repeats what was made
+    if (!c->copy_stream && cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        c->copy_stream = nullptr;
         lg_set_error("board pipeline: stream creation failed");
         return LG_ERR_CUDA;
     }
     for (int r = 0; r < R; ++r)
-        if (cudaEventCreateWithFlags(&c->pl_h2d[r], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&c->pl_comp[r], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&c->pl_d2h[r], cudaEventDisableTiming) != cudaSuccess) {
-            lg_set_error("board pipeline: event creation failed");
-            return LG_ERR_CUDA;
-        }
-    if (cudaMallocHost(&c->pl_h_in, R * c->pl_in_bytes) != cudaSuccess ||
-        cudaMallocHost(&c->pl_h_out, R * c->pl_out_floats * sizeof(float)) != cudaSuccess) {
+        for (cudaEvent_t *e : {&c->pl_h2d[r], &c->pl_comp[r], &c->pl_d2h[r]})
+            if (!*e && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+                *e = nullptr;
+                lg_set_error("board pipeline: event creation failed");
+                return LG_ERR_CUDA;
+            }
+    if ((!c->pl_h_in && cudaMallocHost(&c->pl_h_in, R * c->pl_in_bytes) != cudaSuccess) ||
+        (!c->pl_h_out && cudaMallocHost(&c->pl_h_out, R * c->pl_out_floats * sizeof(float)) != cudaSuccess)) {
         lg_set_error("board pipeline: cudaMallocHost failed");
         return LG_ERR_ALLOC;
     }
+    if (!c->pl_d_out)
+        if (int rc = dev_alloc(c, &c->pl_d_out, R * c->pl_out_floats)) return rc;
+    if (!c->pl_d_planes)
+        if (int rc = dev_alloc(c, &c->pl_d_planes, R * c->pl_planes_bytes)) return rc;
+    // pl_d_in last: its presence marks the pipeline as complete
     int8_t *din = nullptr;
-    float *dout = nullptr;
-    uint8_t *dpl = nullptr;
     if (int rc = dev_alloc(c, &din, R * c->pl_in_bytes)) return rc;
-    if (int rc = dev_alloc(c, &dout, R * c->pl_out_floats)) return rc;
-    if (int rc = dev_alloc(c, &dpl, R * c->pl_planes_bytes)) return rc;
     c->pl_d_in = din;
-    c->pl_d_out = dout;
-    c->pl_d_planes = dpl;
     return LG_OK;
 }
 
