@@ -450,6 +450,13 @@ def summarize(x, value):
         if "fp16_step_positions_per_s" in x:
             out["ratio_fp16_step_vs_fp32_b1"] = r(
                 x["fp16_step_positions_per_s"] / b1["small_batch_device_pairs_per_s"], 1)
+    f32 = x.get("fp32_roofline", {})
+    if f32:
+        pk = f32["fp32_sgemm_tflops"]
+        out["fp32_peak_tflops"] = r(pk, 1)
+        out["fp32_b1_frac_of_fp32_peak"] = r(f32["b1_tflops"] / pk, 3)
+        out["fp32_b256_pairs_per_s"] = round(f32["b256_pairs_per_s"])
+        out["fp32_b256_frac_of_fp32_peak"] = r(f32["b256_tflops"] / pk, 3)
     if "bf16_by_batch_positions_per_s" in x:
         out["bf16_pairs_per_s_by_batch"] = {k: round(v) for k, v in x["bf16_by_batch_positions_per_s"].items()}
     if "fp16_b256_pairs_per_s" in x:
@@ -688,6 +695,34 @@ def step_rate_device(lg, wp, wv, prec, d_p, d_v, dev, sp, steps=10):
         return POSITIONS * steps / (e0.elapsed_time(e1) / 1e3)
 
 
+def fp32_peak_tflops(dev, n=8192, reps=8):
+    """FP32 throughput of the GPU's FFMA pipes, the roofline of the plain FP32
+    path: an n^3 FP32 GEMM through cuBLAS (torch.matmul with TF32 off, so
+    FP32 FFMA, no tensor cores), best of reps, CUDA events."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(n, n, device=dev)
+        b = torch.randn(n, n, device=dev)
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        del a, b
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, sp, quick=False):
     """FP32 batch 1 (the ratio's denominator), BF16 at the other batch sizes,
     FP16 at batch 256, the precision variants against FP64 over 65,536
@@ -708,6 +743,12 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
             c32.policy(planes_p[i:i + 1])
             c32.value(planes_v[i:i + 1])
         host_rate = n / (time.perf_counter() - t0)
+    # the FP32 path batched, and the FP32 peak both are measured against
+    r_b256, _ = pair_rate_device(lg, wp, wv, "fp32", 256, d_p, d_v, dev, sp, reps=8)
+    peak32 = fp32_peak_tflops(dev)
+    out["fp32_roofline"] = {"fp32_sgemm_tflops": peak32, "b1_tflops": r_lat * FLOP_PAIR_PER_POS / 1e12,
+                            "b256_pairs_per_s": r_b256, "b256_tflops": r_b256 * FLOP_PAIR_PER_POS / 1e12,
+                            "note": "peak: cuBLAS FP32 GEMM 8192^3 with TF32 off (FFMA), best of 8"}
     out["fp32_batch1"] = {"small_batch_device_pairs_per_s": r_lat, "per_layer_device_pairs_per_s": r_gen,
                           "small_batch_host_api_pairs_per_s": host_rate,
                           "note": "policy + value per position, batch 1; device = inputs resident, CUDA "
