@@ -100,7 +100,7 @@ def test_bf16_device_path(gpu_lib, weights, positions):
         assert np.array_equal(out.cpu().numpy(), host)
 
 
-@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+@pytest.mark.parametrize("prec", ["bf16", "fp16", "fp8w"])
 def test_chunked_device_call_equals_one_call_per_chunk(gpu_lib, weights, positions, prec):
     """A device call over several chunks packs chunk k+1's planes in the CTAs
     of chunk k's finish launch (softmax, or the value head).  The results
