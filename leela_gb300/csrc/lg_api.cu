@@ -750,7 +750,7 @@ int forward_tc(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *
             tt.pdl = pdl;
             if (c->stall_kind == 0) {
                 // the first item of the second 3x3 layer
-                tt.stall_item = (fuse_first ? (tt.rows5 + 255) / 256 : 0) + (tt.rows + 255) / 256;
+                tt.stall_item = trunk_layer_item(tt.rows, fuse_first ? tt.rows5 : 0, 1);
                 tt.wait_limit = tt.poll_limit = c->stall_polls;
                 c->stall_kind = -1;
             }

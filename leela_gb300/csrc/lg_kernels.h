@@ -190,6 +190,8 @@ struct TcTrunk {
 int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *flags, int *err,
                     cudaStream_t s, int sm_count);
 size_t trunk_flag_ints(int rows, int rows5);
+// index of the first work item of 3x3 layer k (rows5 = 0: no fused first layer)
+int trunk_layer_item(int rows, int rows5, int k);
 size_t tc_conv_smem_bytes(int n, int ntaps, int cin_halves);
 int tc_init_device();
 // Head kernels for the tensor-core path (logits already produced by the

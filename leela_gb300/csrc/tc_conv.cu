@@ -650,7 +650,8 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
 
 // ===========================================================================
 // Kernel "trunk": every 3x3 128->128 layer of a net in one persistent
-// launch, scheduled as work items (layer l, chunk j) of 256 rows.  The
+// launch, scheduled as work items (layer l, chunk j) of 256 rows (224 for
+// the fused 5x5 first layer's items).  The
 // producer of each CTA claims items from a global counter in (layer, chunk)
 // order and runs kernel T's pipeline over each (its windows, weight stages,
 // MMAs, epilogue), ping-ponging between two L3 buffers (layer l reads A when
@@ -688,42 +689,68 @@ struct TrunkParams {
     int count_base;       // boards before this launch's first
 };
 
-// Shared memory of kernel "trunk": window slots sized for the first layer's
-// taller windows (5 taps of pitch 19) and used by both kinds of item.
+constexpr uint32_t kFlagPolls = 1u << 22;  // x ~64 ns sleep: bounded at ~0.3 s
+constexpr int kItemRing = 4;               // item descriptors in flight per CTA
+
+// The trunk's barriers and item ring, kept after its buffers in the dynamic
+// shared memory (the kernel has no static shared memory, so the buffers can
+// use all but the alignment slack of the 227 KB a CTA may have).
+template <int NWIN, int S>
+struct TrunkCtl {
+    uint64_t win_full[NWIN], win_empty[NWIN], w_full[S], w_empty[S];
+    uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], item_done[4], mma_done;
+    uint64_t item_full[kItemRing], item_empty[kItemRing];
+    int item_id[kItemRing];
+    uint32_t tmem_base;
+    int abort_flag;
+    int last_out;
+};
+
+// Shared memory of kernel "trunk": three half-window slots, four staging
+// tiles, five weight stages, the control block.  A 3x3 item covers 256 rows
+// (window 256 + 2 x 24); a first-layer item covers 224 rows so that its
+// window (5 taps of pitch 19: 224 + 2 x 40) fits the same slot: the fifth
+// weight stage lives in the bytes a taller slot would take.  The buffers
+// start at the first 1024-byte boundary of the dynamic region (the 128-byte
+// swizzle's alignment); PAD is the slack left for that.
 struct TrunkCfg {
     using C0 = TcTCfg<2, 0>;
     using C1 = TcTCfg<2, 1>;
     static constexpr int TP = 256;
+    static constexpr int TP5 = 224;
+    static constexpr int WIN5_ROWS = TP5 + 2 * C1::WPRE;
+    static constexpr int SUB5 = WIN5_ROWS / 2;  // TMA box rows of a first-layer half-window
+    static constexpr int WIN5_HALF = WIN5_ROWS * 128;
     static constexpr int NWIN = 3;
-    static constexpr int WIN_SLOT = C1::WIN_HALF > C0::WIN_HALF ? C1::WIN_HALF : C0::WIN_HALF;
-    static constexpr int S = 4;
+    static constexpr int WIN_SLOT = WIN5_HALF > C0::WIN_HALF ? WIN5_HALF : C0::WIN_HALF;
+    static constexpr int S = 5;
     static constexpr int WST_BYTES = C0::WST_BYTES;
     static constexpr int STG_BYTES = C0::STG_BYTES;
     static constexpr int STG_TOTAL = 4 * STG_BYTES;
-    static constexpr int SMEM = 1024 + NWIN * WIN_SLOT + STG_TOTAL + S * WST_BYTES;
-    static_assert(C0::TP == TP && C1::TP == TP, "item rows");
-    static_assert(WIN_SLOT % 1024 == 0 && (C0::SUBROWS * 128) % 1024 == 0 && (C1::SUBROWS * 128) % 1024 == 0,
+    using Ctl = TrunkCtl<NWIN, S>;
+    static constexpr int CTL_OFF = NWIN * WIN_SLOT + STG_TOTAL + S * WST_BYTES;
+    static constexpr int SMEM = 227 * 1024;
+    static constexpr int PAD = SMEM - CTL_OFF - (int)sizeof(Ctl);
+    static_assert(C0::TP == TP && TP5 % 16 == 0 && TP5 <= TP, "item rows");
+    static_assert(WIN_SLOT % 1024 == 0 && (C0::SUBROWS * 128) % 1024 == 0 && (SUB5 * 128) % 1024 == 0,
                   "window boxes keep the 1024-byte swizzle alignment");
-    static_assert(SMEM <= 227 * 1024, "shared memory budget");
+    static_assert(CTL_OFF % 8 == 0 && PAD >= 0, "shared memory budget");
 };
-
-constexpr uint32_t kFlagPolls = 1u << 22;  // x ~64 ns sleep: bounded at ~0.3 s
-constexpr int kItemRing = 4;               // item descriptors in flight per CTA
 
 // The MMAs of one 64-channel half of an item: NTAPS weight stages (one per
 // tap, 4 K steps of 16 each) against the window in the slot whose descriptor
-// is b_desc; stage g of the ring is slot g & 3.  Descriptor start addresses
+// is b_desc; stage g of the ring is slot g % NS.  Descriptor start addresses
 // advance by (bytes >> 4): tap rows of 128 bytes, K steps of 32 bytes.
 // Returns false if a weight stage did not arrive within the wait limit.
-template <int KIND, int NTAPS, int WPRE>
+template <int KIND, int NTAPS, int WPRE, int NS>
 __device__ __forceinline__ bool issue_taps(uint32_t d_tmem, uint64_t a_desc0, uint64_t b_desc, uint32_t idesc,
                                            bool first_half, uint32_t &g, uint64_t *w_full, uint64_t *w_empty,
                                            uint32_t wl) {
     constexpr int kStage16 = TcTCfg<2, 0>::WST_BYTES >> 4;
 #pragma unroll
     for (int t = 0; t < NTAPS; ++t, ++g) {
-        const int s = g & 3;
-        if (!mbar_wait(&w_full[s], (g >> 2) & 1, wl)) return false;
+        const int s = (int)(g % NS);
+        if (!mbar_wait(&w_full[s], (g / NS) & 1, wl)) return false;
         tc_fence_after();
         const uint64_t a = a_desc0 + (uint64_t)(s * kStage16);
         const uint64_t b = b_desc + (uint64_t)((WPRE + (KIND == 0 ? (t / 3 - 1) * kL3Pitch + (t % 3 - 1)
@@ -754,20 +781,31 @@ __global__ void __maxnreg__(96)
     using C1 = TrunkCfg::C1;
     constexpr int HALVES = 2, NO = 128;
     extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    // The buffers need a 1024-byte aligned base; with no static shared
+    // memory the dynamic region starts aligned, and PAD bytes of slack cover
+    // a base that does not.  A launch without room reports code 69.
+    const uint32_t mis = (1024u - (smem_u32(smem_raw) & 1023u)) & 1023u;
+    if (mis > (uint32_t)C::PAD) {
+        if (threadIdx.x == 0) atomicCAS(p.err, 0, 69);
+        return;
+    }
+    uint8_t *smem = smem_raw + mis;
     uint8_t *win = smem;
     uint8_t *stg = smem + C::NWIN * C::WIN_SLOT;
     uint8_t *wst = stg + C::STG_TOTAL;
-
-    __shared__ uint64_t win_full[C::NWIN], win_empty[C::NWIN], w_full[C::S], w_empty[C::S];
+    TrunkCfg::Ctl &ctl = *reinterpret_cast<TrunkCfg::Ctl *>(smem + C::CTL_OFF);
+    uint64_t *const win_full = ctl.win_full, *const win_empty = ctl.win_empty;
+    uint64_t *const w_full = ctl.w_full, *const w_empty = ctl.w_empty;
     // item_done: a ring of 4 (an epilogue warp can be up to two items ahead
     // of the slowest: starting item x needs every warp to have read item
     // x-2's accumulator, hence to have arrived for item x-3)
-    __shared__ uint64_t acc_full[2], acc_empty[2], stg_full[4], stg_empty[4], item_done[4], mma_done;
-    __shared__ uint64_t item_full[kItemRing], item_empty[kItemRing];
-    __shared__ int item_id[kItemRing];
-    __shared__ uint32_t tmem_base;
-    __shared__ int abort_flag;
+    uint64_t *const acc_full = ctl.acc_full, *const acc_empty = ctl.acc_empty;
+    uint64_t *const stg_full = ctl.stg_full, *const stg_empty = ctl.stg_empty;
+    uint64_t *const item_done = ctl.item_done, &mma_done = ctl.mma_done;
+    uint64_t *const item_full = ctl.item_full, *const item_empty = ctl.item_empty;
+    int *const item_id = ctl.item_id;
+    uint32_t &tmem_base = ctl.tmem_base;
+    int &abort_flag = ctl.abort_flag;
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 #define WAIT_LIM (p.wait_limit)  // mbarrier waits (try_wait polls): read from the parameter bank at each use
@@ -783,7 +821,7 @@ __global__ void __maxnreg__(96)
     }
     const int n3L = (p.rows + C::TP - 1) / C::TP;
     const int n3 = (rows + C::TP - 1) / C::TP;
-    const int n5 = rows5 > 0 ? (rows5 + C::TP - 1) / C::TP : 0;
+    const int n5 = rows5 > 0 ? (rows5 + C::TP5 - 1) / C::TP5 : 0;
     const int first = p.rows5 > 0 ? 1 : 0;
     const int nitems = n5 + p.nl * n3;
     int *const flags0 = p.flags + n3L + 1;
@@ -885,7 +923,7 @@ __global__ void __maxnreg__(96)
                     const int hi3 = min(rows, j * C::TP + C::TP + C0::WPRE);
                     const int lo5 = max(0, lo3 - (hi3 - 1) / kL3Board - kBoard);
                     const int hi5 = min(rows5 - 1, hi3 - 1);
-                    for (int jj = lo5 / C::TP; jj <= hi5 / C::TP; ++jj)
+                    for (int jj = lo5 / C::TP5; jj <= hi5 / C::TP5; ++jj)
                         if (!poll_flag(flags0 + jj, 1, p.poll_limit)) {
                             fail(71);
                             goto done_windows;
@@ -905,9 +943,9 @@ __global__ void __maxnreg__(96)
                     fence_proxy_async_global();
                 }
                 const CUtensorMap *im = fl ? &in5 : ((k & 1) ? &in_b : &in_a);
-                const int sub = fl ? C1::SUBROWS : C0::SUBROWS;
-                const uint32_t bytes = fl ? C1::WIN_HALF : C0::WIN_HALF;
-                const int row0 = j * C::TP - (fl ? C1::WPRE : C0::WPRE);
+                const int sub = fl ? C::SUB5 : C0::SUBROWS;
+                const uint32_t bytes = fl ? C::WIN5_HALF : C0::WIN_HALF;
+                const int row0 = fl ? j * C::TP5 - C1::WPRE : j * C::TP - C0::WPRE;
                 for (int h = 0; h < HALVES; ++h, ++wn) {
                     const int ws = wn % C::NWIN;
                     const uint32_t wk = wn / C::NWIN;
@@ -956,7 +994,6 @@ __global__ void __maxnreg__(96)
         // tap and K loops are unrolled per item kind, so issuing an MMA costs
         // a 64-bit add per operand (an MMA of N = 256 lasts ~128 cycles).
         if (lane == 0) {
-            static_assert(C::S == 4, "stage index is g & 3");
             const uint64_t a_desc0 = sdesc_sw128(smem_u32(wst));
             const uint64_t b_desc0 = sdesc_sw128(smem_u32(win));
             uint32_t g = 0, wn = 0;
@@ -971,7 +1008,7 @@ __global__ void __maxnreg__(96)
                 const bool fl = first && l == 0;
                 // N: the item's rows, rounded up to the MMA's multiple of 16
                 // (rows past the tensor are zero-filled and not stored)
-                const int nrows = fl ? min(C::TP, (rows5 - j * C::TP + 15) / 16 * 16) : min(C::TP, rows - j * C::TP);
+                const int nrows = fl ? min(C::TP5, (rows5 - j * C::TP5 + 15) / 16 * 16) : min(C::TP, rows - j * C::TP);
                 const uint32_t idesc = idesc_16(128, nrows, F16);
                 const int acc = q & 1;
                 const uint32_t ak = (uint32_t)(q >> 1);
@@ -986,9 +1023,9 @@ __global__ void __maxnreg__(96)
                     if (!mbar_wait(&win_full[ws], wk & 1, WAIT_LIM)) { fail(77); ok = false; break; }
                     tc_fence_after();
                     const uint64_t b_desc = b_desc0 + (uint64_t)(ws * (C::WIN_SLOT >> 4));
-                    ok = fl ? issue_taps<1, C1::NTAPS, C1::WPRE>(d_tmem, a_desc0, b_desc, idesc, h == 0, g, w_full,
+                    ok = fl ? issue_taps<1, C1::NTAPS, C1::WPRE, C::S>(d_tmem, a_desc0, b_desc, idesc, h == 0, g, w_full,
                                                                  w_empty, WAIT_LIM)
-                            : issue_taps<0, C0::NTAPS, C0::WPRE>(d_tmem, a_desc0, b_desc, idesc, h == 0, g, w_full,
+                            : issue_taps<0, C0::NTAPS, C0::WPRE, C::S>(d_tmem, a_desc0, b_desc, idesc, h == 0, g, w_full,
                                                                  w_empty, WAIT_LIM);
                     if (!ok) { fail(78); break; }
                     mma_commit(&win_empty[ws]);
@@ -1019,14 +1056,14 @@ __global__ void __maxnreg__(96)
             decode(it, l, j);
             const bool fl = first && l == 0;
             const int k = l - first;
-            const int cs = j * C::TP;
+            const int cs = j * (fl ? C::TP5 : C::TP);
             const float bias = fl ? __ldg(p.bias0 + o) : __ldg(p.bias + k * NO + o);
             const float scale = fl ? (p.scale0 ? __ldg(p.scale0 + o) : 1.0f)
                                    : (p.scale ? __ldg(p.scale + k * NO + o) : 1.0f);
             const bool head_layer = HEAD && !fl && k == p.nl - 1;
             const CUtensorMap *om = (k & 1) ? &out_a : &out_b;
             const int rows_l = fl ? rows5 : rows;
-            const int nrows = min(C::TP, rows_l - cs);
+            const int nrows = min(fl ? C::TP5 : C::TP, rows_l - cs);
             const int nhalf = max(0, min(2, (nrows - rq * 64 + 31) / 32));
             const int acc = q & 1;
             const uint32_t ak = (uint32_t)(q >> 1);
@@ -1266,9 +1303,9 @@ __global__ void __maxnreg__(96)
     // reads the flags any more) zeroes the flags and counters for the next
     // launch: no memset between launches.  CTAs that gave up after a timeout
     // leave through here too.
-    const int n5L = p.rows5 > 0 ? (p.rows5 + C::TP - 1) / C::TP : 0;
+    const int n5L = p.rows5 > 0 ? (p.rows5 + C::TP5 - 1) / C::TP5 : 0;
     int *const exit_ctr = flags0 + n5L;
-    __shared__ int last_out;
+    int &last_out = ctl.last_out;
     if (tid == 0) {
         __threadfence();
         last_out = atomicAdd(exit_ctr, 1) == (int)gridDim.x - 1;
@@ -1319,8 +1356,12 @@ int tc_head_parts(int n, int variant) { return (n == 128 && variant != 1) ? 4 : 
 
 size_t trunk_flag_ints(int rows, int rows5) {
     // chunk flags, item counter, first-layer chunk flags, exit counter
-    return (size_t)(rows + TrunkCfg::TP - 1) / TrunkCfg::TP + 1 + (size_t)(rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP +
+    return (size_t)(rows + TrunkCfg::TP - 1) / TrunkCfg::TP + 1 + (size_t)(rows5 + TrunkCfg::TP5 - 1) / TrunkCfg::TP5 +
            1;
+}
+
+int trunk_layer_item(int rows, int rows5, int k) {
+    return (rows5 + TrunkCfg::TP5 - 1) / TrunkCfg::TP5 + k * ((rows + TrunkCfg::TP - 1) / TrunkCfg::TP);
 }
 
 template <int N, int HALVES, int KIND, bool HEAD>
@@ -1372,7 +1413,7 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     if (!rc) rc = encode_map_2d_bf16(&out_b_sw, T.buf_b, 128, (uint64_t)T.rows, 64, 32, true);
     if (!rc) rc = encode_map_2d_bf16(&w_map, T.w, 64, (uint64_t)T.nl * C0::NTAPS * 2 * 128, 64, 128);
     if (fused) {
-        if (!rc) rc = encode_map_2d_bf16(&in5, T.buf5, 128, (uint64_t)T.rows5, 64, C1::SUBROWS);
+        if (!rc) rc = encode_map_2d_bf16(&in5, T.buf5, 128, (uint64_t)T.rows5, 64, TrunkCfg::SUB5);
         if (!rc) rc = encode_map_2d_bf16(&w0_map, T.w0, 64, (uint64_t)C1::NTAPS * 2 * 128, 64, 128);
     } else {
         in5 = in_a;  // unused
@@ -1400,7 +1441,7 @@ int launch_tc_trunk(const TcTrunk &T, float *parts, size_t part_stride, int *fla
     p.poll_limit = T.poll_limit ? T.poll_limit : kFlagPolls;
     p.stall_item = T.stall_item;
     const int n3 = (T.rows + TrunkCfg::TP - 1) / TrunkCfg::TP;
-    const int n5 = fused ? (T.rows5 + TrunkCfg::TP - 1) / TrunkCfg::TP : 0;
+    const int n5 = fused ? (T.rows5 + TrunkCfg::TP5 - 1) / TrunkCfg::TP5 : 0;
     const int grid = std::min(n5 + T.nl * n3, sm_count);
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
