@@ -901,15 +901,17 @@ int run_host_boards_pipe(lg_ctx *c, int net, int B, float T, float *probs, float
     constexpr int R = lg_ctx::kPipe;
     Net &n = c->nets[net];
     if (int rc = pipe_alloc(c)) return rc;
-    // Super-chunks of S positions, except the last ones: the host copies the
-    // last super-chunk's results out after the GPU is done, so the call ends
-    // with one of at most a quarter of S (whole chunks), the rest of the
-    // remainder before it.
+    // Super-chunks of S positions, except the first and the last ones: the
+    // GPU waits for the first one's boards and gather, so it is one chunk;
+    // the host copies the last super-chunk's results out after the GPU is
+    // done, so the call ends with one of at most a quarter of S (whole
+    // chunks), the rest of the remainder before it.
     const int S = pipe_super(c);
     std::vector<int> sb{0};  // super-chunk starts, then B
     {
         const int q = std::max(c->max_batch, S / 4 / c->max_batch * c->max_batch);
         int b = 0;
+        if (S > c->max_batch && B - b > c->max_batch + S + q) sb.push_back(b += c->max_batch);
         while (B - b > S + q) sb.push_back(b += S);
         if (B - b > q) sb.push_back(b = B - q);
         sb.push_back(B);
