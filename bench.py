@@ -463,6 +463,10 @@ def summarize(x, value):
         out["fp16_b256_pairs_per_s"] = round(x["fp16_b256_pairs_per_s"])
     if "fp16_step_positions_per_s" in x:
         out["fp16_step_positions_per_s"] = round(x["fp16_step_positions_per_s"])
+    ens = x.get("ensemble_avg8", {})
+    if ens:
+        out["avg8_root_us_per_pair"] = r(ens["1"]["us_per_call_pair"], 1)
+        out["avg8_b32_positions_per_s"] = round(ens["32"]["positions_per_s"])
     c2 = x.get("config2_vs_fp64", {})
     for prec, d in c2.items():
         if isinstance(d, dict) and "top1" in d:
@@ -667,6 +671,38 @@ def pair_rate_device(lg, wp, wv, prec, B, d_p, d_v, dev, sp, choice=None, reps=N
         return B * reps / (e0.elapsed_time(e1) / 1e3), cb.tuning(B)
 
 
+def ensemble_rates(lg, wp, wv, d_p, d_v, dev, sp):
+    """The 8-symmetry ensemble (AVERAGE_ALL: lg_policy_avg8_device +
+    lg_value_avg8_device, BF16, inputs resident): the root evaluation of a
+    search (1 position = 8 rotated evaluations per net, the small-batch
+    kernel) as microseconds per policy + value call pair, and 32 positions a
+    call (256 evaluations per net, the persistent trunk) as positions/s."""
+    import torch
+    out = {}
+    with lg.Context(policy=lg.NetDesc.config1_policy(wp, "bf16"),
+                    value=lg.NetDesc.config1_value(wv, "bf16"), device=dev.index, max_batch=256) as c:
+        for B, reps in ((1, 200), (32, 100)):
+            probs = torch.empty((B, 361), device=dev)
+            val = torch.empty(B, device=dev)
+
+            def call(i):
+                off = (i * B) % (8192 - B + 1)
+                c.policy_avg8_device(d_p[off].data_ptr(), B, probs.data_ptr(), 1.0, sp)
+                c.value_avg8_device(d_v[off].data_ptr(), B, val.data_ptr(), sp)
+            for i in range(3):
+                call(i)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for i in range(reps):
+                call(i)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            out[str(B)] = {"us_per_call_pair": ms * 1e3, "positions_per_s": B / (ms / 1e3)}
+    return out
+
+
 def step_rate_device(lg, wp, wv, prec, d_p, d_v, dev, sp, steps=10):
     """The headline step (8192 positions through both nets in chained calls
     of 256, inputs resident) at another precision: positions/s."""
@@ -761,6 +797,7 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
     out["fp16_b256_pairs_per_s"], _ = pair_rate_device(lg, wp, wv, "fp16", 256, d_p, d_v, dev, sp)
     # the headline step itself in FP16 (the variant at >= 99% top-1 vs FP64)
     out["fp16_step_positions_per_s"] = step_rate_device(lg, wp, wv, "fp16", d_p, d_v, dev, sp)
+    out["ensemble_avg8"] = ensemble_rates(lg, wp, wv, d_p, d_v, dev, sp)
     out["ratio_bf16_batched_vs_fp32_batch1"] = by_batch["256"] / r_lat
     out["config2_vs_fp64"] = config2_vs_fp64(lg, wp, wv, dev.index, sp)
     if not quick:

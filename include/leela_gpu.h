@@ -254,8 +254,10 @@ LG_API int lg_policy_device_static(lg_ctx *ctx, const uint8_t *planes, int B, fl
  * FP32 kernels, 4 = the small-batch kernel), and keeps the fastest.  With a
  * cache path, a table saved for the same device, SM count and net shapes is
  * loaded instead (unless force), and a new table is saved there (written to
- * a temporary file and renamed).  Without tuning, buckets of at most 8
- * positions use choice 4 and larger ones choice 0.  No reference
+ * a temporary file and renamed).  Without tuning (measured defaults): a
+ * context with a 16-bit net uses choice 4 up to 2 positions and choice 3
+ * above; an FP32-only context uses choice 4 up to 8 positions and its
+ * per-layer kernels above.  No reference
  * counterpart (the OpenCL backend reads a fixed cfg_rowtiles,
  * OpenCL.cpp:634-646).  lg_tuning reports the choice for batch B; it returns
  * 1 once tuned, 0 if not, < 0 on error. */

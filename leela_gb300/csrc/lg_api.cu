@@ -588,6 +588,22 @@ bool use_lat(lg_ctx *c, const Net &n, int B) {
     return n.lat_ok && B <= kLatMaxB && c->lat_part && c->tc_variant[bucket_of(B)][0] == 4;
 }
 
+// Kernel choices without tuning (measured on GB300, policy + value pairs,
+// device-resident inputs): FP32 nets run the small-batch kernel up to 8
+// positions (B = 8: 1.12 against 1.13 ms on the per-layer kernels); 16-bit
+// nets run it up to 2 (B = 2: 220 against 254 us on the persistent trunk;
+// B = 3: 314 against 256 us) and the persistent trunk with the first layer
+// inside from 3 positions on (B = 256: 0.43 against 0.76 ms a pair on the
+// per-layer kernels).  A context with a 16-bit net takes the 16-bit rule.
+void default_tuning(lg_ctx *c) {
+    bool lowp = false;
+    for (const Net &n : c->nets) lowp = lowp || (n.present && n.d.precision != LG_FP32);
+    for (int b = 0; b < 17; ++b) {
+        c->tc_variant[b][0] = lowp ? ((1 << b) <= 2 ? 4 : 3) : ((1 << b) <= kLatMaxB ? 4 : 0);
+        c->tc_variant[b][1] = 0;
+    }
+}
+
 int forward_lat(lg_ctx *c, Net &n, const uint8_t *planes, int B, float T, float *probs, float *logits_out,
                 float *value, cudaStream_t s, int *nlaunch, bool prof) {
     const lg_net_desc &d = n.d;
@@ -1535,9 +1551,7 @@ extern "C" int lg_create(const lg_net_desc *policy, const lg_net_desc *value, in
             return fail(rc);
         if (cudaMemset(c->lat_cnt, 0, sizeof(int) * kLatCntInts) != cudaSuccess) return fail(LG_ERR_CUDA);
     }
-    // small batches default to the small-batch kernel (nets it does not
-    // cover keep their generic path)
-    for (int b = 0; (1 << b) <= kLatMaxB; ++b) c->tc_variant[b][0] = 4;
+    default_tuning(c);
     // An FP32 policy net can be evaluated by lg_policy_device_static: look
     // up its static array's device address now, so that its calls only read
     // the cached pointer.
@@ -2114,8 +2128,7 @@ extern "C" int lg_autotune(lg_ctx *c, const char *cache_path, int force) {
     for (auto &gr : c->graphs) cudaGraphExecDestroy(gr.second.first);
     c->graphs.clear();
     if (rc != LG_OK) {
-        std::memset(c->tc_variant, 0, sizeof c->tc_variant);
-        for (int b = 0; (1 << b) <= kLatMaxB; ++b) c->tc_variant[b][0] = 4;
+        default_tuning(c);
         return rc;
     }
     c->tuned = true;

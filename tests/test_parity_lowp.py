@@ -272,3 +272,37 @@ def test_chained_and_pipelined_calls_random_sizes(gpu_lib, weights, positions):
             assert np.array_equal(pb, p1.cpu().numpy()), B
             assert np.array_equal(vb, v1.cpu().numpy()), B
         assert c.device_error() == 0
+
+
+@pytest.mark.parametrize("B,choice", [(32, 3), (1, 4)])
+def test_avg8_ensemble_on_tensor_cores(gpu_lib, weights, positions, oracle_mod, B, choice):
+    """AVERAGE_ALL on the BF16 path (Network.cpp:642-654, 606-615): the 8
+    rotated copies of each position run as one batch (8 x 32 = 256 through
+    the persistent trunk; 8 x 1 through the small-batch kernel), then are
+    un-rotated and averaged in symmetry order.  Bit for bit the same as the
+    plane-input calls on the rotated planes (board-major, symmetry-minor),
+    averaged in float32 in the same order."""
+    import torch
+    lg, O = gpu_lib, oracle_mod
+    pp = np.ascontiguousarray(positions["planes_p"][:B, :24])
+    pv = np.ascontiguousarray(positions["planes_v"][:B, :24])
+    rp = np.stack([O.rotate_planes(x, r) for x in pp for r in range(8)])
+    rv = np.stack([O.rotate_planes(x, r) for x in pv for r in range(8)])
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"), max_batch=256) as c:
+        c.set_tuning(8 * B, choice, 0)
+        out = torch.empty((B, 361), device="cuda")
+        val = torch.empty(B, device="cuda")
+        s = torch.cuda.current_stream()
+        c.policy_avg8_device(torch.from_numpy(pp).cuda().data_ptr(), B, out.data_ptr(), 0.75, s.cuda_stream)
+        c.value_avg8_device(torch.from_numpy(pv).cuda().data_ptr(), B, val.data_ptr(), s.cuda_stream)
+        s.synchronize()
+        p8 = c.policy(rp, 0.75)
+        v8 = c.value(rv)
+    ref = np.zeros((B, 361), np.float32)
+    vref = np.zeros(B, np.float32)
+    for r in range(8):
+        ref = ref + p8[r::8][:, lg.REV_ROTATE[r]]
+        vref = vref + v8[r::8]
+    assert np.array_equal(out.cpu().numpy(), ref / np.float32(8))
+    assert np.array_equal(val.cpu().numpy(), vref / np.float32(8))
