@@ -920,16 +920,20 @@ int run_host_boards_pipe(lg_ctx *c, int net, int B, float T, float *probs, float
     // Super-chunks of S positions, except the first and the last ones: the
     // GPU waits for the first one's boards and gather, so it is one chunk;
     // the host copies the last super-chunk's results out after the GPU is
-    // done, so the call ends with one of at most a quarter of S (whole
-    // chunks), the rest of the remainder before it.
+    // done, so the call ends with one of at most an eighth of S, the rest of
+    // the remainder before it.  Every super-chunk starts on a multiple of
+    // max_batch, so the chunks are those of the plane-input calls (a ragged
+    // last chunk included) and so are the results, bit for bit.
     const int S = pipe_super(c);
     std::vector<int> sb{0};  // super-chunk starts, then B
     {
-        const int q = std::max(c->max_batch, S / 4 / c->max_batch * c->max_batch);
+        const int mb = c->max_batch;
+        const int q = std::max(mb, S / 8 / mb * mb);
         int b = 0;
-        if (S > c->max_batch && B - b > c->max_batch + S + q) sb.push_back(b += c->max_batch);
+        if (S > mb && B - b > mb + S + q) sb.push_back(b += mb);
         while (B - b > S + q) sb.push_back(b += S);
-        if (B - b > q) sb.push_back(b = B - q);
+        const int last = (B - q + mb - 1) / mb * mb;
+        if (last > b && last < B) sb.push_back(b = last);
         sb.push_back(B);
     }
     const int nsup = (int)sb.size() - 1;

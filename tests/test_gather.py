@@ -148,17 +148,18 @@ def test_board_calls_equal_plane_calls(gpu_lib, positions, weights, prec):
 def test_board_call_pipeline_on_the_trunk(gpu_lib, positions, weights, prec):
     """Board calls over several chunks run as a pipeline: super-chunks of
     2048 positions through a ring of four slots (copies on their own stream,
-    one gather launch per super-chunk, then the chained device path).  Bit
-    for bit the plane calls' results: with the persistent trunk for full
-    chunks, the small-batch kernel for a ragged last chunk, and, at 10,317
-    positions, six super-chunks that wrap the ring."""
+    one gather launch per super-chunk, then the chained device path), a
+    first one of one chunk and a short last one, all starting on chunk
+    boundaries.  Bit for bit the plane calls' results: with the persistent
+    trunk for full chunks, the small-batch kernel for a ragged last chunk,
+    and, at 10,317 positions, seven super-chunks that wrap the ring."""
     lg = gpu_lib
     mb = 64
     with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], prec),
                     value=lg.NetDesc.config1_value(weights["cfg_v"][1], prec), max_batch=mb) as c:
         c.set_tuning(mb, 3, 0)  # buckets 33..64: the trunk with the first layer inside
         c.set_tuning(5, 4, 0)   # buckets 5..8: the small-batch kernel
-        for n in (4 * mb + 5, 3 * mb + 40, 1024, 5 * 2048 + 77):
+        for n in (4 * mb + 5, 3 * mb + 40, 8 * mb + 5, 1024, 2048 + mb + 3, 5 * 2048 + 77):
             idx = np.arange(n) % 1024
             sq, tm = positions["squares"][idx], positions["meta"][idx, 0]
             pb, lb = c.policy_boards(sq, tm, 1.0, return_logits=True)
