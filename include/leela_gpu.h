@@ -168,8 +168,11 @@ LG_API int lg_gather_device(const int8_t *squares, const int8_t *to_move, const 
  * lg_gather_device): copies 362 bytes a position to the device (378 with
  * moves), gathers the net's input planes there (for BF16 / FP8 nets straight
  * into the first layer's input rows), then runs the forward;
- * results as lg_policy / lg_value.  moves may be NULL when the net reads at
- * most 24 planes.
+ * results as lg_policy / lg_value, bit for bit.  Calls of more than
+ * max_batch positions on the tensor-core nets run as a pipeline of
+ * super-chunks (copies in and out on a second stream, overlapping the
+ * forward of the super-chunk before), chunked as lg_policy / lg_value chunk.
+ * moves may be NULL when the net reads at most 24 planes.
  * Replaces: Network::get_scored_moves (Network.cpp:624-674) and
  * Network::get_value (Network.cpp:590-622) at the DIRECT rotation, gather
  * included. */
