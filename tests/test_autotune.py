@@ -98,3 +98,21 @@ def test_fused_first_layer_trunk_equals_separate_first_layer(gpu_lib, weights, p
         v3 = c.value(positions["planes_v"][idx, :24])
     assert rel_logit_err(l3, l2).max() < 1e-5
     assert np.abs(v3 - v2).max() < 1e-5
+
+
+def test_untuned_defaults(gpu_lib, weights):
+    """Without tuning a context takes the measured defaults: with a 16-bit
+    net the small-batch kernel (choice 4) up to 2 positions and the
+    persistent trunk with the first layer inside (choice 3) above; FP32
+    nets the small-batch kernel up to 8 positions and their per-layer
+    kernels above."""
+    lg = gpu_lib
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1], "bf16"),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1], "bf16"), max_batch=256) as c:
+        got = {b: c.tuning(b)["conv3x3"] for b in (1, 2, 3, 8, 9, 256)}
+        assert got == {1: 4, 2: 4, 3: 3, 8: 3, 9: 3, 256: 3}
+        assert not c.tuning(256)["tuned"]
+    with lg.Context(policy=lg.NetDesc.config1_policy(weights["cfg_p"][1]),
+                    value=lg.NetDesc.config1_value(weights["cfg_v"][1]), max_batch=64) as c:
+        got = {b: c.tuning(b)["conv3x3"] for b in (1, 8, 9, 64)}
+        assert got == {1: 4, 8: 4, 9: 0, 64: 0}
