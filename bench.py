@@ -28,7 +28,9 @@ Reported (one JSON line on rank 0):
   summary     the plain FP32 drop-in path at batch 1 (the ratio target's
               denominator), BF16 and FP16 at other batch sizes, the same step
               in FP16 (the variant at >= 99% top-1 vs FP64), top-1 agreement
-              vs FP64 over 65,536 positions, serving and the distilled path
+              vs FP64 over 65,536 positions, the 8-symmetry ensemble (a
+              search's root, and 32 positions a call), serving and the
+              distilled path
 
 --impl reference: the reference's CPU path (the C restatement of
 Network.cpp's im2col + sgemm + bias + activation over scipy's OpenBLAS; the
