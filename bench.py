@@ -29,8 +29,9 @@ Reported (one JSON line on rank 0):
               denominator), BF16 and FP16 at other batch sizes, the same step
               in FP16 (the variant at >= 99% top-1 vs FP64), top-1 agreement
               vs FP64 over 65,536 positions, the 8-symmetry ensemble (a
-              search's root, and 32 positions a call), serving and the
-              distilled path
+              search's root, and 32 positions a call), serving, the
+              distilled path, and leaf evaluations/s under the engine's
+              request pattern (search_pattern.cpp)
 
 --impl reference: the reference's CPU path (the C restatement of
 Network.cpp's im2col + sgemm + bias + activation over scipy's OpenBLAS; the
@@ -465,6 +466,10 @@ def summarize(x, value):
         out["fp16_b256_pairs_per_s"] = round(x["fp16_b256_pairs_per_s"])
     if "fp16_step_positions_per_s" in x:
         out["fp16_step_positions_per_s"] = round(x["fp16_step_positions_per_s"])
+    sp_runs = x.get("search_pattern", {})
+    if sp_runs and "unavailable" not in sp_runs:
+        out["search_pattern_leaf_evals_per_s"] = {k: round(v["leaf_evals_per_s"]) for k, v in sp_runs.items()
+                                                  if "leaf_evals_per_s" in v}
     ens = x.get("ensemble_avg8", {})
     if ens:
         out["avg8_root_us_per_pair"] = r(ens["1"]["us_per_call_pair"], 1)
@@ -705,6 +710,35 @@ def ensemble_rates(lg, wp, wv, d_p, d_v, dev, sp):
     return out
 
 
+def search_pattern_rates(dev, runs=(("bf16", 64, "server"), ("bf16", 64, "direct"), ("bf16", 16, "server"),
+                                        ("fp32", 64, "server"), ("fp32", 64, "direct")), seconds=3.0):
+    """Leaf evaluations per second under the engine's request pattern
+    (leela_gb300/integration/search_pattern.cpp, a C++ program over the C
+    ABI): N threads, each with up to 2 asynchronous policy requests
+    outstanding and one value evaluation per leaf, either through the
+    batching server (merged across threads, as the backend does) or as
+    blocking one-position calls.  Synthetic: no tree, board or host gather."""
+    src = os.path.join(ROOT, "leela_gb300", "integration", "search_pattern.cpp")
+    exe = os.path.join(ROOT, "leela_gb300", "integration", "_build", "search_pattern")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", src, "-I" + os.path.join(ROOT, "include"),
+                        "-L" + os.path.join(ROOT, "leela_gb300"), "-lleela_gb300",
+                        "-Wl,-rpath," + os.path.join(ROOT, "leela_gb300"), "-o", exe], capture_output=True, text=True)
+    if r.returncode != 0:
+        return {"unavailable": r.stderr[-300:]}
+    out = {}
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES=os.environ.get("CUDA_VISIBLE_DEVICES", str(dev.index)))
+    for prec, threads, mode in runs:
+        p = subprocess.run([exe, str(threads), str(seconds), mode, prec, "64"], capture_output=True, text=True,
+                           timeout=120, env=env)
+        key = f"{prec}_{mode}_{threads}t"
+        try:
+            out[key] = json.loads(p.stdout.strip().splitlines()[-1])
+        except (IndexError, ValueError):
+            out[key] = {"error": (p.stderr or p.stdout)[-300:]}
+    return out
+
+
 def step_rate_device(lg, wp, wv, prec, d_p, d_v, dev, sp, steps=10):
     """The headline step (8192 positions through both nets in chained calls
     of 256, inputs resident) at another precision: positions/s."""
@@ -805,6 +839,7 @@ def secondary_measurements(lg, ctx, wp, wv, planes_p, planes_v, d_p, d_v, dev, s
     if not quick:
         out["serving_config3"] = serving_config3(lg, wp, wv, planes_p, planes_v, dev.index)
         out["distill"] = distill_rates(wp, wv, planes_p, planes_v, dev.index)
+        out["search_pattern"] = search_pattern_rates(dev)
     return out
 
 

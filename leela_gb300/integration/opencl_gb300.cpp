@@ -14,8 +14,12 @@
 //       of a net creates its context (lg_create) from them.
 //   OpenCL_Network::forward (OpenCL.cpp:490-569)
 //       without a callback (the value net, and the policy net's synchronous
-//       calls): lg_policy (head outputs) / lg_value (the FC output, no map:
+//       calls): a request to the batching server that the calling thread
+//       waits for, so that the value evaluations of all search threads are
+//       merged into GPU batches too (head outputs / the FC output, no map:
 //       the engine applies (1 + tanh) / 2 itself, Network.cpp:704-705);
+//       LEELA_GB300_SYNC=direct makes them blocking lg_policy / lg_value
+//       calls of one position instead;
 //       with a callback (Network::async_scored_moves, Network.cpp:536-587):
 //       lg_submit of the head outputs, and a drain thread per net runs the
 //       callback (forward_cb, Network.cpp:484-534: softmax, Netresult,
@@ -30,7 +34,8 @@
 //
 // Environment: LEELA_GB300_PRECISION = fp32 (default: the drop-in),
 // bf16, fp16 or fp8w for nets the tensor-core path covers;
-// LEELA_GB300_DEVICE (default 0); LEELA_GB300_MAX_BATCH (default 64).
+// LEELA_GB300_DEVICE (default 0); LEELA_GB300_MAX_BATCH (default 64);
+// LEELA_GB300_SYNC = server (default) or direct.
 #include <atomic>
 #include <chrono>
 #include <cstdio>
@@ -67,13 +72,23 @@ int env_precision() {
     throw std::runtime_error(std::string("LEELA_GB300_PRECISION: unknown precision ") + v);
 }
 
-// A request submitted with a callback: the engine's callback and its data,
-// and the input planes, which must live until the request completes.
+// A request to the batching server: the engine's callback and its data (or,
+// for a synchronous call, the flag its thread waits on), and the input
+// planes, which must live until the request completes.
 struct Pending {
     OpenCL_Network::event_callback cb;
     void *data;
     std::vector<uint8_t> planes;
+    std::atomic<int> *done = nullptr;
 };
+
+bool sync_direct() {
+    static const bool direct = [] {
+        const char *v = std::getenv("LEELA_GB300_SYNC");
+        return v && !std::strcmp(v, "direct");
+    }();
+    return direct;
+}
 
 // One context per engine net, created on the net's first forward, and the
 // thread that hands completed asynchronous requests back to the engine.
@@ -107,8 +122,12 @@ void drain_main(NetState *st) {
         }
         for (int i = 0; i < n; ++i) {
             Pending *pd = static_cast<Pending *>(tags[i]);
-            pd->cb(nullptr, CL_COMPLETE, pd->data);
-            delete pd;
+            if (pd->done) {
+                pd->done->store(1, std::memory_order_release);  // a synchronous call: its thread owns pd
+            } else {
+                pd->cb(nullptr, CL_COMPLETE, pd->data);
+                delete pd;
+            }
         }
     }
 }
@@ -190,7 +209,7 @@ void OpenCL_Network::forward(std::vector<float> &input, std::vector<float> &outp
                                 : lg_create(&d, nullptr, env_int("LEELA_GB300_DEVICE", 0),
                                             env_int("LEELA_GB300_MAX_BATCH", 64), &st.ctx);
         if (rc != LG_OK) throw std::runtime_error(std::string("leela_gb300: lg_create: ") + lg_last_error());
-        if (!st.value) st.drain = std::thread(drain_main, &st);
+        st.drain = std::thread(drain_main, &st);
     });
 
     opencl.ensure_thread_initialized();
@@ -209,7 +228,26 @@ void OpenCL_Network::forward(std::vector<float> &input, std::vector<float> &outp
         return;  // the drain thread runs cb
     }
     int rc;
-    if (st.value) {
+    if (!sync_direct()) {
+        // a request like the asynchronous ones; this thread waits for the
+        // drain thread.  The server completes every request it accepted (a
+        // failed batch too), so the wait ends; past a minute the process
+        // stops rather than free a request the server may still write.
+        std::atomic<int> done{0};
+        Pending pd{nullptr, nullptr, std::move(planes), &done};
+        rc = lg_submit(st.ctx, st.value ? LG_NET_VALUE : LG_NET_POLICY_LOGITS, pd.planes.data(), 1, 1.0f,
+                       output.data(), &pd);
+        if (rc == LG_OK) {
+            const auto t0 = std::chrono::steady_clock::now();
+            while (!done.load(std::memory_order_acquire)) {
+                std::this_thread::yield();
+                if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60)) {
+                    std::fprintf(stderr, "leela_gb300: a synchronous request did not complete within 60 s\n");
+                    std::abort();
+                }
+            }
+        }
+    } else if (st.value) {
         rc = lg_value(st.ctx, planes.data(), 1, output.data());
     } else {
         std::vector<float> probs(361);

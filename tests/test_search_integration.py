@@ -34,9 +34,11 @@ def driver():
     return os.path.join(d, "_build", "search_driver")
 
 
-def run(driver, playouts, threads):
+def run(driver, playouts, threads, sync=None):
     from oracle import oracle as O
     env = dict(os.environ)
+    if sync:
+        env["LEELA_GB300_SYNC"] = sync
     blas = O.find_openblas()
     if blas:
         env["LEELA_OPENBLAS"] = blas
@@ -55,10 +57,20 @@ def test_engine_search_runs_on_the_backend(driver):
     assert int(res["direct_moves"]) == 355
     assert 0.9 < float(res["direct_sum"]) <= 1.0 + 1e-5
     assert 0.0 <= float(res["value"]) <= 1.0  # the engine's (1 + tanh) / 2 of the raw FC output
-    assert int(res["submitted"]) > 0        # async_scored_moves went through lg_submit
-    assert int(res["sync"]) > 0             # value net, root AVERAGE_ALL
+    assert int(res["submitted"]) > 0        # async_scored_moves, and the synchronous calls too,
+    assert int(res["sync"]) == 0            # went through lg_submit (merged across threads)
     assert int(res["outstanding"]) == 0     # every callback ran; the join returned
     assert int(res["thread_outstanding"]) == 0
+
+
+def test_engine_search_with_direct_synchronous_calls(driver):
+    """LEELA_GB300_SYNC=direct: the value net and the root's synchronous
+    policy calls are blocking lg_value / lg_policy calls of one position."""
+    res = run(driver, 1000, 4, sync="direct")
+    assert res["legal"] == "1"
+    assert int(res["submitted"]) > 0        # the asynchronous policy requests
+    assert int(res["sync"]) > 0             # value net, root AVERAGE_ALL
+    assert int(res["outstanding"]) == 0 and int(res["thread_outstanding"]) == 0
 
 
 def test_engine_search_single_thread(driver):
